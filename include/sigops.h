@@ -1,0 +1,169 @@
+/*
+ * sigops.h -- C ABI of the GB300-native batch signature engine.
+ *
+ * Drop-in boundary for the batch signature path of wgpu_sig_ops
+ * (FuelLabs/wgpu-sigops): secp256k1 / secp256r1 ECDSA public-key recovery
+ * (`ecrecover`), ed25519 verification (`ecverify`) and the generator-table API
+ * `precompute::*_bases(log_limb_size)`.  Every entry point replaces the Rust
+ * function cited beside it (paths relative to the reference repository); the
+ * Rust-side binding a maintainer adds is shown in INTEGRATION.md.
+ *
+ * Conventions
+ *  - Plain pointers and sizes, caller-owned buffers, no exceptions across the
+ *    ABI.  Functions return SIGOPS_OK (0) or a negative SIGOPS_E_* code.
+ *  - Byte layouts are the reference's: signatures 64 bytes per item
+ *    (ECDSA: r || s big-endian with the recovery parity in bit 7 of byte 32,
+ *    fuel-crypto encoding; ed25519: R || S), messages 32 bytes (fuel
+ *    `Message`), ed25519 keys 32 bytes (compressed), recovered keys 64 bytes
+ *    (x || y big-endian, `PublicKey::as_slice()` / `to_sec1_bytes()[1..65]`).
+ *  - Per-item status codes (SIGOPS_ST_*) extend the reference, which reports
+ *    only a whole-batch `ShaderFailureError` (src/lib.rs:12-14): an item whose
+ *    status is not SIGOPS_ST_OK has a zeroed key (ECDSA) or `false` (ed25519);
+ *    the Rust wrapper maps it to an empty `Vec<u8>`, matching the CPU crates'
+ *    `Err` for that signature.
+ *  - A context owns one CUDA stream, the device-resident generator tables and
+ *    staging buffers.  Calls on one context are serialised internally; use
+ *    several contexts for concurrency.  `ctx == NULL` selects a process-wide
+ *    default context on device 0, created on first use.
+ *  - n == 0 returns SIGOPS_OK without touching the GPU (the reference returns
+ *    Ok(vec![]), src/secp256k1_ecdsa.rs:71-73).  There is no power-of-two
+ *    padding and no 2^22 cap (src/secp256k1_ecdsa.rs:22-44).
+ */
+#ifndef SIGOPS_H
+#define SIGOPS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* return codes */
+#define SIGOPS_OK 0
+#define SIGOPS_E_INVAL (-22)     /* bad argument (null pointer, unknown curve, bad log_limb_size, misaligned device pointer) */
+#define SIGOPS_E_NOMEM (-12)     /* device or pinned host allocation failed */
+#define SIGOPS_E_NODEV (-19)     /* no CUDA device / device index out of range */
+#define SIGOPS_E_CUDA (-5)       /* CUDA runtime error (see sigops_last_error) */
+#define SIGOPS_E_TABLE (-74)     /* table_limbs do not match precompute::*_bases(log_limb_size) */
+#define SIGOPS_E_TIMEDOUT (-110) /* a bounded device wait expired (the kernel returned instead of hanging) */
+#define SIGOPS_E_BUSY (-16)      /* serving queue full / admission refused */
+#define SIGOPS_E_RANGE (-34)     /* batch larger than the fixed capacity of an entry point */
+
+/* curves */
+#define SIGOPS_SECP256K1 0
+#define SIGOPS_SECP256R1 1
+#define SIGOPS_ED25519 2
+
+/* per-item status */
+#define SIGOPS_ST_OK 0         /* recovered / verified */
+#define SIGOPS_ST_BAD_SCALAR 1 /* ECDSA: r or s outside [1, n-1]; ed25519: S >= l (non-canonical) */
+#define SIGOPS_ST_NO_POINT 2   /* ECDSA: r is not the x-coordinate of a curve point; ed25519: key does not decompress */
+#define SIGOPS_ST_INFINITY 3   /* ECDSA: the recovered key is the point at infinity */
+#define SIGOPS_ST_MISMATCH 4   /* ed25519: [S]B - [k]A does not encode to R */
+
+typedef struct sigops_ctx sigops_ctx;
+
+/* ---------------------------------------------------------------- context */
+
+/* Create a context on `device`.  Builds and uploads the generator tables.
+ * Returns NULL on failure (sigops_last_error() says why). */
+sigops_ctx* sigops_create(int device);
+void sigops_destroy(sigops_ctx* ctx);
+/* Message for the last failure on this thread (never NULL). */
+const char* sigops_last_error(void);
+const char* sigops_strerror(int code);
+/* Library version string. */
+const char* sigops_version(void);
+
+/* ------------------------------------------------------- generator tables */
+
+/* Number of u32 limbs precompute::*_bases(log_limb_size) returns for `curve`
+ * (16 points x {2,3} coordinates x ceil(256/L) limbs), or SIGOPS_E_INVAL.
+ * log_limb_size must be in [11, 15], the range the reference's Montgomery
+ * shaders support (src/wgsl/mont.wgsl:12,37). */
+long sigops_bases_len(int curve, uint32_t log_limb_size);
+
+/* precompute::secp256k1_bases / secp256r1_bases / ed25519_bases
+ * (src/precompute.rs:36-69): writes the table, bit-identical to the reference,
+ * into out[0 .. cap) and returns its length (or a negative code).  CPU only;
+ * needs no GPU. */
+long sigops_bases(int curve, uint32_t log_limb_size, uint32_t* out, size_t cap);
+
+/* SIGOPS_OK if table_limbs equals precompute::*_bases(log_limb_size), else
+ * SIGOPS_E_TABLE (or SIGOPS_E_INVAL for a bad log_limb_size).  CPU only. */
+int sigops_check_table(int curve, const uint32_t* table_limbs, size_t table_len, uint32_t log_limb_size);
+
+/* --------------------------------------------- drop-in calls, host buffers */
+
+/* secp256k1_ecdsa::ecrecover (src/secp256k1_ecdsa.rs:61-213).
+ * sigs: n*64 bytes, msgs: n*32 bytes, out_pubkeys: n*64 bytes,
+ * out_status: n bytes (may be NULL).  table_limbs/table_len/log_limb_size are
+ * validated against precompute::secp256k1_bases (SIGOPS_E_TABLE on mismatch);
+ * the kernels use their own wider device-resident tables. */
+int sigops_secp256k1_ecrecover(sigops_ctx* ctx, const uint8_t* sigs, const uint8_t* msgs, size_t n, const uint32_t* table_limbs,
+                               size_t table_len, uint32_t log_limb_size, uint8_t* out_pubkeys, uint8_t* out_status);
+
+/* secp256k1_ecdsa::ecrecover_single_shader (src/secp256k1_ecdsa.rs:215-274). */
+int sigops_secp256k1_ecrecover_single_shader(sigops_ctx* ctx, const uint8_t* sigs, const uint8_t* msgs, size_t n,
+                                             uint32_t log_limb_size, uint8_t* out_pubkeys, uint8_t* out_status);
+
+/* secp256r1_ecdsa::ecrecover (src/secp256r1_ecdsa.rs; signatures are fuel
+ * Bytes64 with the same encoding). */
+int sigops_secp256r1_ecrecover(sigops_ctx* ctx, const uint8_t* sigs, const uint8_t* msgs, size_t n, const uint32_t* table_limbs,
+                               size_t table_len, uint32_t log_limb_size, uint8_t* out_pubkeys, uint8_t* out_status);
+
+/* secp256r1_ecdsa::ecrecover_single_shader (src/secp256r1_ecdsa.rs). */
+int sigops_secp256r1_ecrecover_single_shader(sigops_ctx* ctx, const uint8_t* sigs, const uint8_t* msgs, size_t n,
+                                             uint32_t log_limb_size, uint8_t* out_pubkeys, uint8_t* out_status);
+
+/* ed25519_eddsa::ecverify (src/ed25519_eddsa.rs:67-257).
+ * sigs: n*64 (R || S), msgs: n*32, pks: n*32 (VerifyingKey::to_bytes()),
+ * out_valid: n bytes of 0/1, out_status: n bytes (may be NULL). */
+int sigops_ed25519_ecverify(sigops_ctx* ctx, const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks, size_t n,
+                            const uint32_t* table_limbs, size_t table_len, uint32_t log_limb_size, uint8_t* out_valid,
+                            uint8_t* out_status);
+
+/* ed25519_eddsa::ecverify_single (src/ed25519_eddsa.rs:259-324). */
+int sigops_ed25519_ecverify_single(sigops_ctx* ctx, const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks, size_t n,
+                                   uint32_t log_limb_size, uint8_t* out_valid, uint8_t* out_status);
+
+/* ------------------------------------------ device-resident plain kernels */
+
+/* One plain (one signature per thread) kernel over device buffers on `stream`
+ * (a cudaStream_t; NULL = the context's stream).  No host synchronisation.
+ * Pointers must be 16-byte aligned.  ECDSA: d_out receives n*64 key bytes;
+ * ed25519: d_out receives n validity bytes and d_pks is required.
+ * Device-side failures (a bounded wait that expired) are reported by the next
+ * sigops_sync().  Equivalent of one reference dispatch
+ * (src/gpu.rs:88-104) without its per-call device creation. */
+int sigops_plain_device(sigops_ctx* ctx, int curve, const uint8_t* d_sigs, const uint8_t* d_msgs, const uint8_t* d_pks, size_t n,
+                        uint8_t* d_out, uint8_t* d_status, void* stream);
+
+/* Wait for the context's stream and report device-side errors since the last
+ * call (SIGOPS_E_TIMEDOUT if a bounded wait expired). */
+int sigops_sync(sigops_ctx* ctx);
+
+/* ------------------------------------------------------------ diagnostics */
+
+/* Measured 32-bit integer multiply-add throughput of this device (IMAD per
+ * second), from a dependency-free mad.lo probe timed with CUDA events. */
+int sigops_probe_imad(sigops_ctx* ctx, double* imad_per_second);
+
+/* Number of SMs and the plain kernels' grid (blocks) for `curve`. */
+int sigops_device_info(sigops_ctx* ctx, int* num_sms, int* plain_grid_k1, int* plain_grid_r1, int* plain_grid_ed);
+
+/* Arithmetic self-test hooks (run the kernels' field / hash code on the
+ * device): field 0..5 = secp256k1 p, P-256 p, 2^255-19, secp256k1 n,
+ * P-256 n, l; op 0 mul, 1 add, 2 sub, 3 inverse, 4 square-root candidate /
+ * (p-5)/8 power, 5 full 512-bit product.  a, b, out: host arrays of n 32-byte
+ * little-endian integers (out: 2n entries). */
+int sigops_test_field(sigops_ctx* ctx, int field, int op, const uint8_t* a, const uint8_t* b, uint8_t* out, size_t n);
+/* SHA-512 of n 96-byte inputs (R || A || M preimages); out n*64 bytes. */
+int sigops_test_sha512(sigops_ctx* ctx, const uint8_t* in, uint8_t* out, size_t n);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SIGOPS_H */

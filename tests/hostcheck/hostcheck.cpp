@@ -1,0 +1,98 @@
+// Host build of the kernels' arithmetic (field, curve, recovery, tables) for
+// the CPU test tier: the carry flag is emulated (arith.cuh), everything else is
+// the exact source the sm_103a kernels compile.  Test-only; never linked into
+// the library.
+#include <string.h>
+#include "../../wgpu-sigops_gb300/csrc/tables.cuh"
+
+using namespace sg;
+
+static uint32_t g_k1[ECDSA_GTAB * 16], g_r1[ECDSA_GTAB * 16], g_ed[ED_GTAB * 24];
+static bool g_init = false;
+
+static void init() {
+  if (g_init) return;
+  build_weier_gtab<K1Traits>(k1_gx(), k1_gy(), g_k1);
+  build_weier_gtab<R1Traits>(r1_gx(), r1_gy(), g_r1);
+  build_ed_btab(g_ed);
+  g_init = true;
+}
+
+static u256 load_le(const uint8_t* b) { u256 r; memcpy(r.w, b, 32); return r; }
+static void store_le(const u256& v, uint8_t* b) { memcpy(b, v.w, 32); }
+
+extern "C" {
+
+int hc_bases(int curve, uint32_t L, uint32_t* out) { return build_bases(curve, L, out); }
+
+void hc_gtab(int curve, uint32_t* out) {
+  init();
+  if (curve == 0) memcpy(out, g_k1, sizeof g_k1);
+  else if (curve == 1) memcpy(out, g_r1, sizeof g_r1);
+  else memcpy(out, g_ed, sizeof g_ed);
+}
+
+// field op test: field 0 k1-p, 1 r1-p, 2 ed-p, 3 k1-n, 4 r1-n, 5 ed-l ; op 0 mul, 1 add, 2 sub, 3 inv, 4 sqrt_candidate/pow_p58
+// integers little-endian; inputs < modulus
+void hc_field(int field, int op, const uint8_t* a, const uint8_t* b, uint8_t* out) {
+  u256 x = load_le(a), y = load_le(b), r = u256_zero();
+#define OPS(F)                                                        \
+  {                                                                   \
+    u256 xa = F::from_int(x), ya = F::from_int(y), ra;                \
+    if (op == 0) ra = F::mul(xa, ya);                                 \
+    else if (op == 1) ra = F::add(xa, ya);                            \
+    else if (op == 2) ra = F::sub(xa, ya);                            \
+    else ra = F::inv(xa);                                             \
+    r = F::to_int(ra);                                                \
+  }
+  switch (field) {
+    case 0: if (op == 4) r = FpK1::sqrt_candidate(FpK1::from_int(x)); else OPS(FpK1); break;
+    case 1: if (op == 4) r = FpR1::to_int(FpR1::sqrt_candidate(FpR1::from_int(x))); else OPS(FpR1); break;
+    case 2: if (op == 4) r = FpEd::pow_p58(FpEd::from_int(x)); else OPS(FpEd); break;
+    case 3: OPS(ScK1); break;
+    case 4: OPS(ScR1); break;
+    case 5: OPS(ScEd); break;
+  }
+#undef OPS
+  store_le(r, out);
+}
+
+void hc_mul_wide(const uint8_t* a, const uint8_t* b, uint8_t* out64) {
+  uint32_t t[16];
+  mul_wide(t, load_le(a), load_le(b));
+  memcpy(out64, t, 64);
+}
+
+int hc_k1_recover(const uint8_t* sig, const uint8_t* msg, uint8_t* out) {
+  init();
+  uint32_t s[16], m[8], o[16];
+  memcpy(s, sig, 64); memcpy(m, msg, 32);
+  int st = ecdsa_recover<K1Traits>(s, m, g_k1, o);
+  memcpy(out, o, 64);
+  return st;
+}
+
+int hc_r1_recover(const uint8_t* sig, const uint8_t* msg, uint8_t* out) {
+  init();
+  uint32_t s[16], m[8], o[16];
+  memcpy(s, sig, 64); memcpy(m, msg, 32);
+  int st = ecdsa_recover<R1Traits>(s, m, g_r1, o);
+  memcpy(out, o, 64);
+  return st;
+}
+
+int hc_ed_verify(const uint8_t* sig, const uint8_t* msg, const uint8_t* pk) {
+  init();
+  uint32_t s[16], m[8], p[8];
+  memcpy(s, sig, 64); memcpy(m, msg, 32); memcpy(p, pk, 32);
+  return ed25519_verify(s, m, p, g_ed);
+}
+
+void hc_sha512_96(const uint8_t* in, uint8_t* out) {
+  uint32_t m[24], h[16];
+  memcpy(m, in, 96);
+  sha512_96(m, h);
+  memcpy(out, h, 64);
+}
+
+}  // extern "C"

@@ -1,0 +1,141 @@
+"""Parity of the CUDA path with the oracle and the golden vectors, through the
+drop-in API (the calls a user of the reference makes).  Bit-exact."""
+import random
+
+import numpy as np
+import pytest
+
+from oracle import sigops_oracle as o
+from tests.golden_io import load
+
+pytestmark = pytest.mark.gpu
+G = load()
+L = 13
+
+
+@pytest.fixture(scope="module")
+def w():
+    import wgpu_sig_ops
+
+    return wgpu_sig_ops
+
+
+def test_k1_reference_kat(w):
+    """src/curve_algos/secp256k1_ecdsa.rs:206-214: the signature under secret key 1 recovers G."""
+    kat = G["secp256k1_kat"]
+    table = w.precompute.secp256k1_bases(L)
+    res = w.secp256k1_ecdsa.ecrecover([bytes.fromhex(kat["sig"])], [bytes.fromhex(kat["msg"])], table, L)
+    assert res[0].hex() == kat["pubkey"]
+    res = w.secp256k1_ecdsa.ecrecover_single_shader([bytes.fromhex(kat["sig"])], [bytes.fromhex(kat["msg"])], L)
+    assert res[0].hex() == kat["pubkey"]
+
+
+@pytest.mark.parametrize("curve", ["secp256k1", "secp256r1"])
+@pytest.mark.parametrize("single", [False, True])
+def test_ecdsa_golden(w, curve, single):
+    mod = getattr(w, curve + "_ecdsa")
+    vecs = G[curve] + G[curve + "_edge"]
+    sigs = [bytes.fromhex(v["sig"]) for v in vecs]
+    msgs = [bytes.fromhex(v["msg"]) for v in vecs]
+    if single:
+        res = mod.ecrecover_single_shader(sigs, msgs, L)
+    else:
+        res = mod.ecrecover(sigs, msgs, getattr(w.precompute, curve + "_bases")(L), L)
+    _, status = mod.ecrecover_arrays(sigs, msgs, None, L)
+    for v, r, st in zip(vecs, res, status):
+        assert r.hex() == v["pubkey"], v.get("case")
+        assert st == v["status"], v.get("case")
+
+
+@pytest.mark.parametrize("single", [False, True])
+def test_ed25519_golden(w, single):
+    vecs = G["ed25519"]
+    args = ([bytes.fromhex(v["sig"]) for v in vecs], [bytes.fromhex(v["msg"]) for v in vecs], [bytes.fromhex(v["pubkey"]) for v in vecs])
+    if single:
+        res = w.ed25519_eddsa.ecverify_single(*args, L)
+    else:
+        res = w.ed25519_eddsa.ecverify(*args, w.precompute.ed25519_bases(L), L)
+    valid, status = w.ed25519_eddsa.ecverify_arrays(*args)
+    for v, r, st in zip(vecs, res, status):
+        assert r == v["valid"] and st == v["status"], v["case"]
+
+
+def _ecdsa_batch(curve, n, seed, tamper_no_point=0.0):
+    rng = random.Random(seed)
+    sigs, msgs = [], []
+    for i in range(n):
+        d = rng.randrange(1, curve.n)
+        msg = rng.randbytes(32)
+        sig = o.ecdsa_sign_fuel(curve, d, msg, k=rng.randrange(1, curve.n))
+        if rng.random() < tamper_no_point:
+            while True:
+                x = rng.randrange(1, curve.n)
+                if pow((x**3 + curve.a * x + curve.b) % curve.p, (curve.p - 1) // 2, curve.p) == curve.p - 1:
+                    break
+            sig = x.to_bytes(32, "big") + sig[32:]
+        sigs.append(sig)
+        msgs.append(msg)
+    return sigs, msgs
+
+
+@pytest.mark.parametrize("curve_name", ["secp256k1", "secp256r1"])
+def test_ecdsa_random_batch_vs_oracle(w, curve_name):
+    c = o.SECP256K1 if curve_name == "secp256k1" else o.SECP256R1
+    sigs, msgs = _ecdsa_batch(c, 700, seed=11, tamper_no_point=0.05)
+    keys, status = getattr(w, curve_name + "_ecdsa").ecrecover_arrays(sigs, msgs, None, L)
+    for i in range(len(sigs)):
+        st, pk = o.ecdsa_recover(c, sigs[i], msgs[i])
+        assert status[i] == st
+        assert keys[i].tobytes() == (pk if pk else bytes(64))
+    assert (status == o.ST_NO_POINT).sum() > 10
+
+
+def test_ed25519_random_batch_vs_oracle(w):
+    rng = random.Random(12)
+    sigs, msgs, pks = [], [], []
+    for i in range(600):
+        seed = rng.randbytes(32)
+        msg = o.fuel_message(rng.randbytes(rng.randrange(0, 257)))
+        _, _, pk = o.ed25519_keypair(seed)
+        sig = o.ed25519_sign(seed, msg)
+        mode = rng.randrange(8)
+        if mode == 1:
+            b = rng.randrange(256)
+            sig = bytearray(sig)
+            sig[b // 8] ^= 1 << (b % 8)
+            sig = bytes(sig)
+        elif mode == 2:
+            msg = bytes([msg[0] ^ 1]) + msg[1:]
+        elif mode == 3:
+            sig = sig[:32] + (int.from_bytes(sig[32:], "little") + o.ED_L).to_bytes(32, "little")
+        elif mode == 4:
+            pk = rng.randbytes(32)
+        sigs.append(sig)
+        msgs.append(msg)
+        pks.append(pk)
+    valid, status = w.ed25519_eddsa.ecverify_arrays(sigs, msgs, pks)
+    for i in range(len(sigs)):
+        st, ok = o.ed25519_ecverify(sigs[i], msgs[i], pks[i])
+        assert (status[i], bool(valid[i])) == (st, ok), i
+
+
+def test_empty_and_errors(w):
+    t = w.precompute.secp256k1_bases(L)
+    assert w.secp256k1_ecdsa.ecrecover([], [], t, L) == []
+    assert w.ed25519_eddsa.ecverify([], [], [], w.precompute.ed25519_bases(L), L) == []
+    with pytest.raises(w.SigopsError):
+        w.secp256k1_ecdsa.ecrecover([bytes(64)], [bytes(32)], t[:-1], L)
+    with pytest.raises(w.SigopsError):
+        w.secp256r1_ecdsa.ecrecover([bytes(64)], [bytes(32)], t, L)  # k1 table for r1
+    with pytest.raises(ValueError):
+        w.secp256k1_ecdsa.ecrecover([bytes(64)], [], t, L)
+
+
+def test_ragged_sizes(w):
+    """Sizes that are not multiples of the block or of a power of two."""
+    c = o.SECP256K1
+    sigs, msgs = _ecdsa_batch(c, 257, seed=3)
+    for n in (1, 2, 31, 33, 255, 257):
+        res = w.secp256k1_ecdsa.ecrecover_single_shader(sigs[:n], msgs[:n], L)
+        assert res[-1] == o.ecdsa_recover(c, sigs[n - 1], msgs[n - 1])[1]
+        assert res[0] == o.ecdsa_recover(c, sigs[0], msgs[0])[1]

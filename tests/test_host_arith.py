@@ -1,0 +1,139 @@
+"""The kernels' arithmetic compiled for the host (carry flag emulated), checked
+against Python integers, the oracle and the golden vectors.  CPU only."""
+import ctypes
+import random
+
+import pytest
+
+from oracle import sigops_oracle as o
+from tests._paths import build_hostcheck
+from tests.golden_io import load
+
+G = load()
+
+
+@pytest.fixture(scope="module")
+def hc():
+    return ctypes.CDLL(build_hostcheck())
+
+
+def le(v):
+    return v.to_bytes(32, "little")
+
+
+MODS = [o.SECP256K1.p, o.SECP256R1.p, o.ED_P, o.SECP256K1.n, o.SECP256R1.n, o.ED_L]
+
+
+def expected(field, op, a, b):
+    m = MODS[field]
+    if op == 0:
+        return a * b % m
+    if op == 1:
+        return (a + b) % m
+    if op == 2:
+        return (a - b) % m
+    if op == 3:
+        return pow(a, m - 2, m)
+    return pow(a, (m + 1) // 4, m) if field < 2 else pow(a, (m - 5) // 8, m)
+
+
+def test_mul_wide(hc):
+    rng = random.Random(5)
+    cases = [(2**256 - 1, 2**256 - 1), (0, 5), (2**255, 2)] + [(rng.getrandbits(256), rng.getrandbits(256)) for _ in range(300)]
+    for a, b in cases:
+        out = ctypes.create_string_buffer(64)
+        hc.hc_mul_wide(le(a), le(b), out)
+        assert int.from_bytes(out.raw, "little") == a * b
+
+
+@pytest.mark.parametrize("field", range(6))
+@pytest.mark.parametrize("op", range(5))
+def test_field_ops(hc, field, op):
+    if op == 4 and field > 2:
+        pytest.skip("no root / p58 power in scalar fields")
+    m = MODS[field]
+    rng = random.Random(field * 10 + op)
+    cases = [(m - 1, m - 1), (0, m - 1), (1, 1), (m - 1, 1)] + [(rng.randrange(m), rng.randrange(m)) for _ in range(60)]
+    for a, b in cases:
+        out = ctypes.create_string_buffer(32)
+        hc.hc_field(field, op, le(a), le(b), out)
+        assert int.from_bytes(out.raw, "little") == expected(field, op, a, b), (field, op, hex(a), hex(b))
+
+
+def test_sha512(hc):
+    for v in G["sha512_96"]:
+        out = ctypes.create_string_buffer(64)
+        hc.hc_sha512_96(bytes.fromhex(v["in"]), out)
+        assert out.raw.hex() == v["out"]
+
+
+@pytest.mark.parametrize("curve", ["secp256k1", "secp256r1"])
+def test_ecdsa_golden(hc, curve):
+    fn = hc.hc_k1_recover if curve == "secp256k1" else hc.hc_r1_recover
+    for v in G[curve] + G[curve + "_edge"]:
+        out = ctypes.create_string_buffer(64)
+        st = fn(bytes.fromhex(v["sig"]), bytes.fromhex(v["msg"]), out)
+        want = bytes.fromhex(v["pubkey"]) if v["pubkey"] else bytes(64)
+        assert (st, out.raw) == (v["status"], want), v.get("case")
+
+
+def test_k1_kat(hc):
+    kat = G["secp256k1_kat"]
+    out = ctypes.create_string_buffer(64)
+    assert hc.hc_k1_recover(bytes.fromhex(kat["sig"]), bytes.fromhex(kat["msg"]), out) == 0
+    assert out.raw.hex() == kat["pubkey"]
+
+
+def test_ed25519_golden(hc):
+    for v in G["ed25519"]:
+        st = hc.hc_ed_verify(bytes.fromhex(v["sig"]), bytes.fromhex(v["msg"]), bytes.fromhex(v["pubkey"]))
+        assert st == v["status"], v["case"]
+
+
+def test_random_vs_oracle(hc):
+    rng = random.Random(77)
+    for i in range(12):
+        d = rng.randrange(1, o.SECP256R1.n)
+        msg = rng.randbytes(32)
+        for c, fn in ((o.SECP256K1, hc.hc_k1_recover), (o.SECP256R1, hc.hc_r1_recover)):
+            sig = o.ecdsa_sign_fuel(c, d % c.n or 1, msg)
+            out = ctypes.create_string_buffer(64)
+            st = fn(sig, msg, out)
+            assert (st, out.raw) == (0, o.ws_public_key(c, d % c.n or 1))
+        seed = rng.randbytes(32)
+        _, _, pk = o.ed25519_keypair(seed)
+        sig = o.ed25519_sign(seed, msg)
+        assert hc.hc_ed_verify(sig, msg, pk) == 0
+
+
+def test_kernel_tables(hc):
+    """The device tables hold (i+1)*G for i < 64 (affine; P-256 in Montgomery form)."""
+    R = 2**256
+    for curve, c in ((0, o.SECP256K1), (1, o.SECP256R1)):
+        buf = (ctypes.c_uint32 * (64 * 16))()
+        hc.hc_gtab(curve, buf)
+        words = list(buf)
+        for i in (0, 1, 15, 63):
+            x = sum(words[i * 16 + k] << (32 * k) for k in range(8))
+            y = sum(words[i * 16 + 8 + k] << (32 * k) for k in range(8))
+            if curve == 1:
+                rinv = pow(R, -1, c.p)
+                x, y = x * rinv % c.p, y * rinv % c.p
+            assert (x, y) == o.ws_mul(c, i + 1, c.g)
+    buf = (ctypes.c_uint32 * (64 * 24))()
+    hc.hc_gtab(2, buf)
+    words = list(buf)
+    for i in (0, 7, 63):
+        x, y = o.ed_mul(i + 1, o.ED_B)
+        ypx = sum(words[i * 24 + k] << (32 * k) for k in range(8))
+        assert ypx == (x + y) % o.ED_P
+
+
+@pytest.mark.parametrize("curve", [0, 1, 2])
+def test_bases_bit_identical(hc, curve):
+    fn = [o.secp256k1_bases, o.secp256r1_bases, o.ed25519_bases][curve]
+    for L in range(11, 16):
+        exp = fn(L)
+        buf = (ctypes.c_uint32 * len(exp))()
+        assert hc.hc_bases(curve, L, buf) == len(exp)
+        assert list(buf) == exp

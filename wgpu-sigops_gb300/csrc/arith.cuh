@@ -1,0 +1,161 @@
+// 32-bit limb carry-chain primitives for sm_103a.
+//
+// Each primitive is one PTX instruction (add.cc / addc / mad.lo.cc / madc.hi
+// ...), issued as its own `asm volatile` statement so that chains keep their
+// program order; the PTX carry flag (CC.CF) links consecutive primitives.
+// These replace the reference's 13-bit-limb WGSL bigint layer
+// (src/wgsl/bigint.wgsl:1-246), whose u32-only arithmetic had no wide
+// multiply and no carry flag.
+//
+// When compiled for the host (test builds only, never in libsigops.so's host
+// code path) the carry flag is emulated with a thread-local word so that the
+// device arithmetic can be checked against the oracle without a GPU.
+#pragma once
+#include <stdint.h>
+
+#if defined(__CUDACC__)
+#define SG_HD __host__ __device__ __forceinline__
+#define SG_DEV __device__ __forceinline__
+#else
+#define SG_HD inline
+#define SG_DEV inline
+#endif
+
+namespace sg {
+
+#if defined(__CUDA_ARCH__)
+
+SG_DEV uint32_t add_cc(uint32_t a, uint32_t b) { uint32_t r; asm volatile("add.cc.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(b)); return r; }
+SG_DEV uint32_t addc_cc(uint32_t a, uint32_t b) { uint32_t r; asm volatile("addc.cc.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(b)); return r; }
+SG_DEV uint32_t addc(uint32_t a, uint32_t b) { uint32_t r; asm volatile("addc.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(b)); return r; }
+SG_DEV uint32_t sub_cc(uint32_t a, uint32_t b) { uint32_t r; asm volatile("sub.cc.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(b)); return r; }
+SG_DEV uint32_t subc_cc(uint32_t a, uint32_t b) { uint32_t r; asm volatile("subc.cc.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(b)); return r; }
+SG_DEV uint32_t subc(uint32_t a, uint32_t b) { uint32_t r; asm volatile("subc.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(b)); return r; }
+SG_DEV uint32_t mad_lo_cc(uint32_t a, uint32_t b, uint32_t c) { uint32_t r; asm volatile("mad.lo.cc.u32 %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(b), "r"(c)); return r; }
+SG_DEV uint32_t madc_lo_cc(uint32_t a, uint32_t b, uint32_t c) { uint32_t r; asm volatile("madc.lo.cc.u32 %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(b), "r"(c)); return r; }
+SG_DEV uint32_t madc_lo(uint32_t a, uint32_t b, uint32_t c) { uint32_t r; asm volatile("madc.lo.u32 %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(b), "r"(c)); return r; }
+SG_DEV uint32_t mad_hi_cc(uint32_t a, uint32_t b, uint32_t c) { uint32_t r; asm volatile("mad.hi.cc.u32 %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(b), "r"(c)); return r; }
+SG_DEV uint32_t madc_hi_cc(uint32_t a, uint32_t b, uint32_t c) { uint32_t r; asm volatile("madc.hi.cc.u32 %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(b), "r"(c)); return r; }
+SG_DEV uint32_t madc_hi(uint32_t a, uint32_t b, uint32_t c) { uint32_t r; asm volatile("madc.hi.u32 %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(b), "r"(c)); return r; }
+SG_DEV uint32_t mul_lo(uint32_t a, uint32_t b) { return a * b; }
+SG_DEV uint32_t mul_hi(uint32_t a, uint32_t b) { return __umulhi(a, b); }
+
+#else  // host emulation (test builds)
+
+inline uint32_t& cf_() { static thread_local uint32_t cf = 0; return cf; }
+inline uint32_t add_cc(uint32_t a, uint32_t b) { uint64_t s = (uint64_t)a + b; cf_() = (uint32_t)(s >> 32); return (uint32_t)s; }
+inline uint32_t addc_cc(uint32_t a, uint32_t b) { uint64_t s = (uint64_t)a + b + cf_(); cf_() = (uint32_t)(s >> 32); return (uint32_t)s; }
+inline uint32_t addc(uint32_t a, uint32_t b) { return a + b + cf_(); }
+inline uint32_t sub_cc(uint32_t a, uint32_t b) { uint64_t d = (uint64_t)a - b; cf_() = (uint32_t)(d >> 63); return (uint32_t)d; }
+inline uint32_t subc_cc(uint32_t a, uint32_t b) { uint64_t d = (uint64_t)a - b - cf_(); cf_() = (uint32_t)(d >> 63); return (uint32_t)d; }
+inline uint32_t subc(uint32_t a, uint32_t b) { return a - b - cf_(); }
+inline uint32_t mad_lo_cc(uint32_t a, uint32_t b, uint32_t c) { uint64_t s = (uint64_t)(uint32_t)(a * b) + c; cf_() = (uint32_t)(s >> 32); return (uint32_t)s; }
+inline uint32_t madc_lo_cc(uint32_t a, uint32_t b, uint32_t c) { uint64_t s = (uint64_t)(uint32_t)(a * b) + c + cf_(); cf_() = (uint32_t)(s >> 32); return (uint32_t)s; }
+inline uint32_t madc_lo(uint32_t a, uint32_t b, uint32_t c) { return (uint32_t)(a * b) + c + cf_(); }
+inline uint32_t mad_hi_cc(uint32_t a, uint32_t b, uint32_t c) { uint64_t s = (((uint64_t)a * b) >> 32) + c; cf_() = (uint32_t)(s >> 32); return (uint32_t)s; }
+inline uint32_t madc_hi_cc(uint32_t a, uint32_t b, uint32_t c) { uint64_t s = (((uint64_t)a * b) >> 32) + c + cf_(); cf_() = (uint32_t)(s >> 32); return (uint32_t)s; }
+inline uint32_t madc_hi(uint32_t a, uint32_t b, uint32_t c) { return (uint32_t)(((uint64_t)a * b) >> 32) + c + cf_(); }
+inline uint32_t mul_lo(uint32_t a, uint32_t b) { return a * b; }
+inline uint32_t mul_hi(uint32_t a, uint32_t b) { return (uint32_t)(((uint64_t)a * b) >> 32); }
+
+#endif
+
+// 256-bit unsigned integer, little-endian 32-bit limbs.
+struct u256 {
+  uint32_t w[8];
+};
+
+SG_HD u256 u256_zero() { u256 r; for (int i = 0; i < 8; ++i) r.w[i] = 0; return r; }
+SG_HD u256 u256_small(uint32_t v) { u256 r = u256_zero(); r.w[0] = v; return r; }
+
+SG_HD bool u256_is_zero(const u256& a) {
+  uint32_t acc = 0;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) acc |= a.w[i];
+  return acc == 0;
+}
+
+SG_HD bool u256_eq(const u256& a, const u256& b) {
+  uint32_t acc = 0;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) acc |= a.w[i] ^ b.w[i];
+  return acc == 0;
+}
+
+// r = a + b, returns the carry out (0/1)
+SG_HD uint32_t u256_add(u256& r, const u256& a, const u256& b) {
+  r.w[0] = add_cc(a.w[0], b.w[0]);
+#pragma unroll
+  for (int i = 1; i < 8; ++i) r.w[i] = addc_cc(a.w[i], b.w[i]);
+  return addc(0u, 0u);
+}
+
+// r = a - b, returns the borrow out (0/1)
+SG_HD uint32_t u256_sub(u256& r, const u256& a, const u256& b) {
+  r.w[0] = sub_cc(a.w[0], b.w[0]);
+#pragma unroll
+  for (int i = 1; i < 8; ++i) r.w[i] = subc_cc(a.w[i], b.w[i]);
+  return subc(0u, 0u) & 1u;
+}
+
+// a >= b
+SG_HD bool u256_gte(const u256& a, const u256& b) {
+  u256 t;
+  return u256_sub(t, a, b) == 0;
+}
+
+SG_HD u256 u256_select(bool c, const u256& a, const u256& b) {  // c ? a : b
+  u256 r;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) r.w[i] = c ? a.w[i] : b.w[i];
+  return r;
+}
+
+// 512-bit product r[0..15] = a * b.
+// Row i adds b_i * a into two accumulators: `e` collects the products with even
+// a-limbs (lo at column i+j, hi at i+j+1 for j even -- a contiguous 256-bit
+// run), `o` those with odd a-limbs (a run starting at column i+1).  Each row is
+// therefore one unbroken carry chain; the two are summed at the end.
+SG_HD void mul_wide(uint32_t r[16], const u256& a, const u256& b) {
+  uint32_t e[16], o[17];
+  // row 0: plain products, no carries (e: columns 0..7, o: columns 1..8)
+#pragma unroll
+  for (int j = 0; j < 8; j += 2) {
+    e[j] = mul_lo(a.w[j], b.w[0]);
+    e[j + 1] = mul_hi(a.w[j], b.w[0]);
+    o[j + 1] = mul_lo(a.w[j + 1], b.w[0]);
+    o[j + 2] = mul_hi(a.w[j + 1], b.w[0]);
+  }
+  e[8] = 0;
+  o[9] = 0;
+#pragma unroll
+  for (int i = 1; i < 8; ++i) {
+    const uint32_t bi = b.w[i];
+    // even chain over columns i .. i+7; column i+7 holds the previous row's
+    // carry and the carry out lands in the fresh column i+8
+    e[i] = mad_lo_cc(a.w[0], bi, e[i]);
+    e[i + 1] = madc_hi_cc(a.w[0], bi, e[i + 1]);
+#pragma unroll
+    for (int j = 2; j < 8; j += 2) {
+      e[i + j] = madc_lo_cc(a.w[j], bi, e[i + j]);
+      e[i + j + 1] = madc_hi_cc(a.w[j], bi, e[i + j + 1]);
+    }
+    e[i + 8] = addc(0u, 0u);
+    // odd chain over columns i+1 .. i+8, carry out into the fresh column i+9
+    o[i + 1] = mad_lo_cc(a.w[1], bi, o[i + 1]);
+    o[i + 2] = madc_hi_cc(a.w[1], bi, o[i + 2]);
+#pragma unroll
+    for (int j = 3; j < 8; j += 2) {
+      o[i + j] = madc_lo_cc(a.w[j], bi, o[i + j]);
+      o[i + j + 1] = madc_hi_cc(a.w[j], bi, o[i + j + 1]);
+    }
+    o[i + 9] = addc(0u, 0u);  // o[16] is always 0: the full product fits 512 bits
+  }
+  // r = e + (o << 32)
+  r[0] = e[0];
+  r[1] = add_cc(e[1], o[1]);
+#pragma unroll
+  for (int k = 2; k < 16; ++k) r[k] = addc_cc(e[k], o[k]);
+}
+
+}  // namespace sg

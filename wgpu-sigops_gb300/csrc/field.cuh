@@ -1,0 +1,460 @@
+// Prime fields for the three curves, 8 x 32-bit limbs, values kept canonical
+// (in [0, p)) after every operation.
+//
+//  * FpK1  p = 2^256 - 2^32 - 977   special-form fold (2^256 = 2^32 + 977)
+//  * FpEd  p = 2^255 - 19           special-form fold (2^256 = 38)
+//  * FpR1  p = NIST P-256           Montgomery form, R = 2^256 (n0' = 1)
+//  * Mont<...> generic Montgomery (CIOS) for the scalar fields mod n and mod l
+//
+// The reference does all of this with 13-bit limbs: Barrett `ff_mul`
+// (src/wgsl/ff.wgsl:122-198), CIOS `mont_mul` (src/wgsl/mont.wgsl:5-78),
+// square-and-multiply `modpow` (src/wgsl/mont.wgsl:80-99), binary-EEA
+// `ff_inverse` (src/wgsl/ff.wgsl:60-120) and the (p+1)/4 square root
+// (src/wgsl/secp256k1_curve.wgsl:12-21).  Here exponentiations use fixed
+// addition chains (255 squarings and 11-15 multiplications each) and the
+// scalar inverse uses Fermat with a 4-bit window, so no input can make a loop
+// run away (the reference's binary EEA never terminates for 0).
+#pragma once
+#include "arith.cuh"
+
+namespace sg {
+
+#define SG_U256(a0, a1, a2, a3, a4, a5, a6, a7) \
+  u256 { { a0, a1, a2, a3, a4, a5, a6, a7 } }
+
+// ---------------------------------------------------------------------------
+// shared helpers
+// ---------------------------------------------------------------------------
+
+// r = (a + b) mod m for a, b < m
+SG_HD u256 mod_add(const u256& a, const u256& b, const u256& m) {
+  u256 t, u;
+  uint32_t c = u256_add(t, a, b);
+  uint32_t bw = u256_sub(u, t, m);
+  return u256_select(c | (bw ^ 1u), u, t);
+}
+
+// r = (a - b) mod m for a, b < m
+SG_HD u256 mod_sub(const u256& a, const u256& b, const u256& m) {
+  u256 t, u;
+  uint32_t bw = u256_sub(t, a, b);
+  u256_add(u, t, m);
+  return u256_select(bw != 0, u, t);
+}
+
+SG_HD u256 mod_neg(const u256& a, const u256& m) {
+  u256 t;
+  u256_sub(t, m, a);
+  return u256_select(u256_is_zero(a), a, t);
+}
+
+// reduce x < 2^256 into [0, m) when m > 2^255 (at most one subtraction)
+SG_HD u256 reduce_once(const u256& x, const u256& m) {
+  u256 t;
+  uint32_t bw = u256_sub(t, x, m);
+  return u256_select(bw == 0, t, x);
+}
+
+// ---------------------------------------------------------------------------
+// secp256k1 base field
+// ---------------------------------------------------------------------------
+struct FpK1 {
+  SG_HD static u256 P() { return SG_U256(0xfffffc2fu, 0xfffffffeu, 0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu); }
+
+  // t = H * 2^256 + L  ==  L + H * 977 + H * 2^32  (mod p)
+  SG_HD static u256 reduce(const uint32_t t[16]) {
+    uint32_t v[10];
+    // v = L + lo(H_j * 977) at column j
+    v[0] = mad_lo_cc(t[8], 977u, t[0]);
+#pragma unroll
+    for (int j = 1; j < 8; ++j) v[j] = madc_lo_cc(t[8 + j], 977u, t[j]);
+    v[8] = addc(0u, 0u);
+    // + hi(H_j * 977) at column j+1
+    v[1] = mad_hi_cc(t[8], 977u, v[1]);
+#pragma unroll
+    for (int j = 1; j < 7; ++j) v[j + 1] = madc_hi_cc(t[8 + j], 977u, v[j + 1]);
+    v[8] = madc_hi(t[15], 977u, v[8]);  // < 2^32: hi(.) < 977 and v[8] <= 1
+    // + H_j at column j+1
+    v[1] = add_cc(v[1], t[8]);
+#pragma unroll
+    for (int j = 1; j < 8; ++j) v[j + 1] = addc_cc(v[j + 1], t[8 + j]);
+    v[9] = addc(0u, 0u);
+    // second fold of the top 33 bits: top = v[8] + v[9] * 2^32 (v[9] <= 1)
+    // top * (2^32 + 977) = v8*977 + (v8 + v9*977) * 2^32 + v9 * 2^64
+    u256 r;
+    r.w[0] = mad_lo_cc(v[8], 977u, v[0]);
+    r.w[1] = madc_hi_cc(v[8], 977u, v[1]);
+    r.w[2] = addc_cc(v[2], v[9]);
+#pragma unroll
+    for (int j = 3; j < 8; ++j) r.w[j] = addc_cc(v[j], 0u);
+    uint32_t c1 = addc(0u, 0u);
+    r.w[1] = add_cc(r.w[1], v[8]);
+#pragma unroll
+    for (int j = 2; j < 8; ++j) r.w[j] = addc_cc(r.w[j], 0u);
+    uint32_t c2 = addc(c1, 0u);
+    uint32_t v9m = v[9] * 977u;
+    r.w[1] = add_cc(r.w[1], v9m);
+#pragma unroll
+    for (int j = 2; j < 8; ++j) r.w[j] = addc_cc(r.w[j], 0u);
+    uint32_t c3 = addc(c2, 0u);
+    // c3 <= 1; when set the low 256 bits are tiny, so adding c once cannot carry
+    uint32_t cm = c3 * 977u;
+    r.w[0] = add_cc(r.w[0], cm);
+    r.w[1] = addc_cc(r.w[1], c3);
+#pragma unroll
+    for (int j = 2; j < 8; ++j) r.w[j] = addc_cc(r.w[j], 0u);
+    (void)addc(0u, 0u);
+    return reduce_once(r, P());
+  }
+
+  SG_HD static u256 mul(const u256& a, const u256& b) { uint32_t t[16]; mul_wide(t, a, b); return reduce(t); }
+  SG_HD static u256 sqr(const u256& a) { uint32_t t[16]; mul_wide(t, a, a); return reduce(t); }
+  SG_HD static u256 add(const u256& a, const u256& b) { return mod_add(a, b, P()); }
+  SG_HD static u256 sub(const u256& a, const u256& b) { return mod_sub(a, b, P()); }
+  SG_HD static u256 neg(const u256& a) { return mod_neg(a, P()); }
+  SG_HD static u256 one() { return u256_small(1); }
+  SG_HD static u256 zero() { return u256_zero(); }
+  SG_HD static u256 from_int(const u256& x) { return reduce_once(x, P()); }  // x < 2^256
+  SG_HD static u256 to_int(const u256& a) { return a; }
+  SG_HD static u256 mul_small(const u256& a, uint32_t k) {  // k < 2^32
+    uint32_t t[16];
+    t[0] = mul_lo(a.w[0], k);
+    t[1] = mad_hi_cc(a.w[0], k, mul_lo(a.w[1], k));
+    // build the 9-limb product, then fold through the generic reducer
+    uint32_t lo[8], hi[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) { lo[j] = mul_lo(a.w[j], k); hi[j] = mul_hi(a.w[j], k); }
+    t[0] = lo[0];
+    t[1] = add_cc(lo[1], hi[0]);
+#pragma unroll
+    for (int j = 2; j < 8; ++j) t[j] = addc_cc(lo[j], hi[j - 1]);
+    t[8] = addc(hi[7], 0u);
+#pragma unroll
+    for (int j = 9; j < 16; ++j) t[j] = 0;
+    return reduce(t);
+  }
+
+  SG_HD static u256 sqr_n(u256 a, int n) {
+#pragma unroll 1
+    for (int i = 0; i < n; ++i) a = sqr(a);
+    return a;
+  }
+
+  // x2 .. x223: a^(2^k - 1) blocks shared by the inverse and the square root
+  SG_HD static void blocks(const u256& a, u256& x2, u256& x22, u256& x223) {
+    x2 = mul(sqr(a), a);
+    u256 x3 = mul(sqr(x2), a);
+    u256 x6 = mul(sqr_n(x3, 3), x3);
+    u256 x9 = mul(sqr_n(x6, 3), x3);
+    u256 x11 = mul(sqr_n(x9, 2), x2);
+    x22 = mul(sqr_n(x11, 11), x11);
+    u256 x44 = mul(sqr_n(x22, 22), x22);
+    u256 x88 = mul(sqr_n(x44, 44), x44);
+    u256 x176 = mul(sqr_n(x88, 88), x88);
+    u256 x220 = mul(sqr_n(x176, 44), x44);
+    x223 = mul(sqr_n(x220, 3), x3);
+  }
+
+  // a^(p-2): 255 squarings, 15 multiplications
+  SG_HD static u256 inv(const u256& a) {
+    u256 x2, x22, t;
+    blocks(a, x2, x22, t);
+    t = mul(sqr_n(t, 23), x22);
+    t = mul(sqr_n(t, 5), a);
+    t = mul(sqr_n(t, 3), x2);
+    t = mul(sqr_n(t, 2), a);
+    return t;
+  }
+
+  // a^((p+1)/4): 253 squarings, 13 multiplications
+  SG_HD static u256 sqrt_candidate(const u256& a) {
+    u256 x2, x22, t;
+    blocks(a, x2, x22, t);
+    t = mul(sqr_n(t, 23), x22);
+    t = mul(sqr_n(t, 6), x2);
+    t = sqr_n(t, 2);
+    return t;
+  }
+};
+
+// ---------------------------------------------------------------------------
+// ed25519 base field
+// ---------------------------------------------------------------------------
+struct FpEd {
+  SG_HD static u256 P() { return SG_U256(0xffffffedu, 0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu, 0x7fffffffu); }
+
+  // x < 2^256  ->  x mod p  (2^255 = 19)
+  SG_HD static u256 canon(u256 x) {
+    uint32_t top = x.w[7] >> 31;
+    x.w[7] &= 0x7fffffffu;
+    x.w[0] = add_cc(x.w[0], top * 19u);
+#pragma unroll
+    for (int j = 1; j < 8; ++j) x.w[j] = addc_cc(x.w[j], 0u);
+    // now x < 2^255 + 19; subtract p when x + 19 >= 2^255
+    u256 y;
+    y.w[0] = add_cc(x.w[0], 19u);
+#pragma unroll
+    for (int j = 1; j < 8; ++j) y.w[j] = addc_cc(x.w[j], 0u);
+    bool ge = (y.w[7] >> 31) != 0;
+    y.w[7] &= 0x7fffffffu;
+    return u256_select(ge, y, x);
+  }
+
+  // t = H * 2^256 + L  ==  L + 38 H  (mod p)
+  SG_HD static u256 reduce(const uint32_t t[16]) {
+    uint32_t v[9];
+    v[0] = mad_lo_cc(t[8], 38u, t[0]);
+#pragma unroll
+    for (int j = 1; j < 8; ++j) v[j] = madc_lo_cc(t[8 + j], 38u, t[j]);
+    v[8] = addc(0u, 0u);
+    v[1] = mad_hi_cc(t[8], 38u, v[1]);
+#pragma unroll
+    for (int j = 1; j < 7; ++j) v[j + 1] = madc_hi_cc(t[8 + j], 38u, v[j + 1]);
+    v[8] = madc_hi(t[15], 38u, v[8]);  // v[8] <= 38
+    u256 r;
+    r.w[0] = mad_lo_cc(v[8], 38u, v[0]);
+#pragma unroll
+    for (int j = 1; j < 8; ++j) r.w[j] = addc_cc(v[j], 0u);
+    uint32_t c = addc(0u, 0u);
+    r.w[0] = add_cc(r.w[0], c * 38u);
+#pragma unroll
+    for (int j = 1; j < 8; ++j) r.w[j] = addc_cc(r.w[j], 0u);
+    (void)addc(0u, 0u);
+    return canon(r);
+  }
+
+  SG_HD static u256 mul(const u256& a, const u256& b) { uint32_t t[16]; mul_wide(t, a, b); return reduce(t); }
+  SG_HD static u256 sqr(const u256& a) { uint32_t t[16]; mul_wide(t, a, a); return reduce(t); }
+  SG_HD static u256 add(const u256& a, const u256& b) { return mod_add(a, b, P()); }
+  SG_HD static u256 sub(const u256& a, const u256& b) { return mod_sub(a, b, P()); }
+  SG_HD static u256 neg(const u256& a) { return mod_neg(a, P()); }
+  SG_HD static u256 one() { return u256_small(1); }
+  SG_HD static u256 zero() { return u256_zero(); }
+  SG_HD static u256 from_int(const u256& x) { return canon(x); }
+  SG_HD static u256 to_int(const u256& a) { return a; }
+  SG_HD static u256 D() { return SG_U256(0x135978a3u, 0x75eb4dcau, 0x4141d8abu, 0x00700a4du, 0x7779e898u, 0x8cc74079u, 0x2b6ffe73u, 0x52036ceeu); }
+  SG_HD static u256 D2() { return SG_U256(0x26b2f159u, 0xebd69b94u, 0x8283b156u, 0x00e0149au, 0xeef3d130u, 0x198e80f2u, 0x56dffce7u, 0x2406d9dcu); }
+  SG_HD static u256 SQRT_M1() { return SG_U256(0x4a0ea0b0u, 0xc4ee1b27u, 0xad2fe478u, 0x2f431806u, 0x3dfbd7a7u, 0x2b4d0099u, 0x4fc1df0bu, 0x2b832480u); }
+
+  SG_HD static u256 sqr_n(u256 a, int n) {
+#pragma unroll 1
+    for (int i = 0; i < n; ++i) a = sqr(a);
+    return a;
+  }
+
+  // z^(2^250 - 1) and z^11 (the shared prefix of the inverse and the p58 power)
+  SG_HD static void pow250(const u256& z, u256& z2_250_0, u256& z11) {
+    u256 z2 = sqr(z);
+    u256 z9 = mul(sqr_n(z2, 2), z);
+    z11 = mul(z9, z2);
+    u256 z2_5_0 = mul(sqr(z11), z9);
+    u256 z2_10_0 = mul(sqr_n(z2_5_0, 5), z2_5_0);
+    u256 z2_20_0 = mul(sqr_n(z2_10_0, 10), z2_10_0);
+    u256 z2_40_0 = mul(sqr_n(z2_20_0, 20), z2_20_0);
+    u256 z2_50_0 = mul(sqr_n(z2_40_0, 10), z2_10_0);
+    u256 z2_100_0 = mul(sqr_n(z2_50_0, 50), z2_50_0);
+    u256 z2_200_0 = mul(sqr_n(z2_100_0, 100), z2_100_0);
+    z2_250_0 = mul(sqr_n(z2_200_0, 50), z2_50_0);
+  }
+
+  // z^(p-2) = z^(2^255 - 21)
+  SG_HD static u256 inv(const u256& z) {
+    u256 t, z11;
+    pow250(z, t, z11);
+    return mul(sqr_n(t, 5), z11);
+  }
+
+  // z^((p-5)/8) = z^(2^252 - 3)
+  SG_HD static u256 pow_p58(const u256& z) {
+    u256 t, z11;
+    pow250(z, t, z11);
+    return mul(sqr_n(t, 2), z);
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Generic Montgomery arithmetic, R = 2^256 (CIOS with even/odd carry chains)
+// ---------------------------------------------------------------------------
+// Row i adds a * b_i and then m * N (m = t0 * n0'), each as an even-limb and
+// an odd-limb carry chain, and drops the (now zero) low word.
+SG_HD u256 mont_mul(const u256& a, const u256& b, const u256& N, uint32_t ninv) {
+  uint32_t t[10];
+#pragma unroll
+  for (int k = 0; k < 10; ++k) t[k] = 0;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const uint32_t bi = b.w[i];
+    t[0] = mad_lo_cc(a.w[0], bi, t[0]);
+    t[1] = madc_hi_cc(a.w[0], bi, t[1]);
+#pragma unroll
+    for (int j = 2; j < 8; j += 2) {
+      t[j] = madc_lo_cc(a.w[j], bi, t[j]);
+      t[j + 1] = madc_hi_cc(a.w[j], bi, t[j + 1]);
+    }
+    t[8] = addc_cc(t[8], 0u);
+    t[9] = addc(t[9], 0u);
+    t[1] = mad_lo_cc(a.w[1], bi, t[1]);
+    t[2] = madc_hi_cc(a.w[1], bi, t[2]);
+#pragma unroll
+    for (int j = 3; j < 8; j += 2) {
+      t[j] = madc_lo_cc(a.w[j], bi, t[j]);
+      t[j + 1] = madc_hi_cc(a.w[j], bi, t[j + 1]);
+    }
+    t[9] = addc(t[9], 0u);
+
+    const uint32_t m = mul_lo(t[0], ninv);
+    t[0] = mad_lo_cc(m, N.w[0], t[0]);
+    t[1] = madc_hi_cc(m, N.w[0], t[1]);
+#pragma unroll
+    for (int j = 2; j < 8; j += 2) {
+      t[j] = madc_lo_cc(m, N.w[j], t[j]);
+      t[j + 1] = madc_hi_cc(m, N.w[j], t[j + 1]);
+    }
+    t[8] = addc_cc(t[8], 0u);
+    t[9] = addc(t[9], 0u);
+    t[1] = mad_lo_cc(m, N.w[1], t[1]);
+    t[2] = madc_hi_cc(m, N.w[1], t[2]);
+#pragma unroll
+    for (int j = 3; j < 8; j += 2) {
+      t[j] = madc_lo_cc(m, N.w[j], t[j]);
+      t[j + 1] = madc_hi_cc(m, N.w[j], t[j + 1]);
+    }
+    t[9] = addc(t[9], 0u);
+    // shift down one word
+#pragma unroll
+    for (int k = 0; k < 9; ++k) t[k] = t[k + 1];
+    t[9] = 0;
+  }
+  // t < 2N: subtract N once when t >= N
+  u256 r, s;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) r.w[k] = t[k];
+  uint32_t bw = u256_sub(s, r, N);
+  return u256_select((t[8] != 0) | (bw == 0), s, r);
+}
+
+template <class C>
+struct Mont {
+  SG_HD static u256 N() { return C::N(); }
+  SG_HD static u256 mul(const u256& a, const u256& b) { return mont_mul(a, b, C::N(), C::NINV); }
+  SG_HD static u256 sqr(const u256& a) { return mont_mul(a, a, C::N(), C::NINV); }
+  SG_HD static u256 add(const u256& a, const u256& b) { return mod_add(a, b, C::N()); }
+  SG_HD static u256 sub(const u256& a, const u256& b) { return mod_sub(a, b, C::N()); }
+  SG_HD static u256 neg(const u256& a) { return mod_neg(a, C::N()); }
+  SG_HD static u256 zero() { return u256_zero(); }
+  SG_HD static u256 one() { return C::ONE_MONT(); }                 // R mod N
+  SG_HD static u256 from_int(const u256& x) { return mul(x, C::R2()); }  // any x < 2^256
+  SG_HD static u256 to_int(const u256& a) { return mul(a, u256_small(1)); }
+  SG_HD static u256 sqr_n(u256 a, int n) {
+#pragma unroll 1
+    for (int i = 0; i < n; ++i) a = sqr(a);
+    return a;
+  }
+  // a^e for a constant exponent given as 8 little-endian words, 4-bit window
+  SG_HD static u256 pow_const(const u256& a, const uint32_t* e) {
+    u256 tab[16];
+    tab[0] = one();
+    tab[1] = a;
+#pragma unroll 1
+    for (int k = 2; k < 16; ++k) tab[k] = mul(tab[k - 1], a);
+    u256 r = tab[e[7] >> 28];
+#pragma unroll 1
+    for (int i = 62; i >= 0; --i) {
+      r = sqr_n(r, 4);
+      uint32_t nib = (e[i >> 3] >> ((i & 7) * 4)) & 15u;
+      if (nib) r = mul(r, tab[nib]);
+    }
+    return r;
+  }
+  // Fermat inverse in the Montgomery domain
+  SG_HD static u256 inv(const u256& a) {
+    uint32_t e[8];
+    u256 m2 = C::N_MINUS_2();
+#pragma unroll
+    for (int k = 0; k < 8; ++k) e[k] = m2.w[k];
+    return pow_const(a, e);
+  }
+};
+
+struct K1ScalarC {
+  SG_HD static u256 N() { return SG_U256(0xd0364141u, 0xbfd25e8cu, 0xaf48a03bu, 0xbaaedce6u, 0xfffffffeu, 0xffffffffu, 0xffffffffu, 0xffffffffu); }
+  SG_HD static u256 R2() { return SG_U256(0x67d7d140u, 0x896cf214u, 0x0e7cf878u, 0x741496c2u, 0x5bcd07c6u, 0xe697f5e4u, 0x81c69bc5u, 0x9d671cd5u); }
+  SG_HD static u256 ONE_MONT() { return SG_U256(0x2fc9bebfu, 0x402da173u, 0x50b75fc4u, 0x45512319u, 0x00000001u, 0x00000000u, 0x00000000u, 0x00000000u); }
+  SG_HD static u256 N_MINUS_2() { return SG_U256(0xd036413fu, 0xbfd25e8cu, 0xaf48a03bu, 0xbaaedce6u, 0xfffffffeu, 0xffffffffu, 0xffffffffu, 0xffffffffu); }
+  static constexpr uint32_t NINV = 0x5588b13fu;
+};
+
+struct R1ScalarC {
+  SG_HD static u256 N() { return SG_U256(0xfc632551u, 0xf3b9cac2u, 0xa7179e84u, 0xbce6faadu, 0xffffffffu, 0xffffffffu, 0x00000000u, 0xffffffffu); }
+  SG_HD static u256 R2() { return SG_U256(0xbe79eea2u, 0x83244c95u, 0x49bd6fa6u, 0x4699799cu, 0x2b6bec59u, 0x2845b239u, 0xf3d95620u, 0x66e12d94u); }
+  SG_HD static u256 ONE_MONT() { return SG_U256(0x039cdaafu, 0x0c46353du, 0x58e8617bu, 0x43190552u, 0x00000000u, 0x00000000u, 0xffffffffu, 0x00000000u); }
+  SG_HD static u256 N_MINUS_2() { return SG_U256(0xfc63254fu, 0xf3b9cac2u, 0xa7179e84u, 0xbce6faadu, 0xffffffffu, 0xffffffffu, 0x00000000u, 0xffffffffu); }
+  static constexpr uint32_t NINV = 0xee00bc4fu;
+};
+
+struct EdScalarC {
+  SG_HD static u256 N() { return SG_U256(0x5cf5d3edu, 0x5812631au, 0xa2f79cd6u, 0x14def9deu, 0x00000000u, 0x00000000u, 0x00000000u, 0x10000000u); }
+  SG_HD static u256 R2() { return SG_U256(0x449c0f01u, 0xa40611e3u, 0x68859347u, 0xd00e1ba7u, 0x17f5be65u, 0xceec73d2u, 0x7c309a3du, 0x0399411bu); }
+  SG_HD static u256 ONE_MONT() { return SG_U256(0x8d98951du, 0xd6ec3174u, 0x737dcf70u, 0xc6ef5bf4u, 0xfffffffeu, 0xffffffffu, 0xffffffffu, 0x0fffffffu); }
+  SG_HD static u256 N_MINUS_2() { return SG_U256(0x5cf5d3ebu, 0x5812631au, 0xa2f79cd6u, 0x14def9deu, 0x00000000u, 0x00000000u, 0x00000000u, 0x10000000u); }
+  static constexpr uint32_t NINV = 0x12547e1bu;
+};
+
+struct R1BaseC {
+  SG_HD static u256 N() { return SG_U256(0xffffffffu, 0xffffffffu, 0xffffffffu, 0x00000000u, 0x00000000u, 0x00000000u, 0x00000001u, 0xffffffffu); }
+  SG_HD static u256 R2() { return SG_U256(0x00000003u, 0x00000000u, 0xffffffffu, 0xfffffffbu, 0xfffffffeu, 0xffffffffu, 0xfffffffdu, 0x00000004u); }
+  SG_HD static u256 ONE_MONT() { return SG_U256(0x00000001u, 0x00000000u, 0x00000000u, 0xffffffffu, 0xffffffffu, 0xffffffffu, 0xfffffffeu, 0x00000000u); }
+  SG_HD static u256 N_MINUS_2() { return SG_U256(0xfffffffdu, 0xffffffffu, 0xffffffffu, 0x00000000u, 0x00000000u, 0x00000000u, 0x00000001u, 0xffffffffu); }
+  static constexpr uint32_t NINV = 0x1u;
+};
+
+using ScK1 = Mont<K1ScalarC>;
+using ScR1 = Mont<R1ScalarC>;
+using ScEd = Mont<EdScalarC>;
+
+// ---------------------------------------------------------------------------
+// P-256 base field: Montgomery form with addition chains for inverse / sqrt
+// ---------------------------------------------------------------------------
+struct FpR1 : Mont<R1BaseC> {
+  using B = Mont<R1BaseC>;
+  SG_HD static u256 P() { return R1BaseC::N(); }
+  SG_HD static u256 from_int(const u256& x) { return B::from_int(reduce_once(x, P())); }
+  SG_HD static u256 curve_b() { return SG_U256(0x29c4bddfu, 0xd89cdf62u, 0x78843090u, 0xacf005cdu, 0xf7212ed6u, 0xe5a220abu, 0x04874834u, 0xdc30061du); }
+
+  // x2, x4, x8, x16, x32 blocks: a^(2^k - 1)
+  SG_HD static void blocks(const u256& a, u256& x2, u256& x4, u256& x8, u256& x16, u256& x32) {
+    x2 = mul(sqr(a), a);
+    x4 = mul(sqr_n(x2, 2), x2);
+    x8 = mul(sqr_n(x4, 4), x4);
+    x16 = mul(sqr_n(x8, 8), x8);
+    x32 = mul(sqr_n(x16, 16), x16);
+  }
+
+  // a^(p-2), p-2 = ones[255..224] 0^31 1 0^96 ones[95..2] 0 1 : 255 S + 13 M
+  SG_HD static u256 inv(const u256& a) {
+    u256 x2, x4, x8, x16, x32;
+    blocks(a, x2, x4, x8, x16, x32);
+    u256 t = mul(sqr_n(x32, 32), a);
+    t = sqr_n(t, 96);
+    t = mul(sqr_n(t, 32), x32);
+    t = mul(sqr_n(t, 32), x32);
+    t = mul(sqr_n(t, 16), x16);
+    t = mul(sqr_n(t, 8), x8);
+    t = mul(sqr_n(t, 4), x4);
+    t = mul(sqr_n(t, 2), x2);
+    t = mul(sqr_n(t, 2), a);
+    return t;
+  }
+
+  // a^((p+1)/4) = a^(2^254 - 2^222 + 2^190 + 2^94): 253 S + 7 M
+  SG_HD static u256 sqrt_candidate(const u256& a) {
+    u256 x2, x4, x8, x16, x32;
+    blocks(a, x2, x4, x8, x16, x32);
+    u256 t = mul(sqr_n(x32, 32), a);
+    t = mul(sqr_n(t, 96), a);
+    t = sqr_n(t, 94);
+    return t;
+  }
+};
+
+}  // namespace sg

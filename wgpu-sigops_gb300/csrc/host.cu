@@ -1,0 +1,423 @@
+// Host runtime behind include/sigops.h: contexts, device-resident tables,
+// pinned staging, launches and the drop-in entry points.
+//
+// Replaces the reference's per-call wgpu plumbing (src/gpu.rs:5-186: a new
+// instance/adapter/device, pipeline compile and buffers on every call) with a
+// resident context: tables are built once, buffers grow and are reused, and a
+// call is H2D copy -> one kernel -> D2H copy on the context's stream.
+#include <cuda_runtime.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <map>
+#include <mutex>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "../../include/sigops.h"
+#include "launch.h"
+#include "tables.cuh"
+
+using namespace sg;
+
+namespace {
+
+thread_local std::string g_last_error = "no error";
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+
+#define SG_CUDA(call)                                                                                 \
+  do {                                                                                                \
+    cudaError_t e_ = (call);                                                                          \
+    if (e_ != cudaSuccess) return fail(SIGOPS_E_CUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+  } while (0)
+
+// host tables (built once per process)
+struct HostTables {
+  std::vector<uint32_t> gtab[3];
+  std::map<std::pair<int, uint32_t>, std::vector<uint32_t>> bases;
+  std::mutex mu;
+  bool built = false;
+  void build() {
+    std::lock_guard<std::mutex> g(mu);
+    if (built) return;
+    gtab[CURVE_SECP256K1].resize(ECDSA_GTAB * 16);
+    gtab[CURVE_SECP256R1].resize(ECDSA_GTAB * 16);
+    gtab[CURVE_ED25519].resize(ED_GTAB * 24);
+    build_weier_gtab<K1Traits>(k1_gx(), k1_gy(), gtab[CURVE_SECP256K1].data());
+    build_weier_gtab<R1Traits>(r1_gx(), r1_gy(), gtab[CURVE_SECP256R1].data());
+    build_ed_btab(gtab[CURVE_ED25519].data());
+    built = true;
+  }
+  const std::vector<uint32_t>* get_bases(int curve, uint32_t L) {
+    std::lock_guard<std::mutex> g(mu);
+    auto key = std::make_pair(curve, L);
+    auto it = bases.find(key);
+    if (it != bases.end()) return &it->second;
+    std::vector<uint32_t> v(bases_len(curve, L));
+    if (build_bases(curve, L, v.data()) < 0) return nullptr;
+    return &(bases[key] = std::move(v));
+  }
+};
+HostTables& host_tables() {
+  static HostTables t;
+  return t;
+}
+
+bool valid_curve(int c) { return c == SIGOPS_SECP256K1 || c == SIGOPS_SECP256R1 || c == SIGOPS_ED25519; }
+bool valid_L(uint32_t L) { return L >= MIN_LOG_LIMB && L <= MAX_LOG_LIMB; }
+
+}  // namespace
+
+struct sigops_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int num_sms = 0;
+  int grid[3] = {0, 0, 0};
+  uint32_t* d_gtab[3] = {nullptr, nullptr, nullptr};
+  uint32_t* d_err = nullptr;
+  uint8_t* d_buf = nullptr;  // inputs then outputs of host-buffer calls
+  size_t d_cap = 0;
+  uint8_t* h_buf = nullptr;  // pinned staging
+  size_t h_cap = 0;
+  std::mutex mu;
+};
+
+namespace {
+
+int ensure_buffers(sigops_ctx* c, size_t bytes) {
+  bytes = (bytes + 255) & ~(size_t)255;
+  if (bytes > c->d_cap) {
+    if (c->d_buf) cudaFree(c->d_buf);
+    c->d_buf = nullptr;
+    c->d_cap = 0;
+    if (cudaMalloc(&c->d_buf, bytes) != cudaSuccess) return fail(SIGOPS_E_NOMEM, "cudaMalloc(%zu) failed", bytes);
+    c->d_cap = bytes;
+  }
+  if (bytes > c->h_cap) {
+    if (c->h_buf) cudaFreeHost(c->h_buf);
+    c->h_buf = nullptr;
+    c->h_cap = 0;
+    if (cudaMallocHost(&c->h_buf, bytes) != cudaSuccess) return fail(SIGOPS_E_NOMEM, "cudaMallocHost(%zu) failed", bytes);
+    c->h_cap = bytes;
+  }
+  return SIGOPS_OK;
+}
+
+int check_device_errors(sigops_ctx* c) {
+  uint32_t e = 0;
+  SG_CUDA(cudaMemcpyAsync(&e, c->d_err, sizeof e, cudaMemcpyDeviceToHost, c->stream));
+  SG_CUDA(cudaStreamSynchronize(c->stream));
+  if (e) {
+    SG_CUDA(cudaMemsetAsync(c->d_err, 0, sizeof(uint32_t), c->stream));
+    SG_CUDA(cudaStreamSynchronize(c->stream));
+    if (e & DEV_ERR_STAGE_TIMEOUT) return fail(SIGOPS_E_TIMEDOUT, "device: table staging wait expired (error bits 0x%x)", e);
+    return fail(SIGOPS_E_TIMEDOUT, "device error bits 0x%x", e);
+  }
+  return SIGOPS_OK;
+}
+
+std::mutex g_default_mu;
+sigops_ctx* g_default = nullptr;
+
+sigops_ctx* resolve(sigops_ctx* c) {
+  if (c) return c;
+  std::lock_guard<std::mutex> g(g_default_mu);
+  if (!g_default) g_default = sigops_create(0);
+  return g_default;
+}
+
+// layout of the staging buffer for one host-buffer call
+struct Layout {
+  size_t sig, msg, pk, out, status, total;
+};
+Layout layout_for(int curve, size_t n) {
+  auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+  Layout l;
+  l.sig = 0;
+  l.msg = al(l.sig + n * 64);
+  l.pk = al(l.msg + n * 32);
+  size_t after_pk = curve == SIGOPS_ED25519 ? al(l.pk + n * 32) : l.pk;
+  l.out = after_pk;
+  l.status = al(l.out + (curve == SIGOPS_ED25519 ? n : n * 64));
+  l.total = al(l.status + n);
+  return l;
+}
+
+int run_host_call(sigops_ctx* ctx, int curve, const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks, size_t n, uint8_t* out,
+                  uint8_t* out_status) {
+  if (n == 0) return SIGOPS_OK;
+  if (!sigs || !msgs || !out || (curve == SIGOPS_ED25519 && !pks)) return fail(SIGOPS_E_INVAL, "null buffer");
+  sigops_ctx* c = resolve(ctx);
+  if (!c) return SIGOPS_E_NODEV;
+  std::lock_guard<std::mutex> g(c->mu);
+  SG_CUDA(cudaSetDevice(c->device));
+  Layout l = layout_for(curve, n);
+  int rc = ensure_buffers(c, l.total);
+  if (rc) return rc;
+  memcpy(c->h_buf + l.sig, sigs, n * 64);
+  memcpy(c->h_buf + l.msg, msgs, n * 32);
+  if (curve == SIGOPS_ED25519) memcpy(c->h_buf + l.pk, pks, n * 32);
+  SG_CUDA(cudaMemcpyAsync(c->d_buf, c->h_buf, l.out, cudaMemcpyHostToDevice, c->stream));
+  SG_CUDA(launch_plain(curve, c->d_buf + l.sig, c->d_buf + l.msg, c->d_buf + l.pk, n, c->d_gtab[curve], c->d_buf + l.out,
+                       c->d_buf + l.status, c->d_err, c->grid[curve], c->stream));
+  SG_CUDA(cudaMemcpyAsync(c->h_buf + l.out, c->d_buf + l.out, l.total - l.out, cudaMemcpyDeviceToHost, c->stream));
+  rc = check_device_errors(c);
+  if (rc) return rc;
+  memcpy(out, c->h_buf + l.out, curve == SIGOPS_ED25519 ? n : n * 64);
+  if (out_status) memcpy(out_status, c->h_buf + l.status, n);
+  return SIGOPS_OK;
+}
+
+int check_table_arg(int curve, const uint32_t* table, size_t len, uint32_t L) {
+  if (!table && len) return fail(SIGOPS_E_INVAL, "null table_limbs");
+  return sigops_check_table(curve, table, len, L);
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* sigops_version(void) { return "sigops-gb300 0.1 (sm_103a)"; }
+
+const char* sigops_last_error(void) { return g_last_error.c_str(); }
+
+const char* sigops_strerror(int code) {
+  switch (code) {
+    case SIGOPS_OK: return "ok";
+    case SIGOPS_E_INVAL: return "invalid argument";
+    case SIGOPS_E_NOMEM: return "out of memory";
+    case SIGOPS_E_NODEV: return "no such CUDA device";
+    case SIGOPS_E_CUDA: return "CUDA error";
+    case SIGOPS_E_TABLE: return "table_limbs do not match the generator table";
+    case SIGOPS_E_TIMEDOUT: return "device wait timed out";
+    case SIGOPS_E_BUSY: return "busy";
+    case SIGOPS_E_RANGE: return "batch exceeds capacity";
+    default: return "unknown error";
+  }
+}
+
+sigops_ctx* sigops_create(int device) {
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
+    fail(SIGOPS_E_NODEV, "no CUDA device %d (count %d)", device, ndev);
+    return nullptr;
+  }
+  host_tables().build();
+  sigops_ctx* c = new sigops_ctx();
+  c->device = device;
+  auto bail = [&](const char* what, cudaError_t e) -> sigops_ctx* {
+    fail(SIGOPS_E_CUDA, "%s: %s", what, cudaGetErrorString(e));
+    sigops_destroy(c);
+    return nullptr;
+  };
+  cudaError_t e;
+  if ((e = cudaSetDevice(device)) != cudaSuccess) return bail("cudaSetDevice", e);
+  if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess) return bail("cudaStreamCreate", e);
+  if ((e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device)) != cudaSuccess) return bail("attr", e);
+  for (int k = 0; k < 3; ++k) {
+    const auto& t = host_tables().gtab[k];
+    if ((e = cudaMalloc(&c->d_gtab[k], t.size() * 4)) != cudaSuccess) return bail("cudaMalloc(table)", e);
+    if ((e = cudaMemcpy(c->d_gtab[k], t.data(), t.size() * 4, cudaMemcpyHostToDevice)) != cudaSuccess) return bail("table upload", e);
+    int bps = plain_max_blocks_per_sm(k);
+    c->grid[k] = c->num_sms * (bps > 0 ? bps : 1);
+  }
+  if ((e = cudaMalloc(&c->d_err, sizeof(uint32_t))) != cudaSuccess) return bail("cudaMalloc(err)", e);
+  if ((e = cudaMemset(c->d_err, 0, sizeof(uint32_t))) != cudaSuccess) return bail("memset", e);
+  return c;
+}
+
+void sigops_destroy(sigops_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  for (int k = 0; k < 3; ++k)
+    if (c->d_gtab[k]) cudaFree(c->d_gtab[k]);
+  if (c->d_err) cudaFree(c->d_err);
+  if (c->d_buf) cudaFree(c->d_buf);
+  if (c->h_buf) cudaFreeHost(c->h_buf);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  {
+    std::lock_guard<std::mutex> g(g_default_mu);
+    if (g_default == c) g_default = nullptr;
+  }
+  delete c;
+}
+
+long sigops_bases_len(int curve, uint32_t L) {
+  if (!valid_curve(curve) || !valid_L(L)) return fail(SIGOPS_E_INVAL, "bad curve %d or log_limb_size %u", curve, L);
+  return bases_len(curve, L);
+}
+
+long sigops_bases(int curve, uint32_t L, uint32_t* out, size_t cap) {
+  long len = sigops_bases_len(curve, L);
+  if (len < 0) return len;
+  if (!out || cap < (size_t)len) return fail(SIGOPS_E_INVAL, "output capacity %zu < %ld", cap, len);
+  const std::vector<uint32_t>* v = host_tables().get_bases(curve, L);
+  if (!v) return fail(SIGOPS_E_INVAL, "table build failed");
+  memcpy(out, v->data(), v->size() * 4);
+  return len;
+}
+
+int sigops_check_table(int curve, const uint32_t* table, size_t len, uint32_t L) {
+  long want = sigops_bases_len(curve, L);
+  if (want < 0) return (int)want;
+  const std::vector<uint32_t>* v = host_tables().get_bases(curve, L);
+  if (!v) return fail(SIGOPS_E_INVAL, "table build failed");
+  if (len != (size_t)want || !table || memcmp(table, v->data(), len * 4) != 0)
+    return fail(SIGOPS_E_TABLE, "table_limbs differ from precompute bases (len %zu, expected %ld)", len, want);
+  return SIGOPS_OK;
+}
+
+int sigops_secp256k1_ecrecover(sigops_ctx* ctx, const uint8_t* sigs, const uint8_t* msgs, size_t n, const uint32_t* table,
+                               size_t table_len, uint32_t L, uint8_t* out, uint8_t* status) {
+  int rc = check_table_arg(SIGOPS_SECP256K1, table, table_len, L);
+  if (rc) return rc;
+  return run_host_call(ctx, SIGOPS_SECP256K1, sigs, msgs, nullptr, n, out, status);
+}
+
+int sigops_secp256k1_ecrecover_single_shader(sigops_ctx* ctx, const uint8_t* sigs, const uint8_t* msgs, size_t n, uint32_t L,
+                                             uint8_t* out, uint8_t* status) {
+  if (!valid_L(L)) return fail(SIGOPS_E_INVAL, "log_limb_size %u outside [11, 15]", L);
+  return run_host_call(ctx, SIGOPS_SECP256K1, sigs, msgs, nullptr, n, out, status);
+}
+
+int sigops_secp256r1_ecrecover(sigops_ctx* ctx, const uint8_t* sigs, const uint8_t* msgs, size_t n, const uint32_t* table,
+                               size_t table_len, uint32_t L, uint8_t* out, uint8_t* status) {
+  int rc = check_table_arg(SIGOPS_SECP256R1, table, table_len, L);
+  if (rc) return rc;
+  return run_host_call(ctx, SIGOPS_SECP256R1, sigs, msgs, nullptr, n, out, status);
+}
+
+int sigops_secp256r1_ecrecover_single_shader(sigops_ctx* ctx, const uint8_t* sigs, const uint8_t* msgs, size_t n, uint32_t L,
+                                             uint8_t* out, uint8_t* status) {
+  if (!valid_L(L)) return fail(SIGOPS_E_INVAL, "log_limb_size %u outside [11, 15]", L);
+  return run_host_call(ctx, SIGOPS_SECP256R1, sigs, msgs, nullptr, n, out, status);
+}
+
+int sigops_ed25519_ecverify(sigops_ctx* ctx, const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks, size_t n,
+                            const uint32_t* table, size_t table_len, uint32_t L, uint8_t* valid, uint8_t* status) {
+  int rc = check_table_arg(SIGOPS_ED25519, table, table_len, L);
+  if (rc) return rc;
+  return run_host_call(ctx, SIGOPS_ED25519, sigs, msgs, pks, n, valid, status);
+}
+
+int sigops_ed25519_ecverify_single(sigops_ctx* ctx, const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks, size_t n, uint32_t L,
+                                   uint8_t* valid, uint8_t* status) {
+  if (!valid_L(L)) return fail(SIGOPS_E_INVAL, "log_limb_size %u outside [11, 15]", L);
+  return run_host_call(ctx, SIGOPS_ED25519, sigs, msgs, pks, n, valid, status);
+}
+
+int sigops_plain_device(sigops_ctx* ctx, int curve, const uint8_t* d_sigs, const uint8_t* d_msgs, const uint8_t* d_pks, size_t n,
+                        uint8_t* d_out, uint8_t* d_status, void* stream) {
+  if (!valid_curve(curve)) return fail(SIGOPS_E_INVAL, "bad curve %d", curve);
+  if (n == 0) return SIGOPS_OK;
+  auto misaligned = [](const void* p) { return ((uintptr_t)p & 15u) != 0; };
+  if (!d_sigs || !d_msgs || !d_out || !d_status || (curve == SIGOPS_ED25519 && !d_pks))
+    return fail(SIGOPS_E_INVAL, "null device buffer");
+  if (misaligned(d_sigs) || misaligned(d_msgs) || misaligned(d_out) || (curve == SIGOPS_ED25519 && misaligned(d_pks)))
+    return fail(SIGOPS_E_INVAL, "device buffers must be 16-byte aligned");
+  sigops_ctx* c = resolve(ctx);
+  if (!c) return SIGOPS_E_NODEV;
+  std::lock_guard<std::mutex> g(c->mu);
+  SG_CUDA(cudaSetDevice(c->device));
+  cudaStream_t s = stream ? (cudaStream_t)stream : c->stream;
+  SG_CUDA(launch_plain(curve, d_sigs, d_msgs, d_pks, n, c->d_gtab[curve], d_out, d_status, c->d_err, c->grid[curve], s));
+  return SIGOPS_OK;
+}
+
+int sigops_sync(sigops_ctx* ctx) {
+  sigops_ctx* c = resolve(ctx);
+  if (!c) return SIGOPS_E_NODEV;
+  std::lock_guard<std::mutex> g(c->mu);
+  SG_CUDA(cudaSetDevice(c->device));
+  SG_CUDA(cudaDeviceSynchronize());
+  return check_device_errors(c);
+}
+
+int sigops_probe_imad(sigops_ctx* ctx, double* rate) {
+  if (!rate) return fail(SIGOPS_E_INVAL, "null output");
+  sigops_ctx* c = resolve(ctx);
+  if (!c) return SIGOPS_E_NODEV;
+  std::lock_guard<std::mutex> g(c->mu);
+  SG_CUDA(cudaSetDevice(c->device));
+  uint32_t* d_out = nullptr;
+  SG_CUDA(cudaMalloc(&d_out, 16));
+  const int block = 256, grid = c->num_sms * 8;
+  const uint32_t iters = 4096;
+  cudaEvent_t a, b;
+  SG_CUDA(cudaEventCreate(&a));
+  SG_CUDA(cudaEventCreate(&b));
+  SG_CUDA(launch_imad_probe(d_out, 64, grid, block, c->stream));  // warm-up
+  SG_CUDA(cudaEventRecord(a, c->stream));
+  SG_CUDA(launch_imad_probe(d_out, iters, grid, block, c->stream));
+  SG_CUDA(cudaEventRecord(b, c->stream));
+  SG_CUDA(cudaEventSynchronize(b));
+  float ms = 0;
+  SG_CUDA(cudaEventElapsedTime(&ms, a, b));
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFree(d_out);
+  double ops = (double)grid * block * iters * 8.0 * 16.0;
+  *rate = ops / (ms * 1e-3);
+  return SIGOPS_OK;
+}
+
+int sigops_device_info(sigops_ctx* ctx, int* num_sms, int* g1, int* g2, int* g3) {
+  sigops_ctx* c = resolve(ctx);
+  if (!c) return SIGOPS_E_NODEV;
+  if (num_sms) *num_sms = c->num_sms;
+  if (g1) *g1 = c->grid[0];
+  if (g2) *g2 = c->grid[1];
+  if (g3) *g3 = c->grid[2];
+  return SIGOPS_OK;
+}
+
+int sigops_test_field(sigops_ctx* ctx, int field, int op, const uint8_t* a, const uint8_t* b, uint8_t* out, size_t n) {
+  if (field < 0 || field > 5 || op < 0 || op > 5 || !a || !b || !out) return fail(SIGOPS_E_INVAL, "bad field test arguments");
+  if (n == 0) return SIGOPS_OK;
+  sigops_ctx* c = resolve(ctx);
+  if (!c) return SIGOPS_E_NODEV;
+  std::lock_guard<std::mutex> g(c->mu);
+  SG_CUDA(cudaSetDevice(c->device));
+  int rc = ensure_buffers(c, n * 32 * 4);
+  if (rc) return rc;
+  uint8_t* da = c->d_buf;
+  uint8_t* db = da + n * 32;
+  uint8_t* dout = db + n * 32;
+  SG_CUDA(cudaMemcpyAsync(da, a, n * 32, cudaMemcpyHostToDevice, c->stream));
+  SG_CUDA(cudaMemcpyAsync(db, b, n * 32, cudaMemcpyHostToDevice, c->stream));
+  SG_CUDA(cudaMemsetAsync(dout, 0, n * 64, c->stream));
+  SG_CUDA(launch_field_test(field, op, da, db, dout, (int)n, c->stream));
+  SG_CUDA(cudaMemcpyAsync(out, dout, n * 64, cudaMemcpyDeviceToHost, c->stream));
+  SG_CUDA(cudaStreamSynchronize(c->stream));
+  return SIGOPS_OK;
+}
+
+int sigops_test_sha512(sigops_ctx* ctx, const uint8_t* in, uint8_t* out, size_t n) {
+  if (!in || !out) return fail(SIGOPS_E_INVAL, "null buffer");
+  if (n == 0) return SIGOPS_OK;
+  sigops_ctx* c = resolve(ctx);
+  if (!c) return SIGOPS_E_NODEV;
+  std::lock_guard<std::mutex> g(c->mu);
+  SG_CUDA(cudaSetDevice(c->device));
+  int rc = ensure_buffers(c, n * 160);
+  if (rc) return rc;
+  SG_CUDA(cudaMemcpyAsync(c->d_buf, in, n * 96, cudaMemcpyHostToDevice, c->stream));
+  SG_CUDA(launch_sha512_test(c->d_buf, c->d_buf + n * 96, (int)n, c->stream));
+  SG_CUDA(cudaMemcpyAsync(out, c->d_buf + n * 96, n * 64, cudaMemcpyDeviceToHost, c->stream));
+  SG_CUDA(cudaStreamSynchronize(c->stream));
+  return SIGOPS_OK;
+}
+
+}  // extern "C"

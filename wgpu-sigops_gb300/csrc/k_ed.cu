@@ -1,0 +1,36 @@
+// Plain ed25519 verification kernel instantiation.
+#include "plain.cuh"
+
+namespace sg {
+
+__global__ void __launch_bounds__(PLAIN_BLOCK) ed_plain_kernel(const uint8_t* __restrict__ sigs, const uint8_t* __restrict__ msgs,
+                                                                const uint8_t* __restrict__ pks, size_t n, const uint32_t* __restrict__ btab,
+                                                                uint8_t* __restrict__ valid, uint8_t* __restrict__ status, uint32_t* err) {
+  __shared__ __align__(128) uint32_t tab[ED_GTAB * 24];
+  __shared__ __align__(8) uint64_t bar;
+  if (!stage_to_smem(tab, btab, sizeof(tab), &bar, err)) return;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    uint32_t s[16], m[8], p[8];
+    load_words(sigs, i, 16, s);
+    load_words(msgs, i, 8, m);
+    load_words(pks, i, 8, p);
+    uint8_t st = ed25519_verify(s, m, p, tab);
+    valid[i] = st == ST_OK;
+    status[i] = st;
+  }
+}
+
+cudaError_t launch_plain_ed(const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks, size_t n, const uint32_t* btab, uint8_t* valid,
+                            uint8_t* status, uint32_t* err, int grid, cudaStream_t stream) {
+  ed_plain_kernel<<<grid, PLAIN_BLOCK, 0, stream>>>(sigs, msgs, pks, n, btab, valid, status, err);
+  return cudaGetLastError();
+}
+
+int occupancy_plain_ed() {
+  int b = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, ed_plain_kernel, PLAIN_BLOCK, 0);
+  return b;
+}
+
+}  // namespace sg

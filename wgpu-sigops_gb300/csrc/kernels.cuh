@@ -1,0 +1,67 @@
+// Kernel-side helpers shared by the plain and batched kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include "launch.h"
+#include "tables.cuh"
+
+namespace sg {
+
+// Upper bound on mbarrier polls before a kernel gives up on a bulk copy and
+// reports DEV_ERR_STAGE_TIMEOUT (each try_wait also suspends in hardware for a
+// bounded time, so this is seconds at most).
+constexpr uint32_t STAGE_MAX_POLLS = 1u << 22;
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Copy `bytes` (multiple of 16, both addresses 16-byte aligned) from global to
+// shared memory with one bulk-copy (TMA) instruction completing on an
+// mbarrier; every thread of the block waits with a bounded poll.  Returns
+// false (and sets DEV_ERR_STAGE_TIMEOUT) if the copy did not complete.
+__device__ __forceinline__ bool stage_to_smem(void* dst, const void* src, uint32_t bytes, uint64_t* bar, uint32_t* err) {
+  const uint32_t b = smem_addr(bar);
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b) : "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(bytes) : "memory");
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_addr(dst)),
+        "l"(src), "r"(bytes), "r"(b)
+        : "memory");
+  }
+  uint32_t done = 0;
+  for (uint32_t i = 0; i < STAGE_MAX_POLLS && !done; ++i) {
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(b)
+        : "memory");
+  }
+  if (!done) {
+    atomicOr(err, DEV_ERR_STAGE_TIMEOUT);
+    return false;
+  }
+  return true;
+}
+
+__device__ __forceinline__ void load_words(const uint8_t* base, size_t idx, int nwords, uint32_t* w) {
+  const uint4* p = reinterpret_cast<const uint4*>(base) + idx * (size_t)(nwords / 4);
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    if (q < nwords / 4) {
+      uint4 v = __ldg(p + q);
+      w[4 * q] = v.x; w[4 * q + 1] = v.y; w[4 * q + 2] = v.z; w[4 * q + 3] = v.w;
+    }
+  }
+}
+
+__device__ __forceinline__ void store_words(uint8_t* base, size_t idx, int nwords, const uint32_t* w) {
+  uint4* p = reinterpret_cast<uint4*>(base) + idx * (size_t)(nwords / 4);
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+    if (q < nwords / 4) p[q] = make_uint4(w[4 * q], w[4 * q + 1], w[4 * q + 2], w[4 * q + 3]);
+}
+
+}  // namespace sg

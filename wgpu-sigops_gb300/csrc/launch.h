@@ -1,0 +1,30 @@
+// Internal launch interface between the kernels and the host runtime.
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+namespace sg {
+
+constexpr int PLAIN_BLOCK = 256;
+
+// error bits reported through the device error word
+enum : uint32_t { DEV_ERR_STAGE_TIMEOUT = 1u, DEV_ERR_MISALIGNED = 2u, DEV_ERR_QUEUE_TIMEOUT = 4u };
+
+cudaError_t launch_plain(int curve, const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks, size_t n, const uint32_t* gtab,
+                         uint8_t* out, uint8_t* status, uint32_t* err, int grid, cudaStream_t stream);
+int plain_max_blocks_per_sm(int curve);
+cudaError_t launch_plain_k1(const uint8_t* sigs, const uint8_t* msgs, size_t n, const uint32_t* gtab, uint8_t* out, uint8_t* status,
+                            uint32_t* err, int grid, cudaStream_t stream);
+cudaError_t launch_plain_r1(const uint8_t* sigs, const uint8_t* msgs, size_t n, const uint32_t* gtab, uint8_t* out, uint8_t* status,
+                            uint32_t* err, int grid, cudaStream_t stream);
+cudaError_t launch_plain_ed(const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks, size_t n, const uint32_t* btab, uint8_t* valid,
+                            uint8_t* status, uint32_t* err, int grid, cudaStream_t stream);
+int occupancy_plain_k1();
+int occupancy_plain_r1();
+int occupancy_plain_ed();
+cudaError_t launch_field_test(int field, int op, const void* a, const void* b, void* out, int n, cudaStream_t stream);
+cudaError_t launch_sha512_test(const void* in, void* out, int n, cudaStream_t stream);
+cudaError_t launch_imad_probe(uint32_t* out, uint32_t iters, int grid, int block, cudaStream_t stream);
+
+}  // namespace sg

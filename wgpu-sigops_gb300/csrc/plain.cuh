@@ -1,0 +1,34 @@
+// Plain kernels: one signature per thread, one curve per launch.
+//
+// They replace the reference's one-kernel entry points secp256k1_recover_main /
+// secp256r1_recover_main / ed25519_verify_main
+// (src/wgsl/main/secp256k1_ecdsa_main.wgsl:22-82 and siblings) and their
+// multi-stage variants (src/wgsl/main/*_main_{0..5}.wgsl), which split the same
+// work into 5-6 dispatches with intermediates in global memory.  The
+// generator table is staged into shared memory with one bulk (TMA) copy per
+// block; each thread then walks a grid-stride loop over signatures.
+#pragma once
+#include "kernels.cuh"
+#include "launch.h"
+
+namespace sg {
+
+template <class T>
+__global__ void __launch_bounds__(PLAIN_BLOCK) ecdsa_plain_kernel(const uint8_t* __restrict__ sigs, const uint8_t* __restrict__ msgs,
+                                                                   size_t n, const uint32_t* __restrict__ gtab, uint8_t* __restrict__ out,
+                                                                   uint8_t* __restrict__ status, uint32_t* err) {
+  __shared__ __align__(128) uint32_t tab[ECDSA_GTAB * 16];
+  __shared__ __align__(8) uint64_t bar;
+  if (!stage_to_smem(tab, gtab, sizeof(tab), &bar, err)) return;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    uint32_t s[16], m[8], o[16];
+    load_words(sigs, i, 16, s);
+    load_words(msgs, i, 8, m);
+    uint8_t st = ecdsa_recover<T>(s, m, tab, o);
+    store_words(out, i, 16, o);
+    status[i] = st;
+  }
+}
+
+}  // namespace sg

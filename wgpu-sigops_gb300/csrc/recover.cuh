@@ -1,0 +1,259 @@
+// One signature: secp256k1 / P-256 public-key recovery and ed25519
+// verification, written once for the plain kernels, the batched kernel and the
+// host-side test build.
+//
+// Inputs and outputs are u32 words exactly as the bytes sit in memory
+// (little-endian loads): signatures 16 words, messages and keys 8 words.
+#pragma once
+#include "curve.cuh"
+#include "sha512.cuh"
+
+namespace sg {
+
+// per-item status (include/sigops.h SIGOPS_ST_*)
+enum : uint8_t { ST_OK = 0, ST_BAD_SCALAR = 1, ST_NO_POINT = 2, ST_INFINITY = 3, ST_MISMATCH = 4 };
+
+SG_HD uint32_t bswap32(uint32_t x) {
+#if defined(__CUDA_ARCH__)
+  return __byte_perm(x, 0, 0x0123);
+#else
+  return (x >> 24) | ((x >> 8) & 0xff00u) | ((x << 8) & 0xff0000u) | (x << 24);
+#endif
+}
+
+// 32 big-endian bytes (as 8 loaded words) -> integer
+SG_HD u256 be_words_to_u256(const uint32_t* w) {
+  u256 r;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) r.w[i] = bswap32(w[7 - i]);
+  return r;
+}
+SG_HD void u256_to_be_words(const u256& v, uint32_t* w) {
+#pragma unroll
+  for (int i = 0; i < 8; ++i) w[7 - i] = bswap32(v.w[i]);
+}
+
+// ---------------------------------------------------------------------------
+// ECDSA recovery
+// ---------------------------------------------------------------------------
+// Window widths of the signed fixed windows (Booth): the per-signature point R
+// uses multiples 1..2^(WR-1) built per thread; the generator uses a shared
+// table of multiples 1..2^(WG-1).
+constexpr int ECDSA_WR = 5;
+constexpr int ECDSA_WG = 7;
+constexpr int ECDSA_GTAB = 1 << (ECDSA_WG - 1);  // 64 affine points
+constexpr int ED_WR = 5;
+constexpr int ED_WG = 7;
+constexpr int ED_GTAB = 1 << (ED_WG - 1);  // 64 affine Niels points
+
+struct K1Traits {
+  using F = FpK1;
+  using S = ScK1;
+  static constexpr bool A_M3 = false;
+  SG_HD static u256 rhs(const u256& x) { return F::add(F::mul(F::sqr(x), x), u256_small(7)); }
+};
+struct R1Traits {
+  using F = FpR1;
+  using S = ScR1;
+  static constexpr bool A_M3 = true;
+  SG_HD static u256 rhs(const u256& x) {
+    u256 x3 = F::mul(F::sqr(x), x);
+    u256 x3a = F::sub(x3, F::add(F::add(x, x), x));
+    return F::add(x3a, F::curve_b());
+  }
+};
+
+SG_HD APoint load_apoint(const uint32_t* t, uint32_t idx) {
+  APoint a;
+  const uint32_t* e = t + idx * 16u;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) { a.x.w[k] = e[k]; a.y.w[k] = e[8 + k]; }
+  return a;
+}
+
+// u1 * G + u2 * R, signed fixed windows, one shared doubling chain.
+// gtab: multiples 1..ECDSA_GTAB of G, affine, field representation.
+template <class T>
+SG_HD JPoint ecdsa_lincomb(const u256& u1, const u256& u2, const APoint& R, const uint32_t* gtab) {
+  using W = Weier<typename T::F, T::A_M3>;
+  constexpr int NR = 1 << (ECDSA_WR - 1);
+  JPoint tab[NR];
+  tab[0] = W::from_affine(R);
+  tab[1] = W::dbl(tab[0]);
+#pragma unroll 1
+  for (int k = 2; k < NR; ++k) tab[k] = W::madd(tab[k - 1], R);
+
+  constexpr int JR = (257 + ECDSA_WR - 1) / ECDSA_WR;  // windows for a 256-bit scalar
+  constexpr int JG = (257 + ECDSA_WG - 1) / ECDSA_WG;
+  constexpr int TOP = (JR * ECDSA_WR > JG * ECDSA_WG ? JR * ECDSA_WR : JG * ECDSA_WG) - 1;
+  JPoint acc = W::infinity();
+#pragma unroll 1
+  for (int pos = TOP; pos >= 0; --pos) {
+    acc = W::dbl(acc);
+    if (pos % ECDSA_WR == 0) {
+      bool neg;
+      uint32_t d = booth_digit(u2, pos / ECDSA_WR, ECDSA_WR, neg);
+      if (d) {
+        JPoint e = tab[d - 1];
+        if (neg) e = W::neg(e);
+        acc = W::add(acc, e);
+      }
+    }
+    if (pos % ECDSA_WG == 0) {
+      bool neg;
+      uint32_t d = booth_digit(u1, pos / ECDSA_WG, ECDSA_WG, neg);
+      if (d) {
+        APoint e = load_apoint(gtab, d - 1);
+        if (neg) e = W::neg(e);
+        acc = W::madd(acc, e);
+      }
+    }
+  }
+  return acc;
+}
+
+// Recover the signer's key from a fuel-encoded signature (recovery parity in
+// bit 7 of s[0]); follows the reference's one-kernel path
+// (src/wgsl/secp256k1_ecdsa.wgsl:87-130, src/wgsl/secp256r1_ecdsa.wgsl:87-130)
+// with the validity rules of libsecp256k1 / p256 recovery: r, s in [1, n-1],
+// z = msg mod n, a checked square root for R.y, Q != infinity.
+template <class T>
+SG_HD uint8_t ecdsa_recover(const uint32_t sig[16], const uint32_t msg[8], const uint32_t* gtab, uint32_t out[16]) {
+  using F = typename T::F;
+  using S = typename T::S;
+  using W = Weier<F, T::A_M3>;
+#pragma unroll
+  for (int k = 0; k < 16; ++k) out[k] = 0;
+
+  const u256 N = S::N();
+  u256 r = be_words_to_u256(sig);
+  uint32_t sw[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) sw[k] = sig[8 + k];
+  const uint32_t parity = (sw[0] >> 7) & 1u;  // byte 32 is the low byte of word 8
+  sw[0] &= 0xffffff7fu;
+  u256 s = be_words_to_u256(sw);
+  u256 z = reduce_once(be_words_to_u256(msg), N);
+  if (u256_is_zero(r) || u256_gte(r, N) || u256_is_zero(s) || u256_gte(s, N)) return ST_BAD_SCALAR;
+
+  // R = (r, y) with y^2 = r^3 + a r + b and the requested parity
+  u256 x = F::from_int(r);
+  u256 rhs = T::rhs(x);
+  u256 y = F::sqrt_candidate(rhs);
+  if (!u256_eq(F::sqr(y), rhs)) return ST_NO_POINT;
+  if ((F::to_int(y).w[0] & 1u) != parity) y = F::neg(y);
+  APoint R;
+  R.x = x;
+  R.y = y;
+
+  // u1 = -z / r, u2 = s / r (mod n)
+  u256 rinv_m = S::inv(S::from_int(r));  // r^-1 in Montgomery form
+  u256 u2 = S::mul(s, rinv_m);
+  u256 u1 = S::neg(S::mul(z, rinv_m));
+
+  JPoint Q = ecdsa_lincomb<T>(u1, u2, R, gtab);
+  if (W::is_inf(Q)) return ST_INFINITY;
+  APoint a = W::to_affine(Q);
+  u256_to_be_words(F::to_int(a.x), out);
+  u256_to_be_words(F::to_int(a.y), out + 8);
+  return ST_OK;
+}
+
+// ---------------------------------------------------------------------------
+// ed25519 verification (ed25519-dalek 2.1.1 VerifyingKey::verify semantics)
+// ---------------------------------------------------------------------------
+SG_HD EAffNiels load_eniels(const uint32_t* t, uint32_t idx) {
+  EAffNiels a;
+  const uint32_t* e = t + idx * 24u;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) { a.ypx.w[k] = e[k]; a.ymx.w[k] = e[8 + k]; a.t2d.w[k] = e[16 + k]; }
+  return a;
+}
+
+// k = SHA-512(R || A || M) mod l  (src/wgsl/ed25519_reduce_fr.wgsl:88-125)
+SG_HD u256 ed_challenge(const uint32_t sig[16], const uint32_t pk[8], const uint32_t msg[8]) {
+  uint32_t m[24], h[16];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) { m[k] = sig[k]; m[8 + k] = pk[k]; m[16 + k] = msg[k]; }
+  sha512_96(m, h);
+  u256 lo, hi;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) { lo.w[k] = h[k]; hi.w[k] = h[8 + k]; }
+  // (lo + hi * 2^256) * R mod l, then out of Montgomery form
+  const u256 R3 = SG_U256(0x7b83a2dbu, 0x2a9e4968u, 0xaef7f3ecu, 0x278324e6u, 0x04ec5b65u, 0x8065dc6cu, 0x3599cec7u, 0x0e530b77u);
+  u256 t = ScEd::add(ScEd::mul(hi, R3), ScEd::from_int(lo));
+  return ScEd::to_int(t);
+}
+
+// [s]B + [k](-A), signed fixed windows; btab: multiples 1..ED_GTAB of B (affine Niels)
+SG_HD EPoint ed_lincomb(const u256& s, const u256& k, const EPoint& negA, const uint32_t* btab) {
+  constexpr int NR = 1 << (ED_WR - 1);
+  ENiels tab[NR];
+  EPoint cur = negA;
+  tab[0] = Edw::to_niels(cur);
+  EPoint two = Edw::dbl(negA);
+  cur = two;
+  tab[1] = Edw::to_niels(cur);
+#pragma unroll 1
+  for (int i = 2; i < NR; ++i) {
+    cur = Edw::add(cur, tab[0]);
+    tab[i] = Edw::to_niels(cur);
+  }
+  // both scalars are < l < 2^253
+  constexpr int JR = (254 + ED_WR - 1) / ED_WR;
+  constexpr int JG = (254 + ED_WG - 1) / ED_WG;
+  constexpr int TOP = (JR * ED_WR > JG * ED_WG ? JR * ED_WR : JG * ED_WG) - 1;
+  EPoint acc = Edw::identity();
+#pragma unroll 1
+  for (int pos = TOP; pos >= 0; --pos) {
+    acc = Edw::dbl(acc);
+    if (pos % ED_WR == 0) {
+      bool neg;
+      uint32_t d = booth_digit(k, pos / ED_WR, ED_WR, neg);
+      if (d) {
+        ENiels e = tab[d - 1];
+        if (neg) e = Edw::neg(e);
+        acc = Edw::add(acc, e);
+      }
+    }
+    if (pos % ED_WG == 0) {
+      bool neg;
+      uint32_t d = booth_digit(s, pos / ED_WG, ED_WG, neg);
+      if (d) {
+        EAffNiels e = load_eniels(btab, d - 1);
+        if (neg) e = Edw::neg(e);
+        acc = Edw::madd(acc, e);
+      }
+    }
+  }
+  return acc;
+}
+
+// Verify one signature: A must decompress (as constructing a VerifyingKey
+// does), S must be canonical (S < l, dalek without legacy_compatibility),
+// and compress([S]B - [k]A) must equal the R bytes.  Follows
+// src/wgsl/main/ed25519_eddsa_main.wgsl:23-113 and
+// src/curve_algos/ed25519_eddsa.rs:49-77; adds the S < l check the reference
+// GPU path lacks (src/wgsl/main/ed25519_eddsa_main_0.wgsl:45-54).
+SG_HD uint8_t ed25519_verify(const uint32_t sig[16], const uint32_t msg[8], const uint32_t pk[8], const uint32_t* btab) {
+  u256 aenc;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) aenc.w[k] = pk[k];
+  EPoint A;
+  if (!Edw::decompress(aenc, A)) return ST_NO_POINT;
+  u256 s, renc;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) { renc.w[k] = sig[k]; s.w[k] = sig[8 + k]; }
+  if (u256_gte(s, EdScalarC::N())) return ST_BAD_SCALAR;
+  u256 k = ed_challenge(sig, pk, msg);
+  EPoint negA;
+  negA.X = FpEd::neg(A.X);
+  negA.Y = A.Y;
+  negA.Z = A.Z;
+  negA.T = FpEd::neg(A.T);
+  EPoint Rp = ed_lincomb(s, k, negA, btab);
+  u256 enc = Edw::compress(Rp);
+  return u256_eq(enc, renc) ? ST_OK : ST_MISMATCH;
+}
+
+}  // namespace sg

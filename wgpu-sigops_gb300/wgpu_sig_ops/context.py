@@ -1,0 +1,58 @@
+"""Owning wrapper of a ``sigops_ctx`` (one CUDA stream + resident tables)."""
+
+from __future__ import annotations
+
+import ctypes
+import threading
+
+from ._lib import check, lib
+
+
+class Context:
+    def __init__(self, device: int = 0):
+        self.ptr = lib.sigops_create(device)
+        if not self.ptr:
+            raise RuntimeError("sigops_create failed: " + lib.sigops_last_error().decode())
+        self.device = device
+
+    def close(self):
+        if self.ptr:
+            lib.sigops_destroy(self.ptr)
+            self.ptr = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def sync(self):
+        check(lib.sigops_sync(self.ptr), "sigops_sync")
+
+    def probe_imad(self) -> float:
+        v = ctypes.c_double()
+        check(lib.sigops_probe_imad(self.ptr, ctypes.byref(v)), "sigops_probe_imad")
+        return v.value
+
+    def device_info(self) -> dict:
+        vals = [ctypes.c_int() for _ in range(4)]
+        check(lib.sigops_device_info(self.ptr, *[ctypes.byref(v) for v in vals]), "sigops_device_info")
+        return {"num_sms": vals[0].value, "plain_grid": [v.value for v in vals[1:]]}
+
+
+_default = None
+_default_lock = threading.Lock()
+
+
+def default_context() -> Context:
+    global _default
+    with _default_lock:
+        if _default is None:
+            _default = Context(0)
+        return _default
