@@ -1,0 +1,434 @@
+#!/usr/bin/env python
+"""Benchmark: batch signature verification / recovery on one GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--n N]
+
+Workload (default): the mixed-curve batch -- 1,048,576 signatures, 40%
+secp256k1 recovery / 30% P-256 recovery / 30% ed25519 verification, grouped
+into single-curve requests of log-uniform size 1..4096 in random order, 2%
+tampered.  A step is one pass of the batched engine over the whole batch.
+
+One JSON line on stdout (rank 0).  Keys beyond the common contract:
+  plain        the plain per-curve kernels over the same batch (split by curve
+               before timing): ms_per_step, sigs/s, batched/plain ratio
+  selfcheck    every output checked against the outcome the generator knows
+  roofline     IMAD-pipe roofline of the batched kernel: algorithmic IMAD per
+               signature (256 per 256-bit field multiply; 1.201e6 per ECDSA
+               recovery, 0.912e6 per ed25519 verification) x sigs/s against the
+               IMAD rate measured in-process by a dependency-free mad.lo probe
+  cpu_baseline the C restatement of the reference's CPU path (oracle port)
+               on a bounded sample of the same batch, all host threads; its
+               outputs are compared bit for bit with the GPU's on that sample
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "wgpu-sigops_gb300"))
+
+METRIC = "sigs/sec on 1 GB300, batched vs plain kernel (bit-exact); serving p50/p99 ms"
+IMAD_PER_SIG = {0: 1.201e6, 1: 1.201e6, 2: 0.912e6}  # frozen work model
+WORKLOAD_DESC = ("mixed-curve batch: 1,048,576 signatures, 40% secp256k1 recover / 30% secp256r1 recover / "
+                 "30% ed25519 verify, single-curve requests log-uniform in 1..4096 interleaved, 2% tampered")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--n", type=int, default=1048576)
+    ap.add_argument("--seed", type=int, default=4001)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU-baseline sample duration")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--block", type=int, default=0, help="batched kernel block size (0 = library default)")
+    return ap.parse_args()
+
+
+# --------------------------------------------------------------------------- distributed (replicas)
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+
+            dist.init_process_group("gloo")
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, v: float) -> float:
+        if not self.pg:
+            return v
+        import torch
+
+        t = torch.tensor([v], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, v: float) -> float:
+        if not self.pg:
+            return v
+        import torch
+
+        t = torch.tensor([v], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.SUM)
+        return float(t.item())
+
+
+# --------------------------------------------------------------------------- clocks
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict | None:
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, mx, power, reasons = [], [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+                power.append(float(f[3]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return None
+        load = [s for s, p in zip(sm, power) if p > 0.5 * max(power)] or sm
+        return {"sm_mhz": statistics.median(load), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# --------------------------------------------------------------------------- reference arm
+def reference_arm(args, dist: Dist):
+    """The reference's CPU path (oracle port in C, all host threads) on a
+    bounded sample of the same workload per step."""
+    if dist.rank != 0:
+        return
+    import numpy as np
+
+    from oracle import c_oracle
+
+    W = cpu_workload(args.n, args.seed)
+    threads = os.cpu_count() or 1
+    # each step: a bounded sample of the batch (distinct items tiled), sized so
+    # that all steps together take about 2 x --cpu-seconds
+    sample = calibrate_sample(W, threads, 2 * args.cpu_seconds / max(1, args.steps + args.warmup), c_oracle)
+    idx = np.arange(sample) % len(W["curves"])
+    times = []
+    for step in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        c_oracle.batch_mixed(W["curves"][idx], W["sigs"][idx], W["msgs"][idx], W["pks"][idx], threads=threads)
+        dt = time.perf_counter() - t0
+        if step >= args.warmup:
+            times.append(dt)
+    rate = sample / statistics.mean(times)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": rate, "unit": "sigs/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": statistics.mean(times) * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded PCG64; signed by the oracle's C signer)",
+        "config": {"workload": WORKLOAD_DESC, "sample_per_step": sample},
+        "cpu_baseline": {"value": rate, "unit": "sigs/s", "cores": threads, "kind": "port",
+                         "sample": f"{sample} items per step: {len(W['curves'])} distinct items of the mixed batch (same mix, untampered) tiled; C restatement of fuel-crypto/p256/dalek semantics"},
+        "e2e": {"value": rate, "unit": "sigs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def request_order(n, seed, mix=(0.4, 0.3, 0.3), max_request=4096):
+    """Curve tag per item: single-curve requests of size floor(exp(U(0, ln 4096)))
+    in random order, each curve filled to its share of the mix."""
+    import numpy as np
+
+    rng = np.random.Generator(np.random.PCG64(seed + 7))
+    quota = [int(round(n * mix[0])), int(round(n * mix[1]))]
+    quota.append(n - quota[0] - quota[1])
+    left = list(quota)
+    tags, sizes = [], []
+    while sum(left):
+        w = np.array(left, dtype=np.float64)
+        c = int(rng.choice(3, p=w / w.sum()))
+        size = max(1, min(int(np.floor(np.exp(rng.uniform(0.0, np.log(max_request))))), left[c]))
+        tags.append(np.full(size, c, np.uint8))
+        sizes.append(size)
+        left[c] -= size
+    return np.concatenate(tags), np.array(sizes, np.int64)
+
+
+def cpu_workload(n, seed, distinct=4096):
+    """`distinct` items of the mixed batch signed by the oracle's C signer
+    (reference arm only: it runs without the GPU library)."""
+    import numpy as np
+
+    from oracle import c_oracle
+
+    order, _ = request_order(n, seed)
+    order = order[:distinct]
+    rng = np.random.Generator(np.random.PCG64(seed))
+    m = len(order)
+    sigs = np.zeros((m, 64), np.uint8)
+    msgs = rng.integers(0, 256, size=(m, 32), dtype=np.uint8)
+    pks = np.zeros((m, 32), np.uint8)
+    ns = {0: 0xFFFFFFFFFFFFFFFFFFFFFFFFFFFFFFFEBAAEDCE6AF48A03BBFD25E8CD0364141,
+          1: 0xFFFFFFFF00000000FFFFFFFFFFFFFFFFBCE6FAADA7179E84F3B9CAC2FC632551}
+    for i in range(m):
+        c = int(order[i])
+        if c == 2:
+            s, pk = c_oracle.ed25519_sign(rng.bytes(32), msgs[i].tobytes())
+            sigs[i] = np.frombuffer(s, np.uint8)
+            pks[i] = np.frombuffer(pk, np.uint8)
+        else:
+            while True:
+                d = int.from_bytes(rng.bytes(32), "big") % ns[c] or 1
+                k = int.from_bytes(rng.bytes(32), "big") % ns[c] or 1
+                r = c_oracle.ecdsa_sign(c, d, msgs[i].tobytes(), k)
+                if r:
+                    sigs[i] = np.frombuffer(r[0], np.uint8)
+                    break
+    return {"curves": order, "sigs": sigs, "msgs": msgs, "pks": pks}
+
+
+def calibrate_sample(W, threads, seconds, c_oracle):
+    import numpy as np
+
+    n = len(W["curves"])
+    probe = min(n, 256 * max(1, threads))
+    idx = np.arange(probe)
+    t0 = time.perf_counter()
+    c_oracle.batch_mixed(W["curves"][idx], W["sigs"][idx], W["msgs"][idx], W["pks"][idx], threads=threads)
+    rate = probe / (time.perf_counter() - t0)
+    return int(max(probe, rate * seconds))
+
+
+# --------------------------------------------------------------------------- our arm
+def main():
+    args = parse()
+    dist = Dist()
+    if args.impl == "reference":
+        reference_arm(args, dist)
+        return
+
+    import numpy as np
+    import torch
+
+    torch.cuda.set_device(dist.local)
+    import wgpu_sig_ops as w
+    from wgpu_sig_ops import workload as wl
+    from wgpu_sig_ops._lib import check, lib
+
+    ctx = w.Context(dist.local)
+    if args.block:
+        check(lib.sigops_set_batched_block(ctx.ptr, args.block), "block")
+    info = ctx.device_info()
+    imad_peak = max(ctx.probe_imad() for _ in range(3))
+
+    t_gen = time.perf_counter()
+    order, sizes = request_order(args.n, args.seed + dist.rank)
+    counts0 = {c: int((order == c).sum()) for c in (0, 1, 2)}
+    W = wl.make(counts0, args.seed + dist.rank, {0: 0.02, 1: 0.02, 2: 0.02}, ctx, name="mixed", curves_order=order)
+    W.requests = sizes
+    t_gen = time.perf_counter() - t_gen
+    n = W.n
+    counts = W.counts()
+    dev = torch.device("cuda", dist.local)
+    d_cur = torch.from_numpy(W.curves).to(dev)
+    d_sig = torch.from_numpy(W.sigs).to(dev)
+    d_msg = torch.from_numpy(W.msgs).to(dev)
+    d_pk = torch.from_numpy(W.pks).to(dev)
+    d_out = torch.zeros((n, 64), dtype=torch.uint8, device=dev)
+    d_st = torch.zeros(n, dtype=torch.uint8, device=dev)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    check(lib.sigops_reserve(ctx.ptr, n), "reserve")
+    plan = w.batch.MixedPlan(ctx, d_cur.data_ptr(), d_sig.data_ptr(), d_msg.data_ptr(), d_pk.data_ptr(), n, d_out.data_ptr(), d_st.data_ptr())
+
+    def timed(fn, steps, warmup):
+        with torch.cuda.stream(stream):
+            for _ in range(warmup):
+                fn()
+            torch.cuda.synchronize()
+            dist.barrier()
+            ms = []
+            for _ in range(steps):
+                flush.zero_()  # evict L2 between steps (outside the timed interval)
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                fn()
+                e1.record(stream)
+                e1.synchronize()
+                ms.append(e0.elapsed_time(e1))
+            torch.cuda.synchronize()
+            dist.barrier()
+        return ms
+
+    # ---- batched engine (the headline kernel), inputs resident in HBM
+    clocks = ClockSampler(dist.local)
+    clocks.start()
+    ms_b = timed(lambda: plan.launch(stream.cuda_stream), args.steps, args.warmup)
+    clk = clocks.stop()
+    check(lib.sigops_sync(ctx.ptr), "batched run")
+    out = d_out.cpu().numpy()
+    status = d_st.cpu().numpy()
+    selfcheck = wl.expected_check(W, out, status)
+
+    # ---- plain per-curve kernels over the same batch (split by curve before timing)
+    parts = []
+    for c in (0, 1, 2):
+        sel = np.nonzero(W.curves == c)[0]
+        parts.append((c, len(sel), torch.from_numpy(W.sigs[sel]).to(dev), torch.from_numpy(W.msgs[sel]).to(dev),
+                      torch.from_numpy(W.pks[sel]).to(dev), torch.zeros((len(sel), 64 if c < 2 else 1), dtype=torch.uint8, device=dev),
+                      torch.zeros(len(sel), dtype=torch.uint8, device=dev), sel))
+
+    def plain_step():
+        for c, m, s, mm, p, o, st, _ in parts:
+            check(lib.sigops_plain_device(ctx.ptr, c, s.data_ptr(), mm.data_ptr(), p.data_ptr() if c == 2 else None, m, o.data_ptr(),
+                                          st.data_ptr(), stream.cuda_stream), "plain")
+
+    ms_p = timed(plain_step, max(3, args.steps // 2), 1)
+    check(lib.sigops_sync(ctx.ptr), "plain run")
+    plain_mismatch = 0
+    for c, m, s, mm, p, o, st, sel in parts:
+        po, ps = o.cpu().numpy(), st.cpu().numpy()
+        plain_mismatch += int((ps != status[sel]).sum())
+        if c < 2:
+            plain_mismatch += int((po != out[sel]).any(axis=1).sum())
+        else:
+            plain_mismatch += int((po[:, 0] != out[sel, 0]).sum())
+
+    # ---- end to end through the public API with page-locked host buffers
+    e2e = None
+    if not args.no_e2e:
+        h_cur = torch.from_numpy(W.curves).pin_memory().numpy()
+        h_sig = torch.from_numpy(W.sigs).pin_memory().numpy()
+        h_msg = torch.from_numpy(W.msgs).pin_memory().numpy()
+        h_pk = torch.from_numpy(W.pks).pin_memory().numpy()
+        h_out = torch.zeros((n, 64), dtype=torch.uint8).pin_memory().numpy()
+        h_st = torch.zeros(n, dtype=torch.uint8).pin_memory().numpy()
+        for _ in range(2):
+            w.batch.verify_mixed_into(ctx, h_cur, h_sig, h_msg, h_pk, h_out, h_st)
+        dist.barrier()
+        ts = []
+        for _ in range(max(3, args.steps // 2)):
+            t0 = time.perf_counter()
+            w.batch.verify_mixed_into(ctx, h_cur, h_sig, h_msg, h_pk, h_out, h_st)
+            ts.append(time.perf_counter() - t0)
+        dist.barrier()
+        e2e_s = dist.max(statistics.mean(ts))
+        e2e_ok = bool((h_out == out).all() and (h_st == status).all())
+        e2e = {"value": dist.sum(n) / e2e_s, "unit": "sigs/s", "h2d_bytes_per_step": int(n * (1 + 64 + 32 + 32)),
+               "d2h_bytes_per_step": int(n * 65), "ms_per_step": e2e_s * 1e3, "matches_device_run": e2e_ok,
+               "api": "sigops_verify_mixed (page-locked host buffers)"}
+
+    ms_step = dist.max(statistics.mean(ms_b))
+    value = dist.sum(n) / (ms_step * 1e-3)
+    plain_ms = dist.max(statistics.mean(ms_p))
+    work = sum(IMAD_PER_SIG[c] * counts[c] for c in counts)
+    achieved = work / (ms_step * 1e-3)
+
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic_batched.json")
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            t = json.load(f)
+        traffic = t.get("dram_bytes_per_sig", 0) * n if t.get("dram_bytes_per_sig") else None
+
+    cpu = None
+    if not args.no_cpu_baseline and dist.rank == 0:
+        cpu = cpu_baseline(W, out, status, args.cpu_seconds)
+
+    if dist.rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": "sigs/s", "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+        "data": "synthetic (seeded PCG64 keys/nonces/seeds/messages; signed on the device; 2% tampered on the host)",
+        "config": {"workload": WORKLOAD_DESC, "n": n, "mix": {"secp256k1": counts[0], "secp256r1": counts[1], "ed25519": counts[2]},
+                   "requests": int(len(W.requests)), "kernel": "batched persistent mixed-curve, CUDA graph",
+                   "l2": "flushed between steps (256 MiB write outside the timed interval)", "grid": info,
+                   "parallelism": f"replicas x{dist.world} (weak scaling, no collective)"},
+        "selfcheck": selfcheck,
+        "plain": {"ms_per_step": plain_ms, "value": dist.sum(n) / (plain_ms * 1e-3), "batched_over_plain": plain_ms / ms_step,
+                  "outputs_equal_batched": plain_mismatch == 0},
+        "roofline": {"bound": "imad", "achieved": achieved / 1e12, "peak": imad_peak / 1e12, "unit": "TIMAD/s",
+                     "frac": achieved / imad_peak, "traffic": traffic,
+                     "peak_source": "measured in-process: mad.lo.u32 probe (MEASURED_PEAKS.json has no integer figure)",
+                     "work_model": "256 IMAD per 256-bit field multiply; 1.201e6 IMAD per ECDSA recovery, 0.912e6 per ed25519 verify"},
+        "e2e": e2e,
+        "cpu_baseline": cpu,
+        "gpu_launches": 2 * args.steps,
+        "clocks": clk,
+        "workload_gen_s": t_gen,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def cpu_baseline(W, out, status, seconds):
+    import numpy as np
+
+    from oracle import c_oracle
+
+    threads = os.cpu_count() or 1
+    # the same batch, a prefix sample sized to about `seconds` of CPU work
+    probe = min(W.n, 512 * threads)
+    t0 = time.perf_counter()
+    c_oracle.batch_mixed(W.curves[:probe], W.sigs[:probe], W.msgs[:probe], W.pks[:probe], threads=threads)
+    rate0 = probe / (time.perf_counter() - t0)
+    sample = int(max(probe, min(W.n, rate0 * seconds)))
+    t0 = time.perf_counter()
+    o_out, o_st = c_oracle.batch_mixed(W.curves[:sample], W.sigs[:sample], W.msgs[:sample], W.pks[:sample], threads=threads)
+    dt = time.perf_counter() - t0
+    mism = int((o_st != status[:sample]).sum() + (o_out != out[:sample]).any(axis=1).sum())
+    return {"value": sample / dt, "unit": "sigs/s", "cores": threads, "kind": "port",
+            "sample": f"first {sample} items of the batch (same mix), {dt:.1f} s", "bit_exact_vs_gpu": mism == 0, "mismatches": mism}
+
+
+if __name__ == "__main__":
+    main()

@@ -63,6 +63,7 @@ extern "C" {
 #define SIGOPS_ST_MISMATCH 4   /* ed25519: [S]B - [k]A does not encode to R */
 
 typedef struct sigops_ctx sigops_ctx;
+typedef struct sigops_plan sigops_plan;
 
 /* ---------------------------------------------------------------- context */
 
@@ -139,6 +140,52 @@ int sigops_ed25519_ecverify_single(sigops_ctx* ctx, const uint8_t* sigs, const u
  * (src/gpu.rs:88-104) without its per-call device creation. */
 int sigops_plain_device(sigops_ctx* ctx, int curve, const uint8_t* d_sigs, const uint8_t* d_msgs, const uint8_t* d_pks, size_t n,
                         uint8_t* d_out, uint8_t* d_status, void* stream);
+
+/* ----------------------------------------- batched mixed-curve engine */
+
+/* Verify a batch that mixes the three curves in one persistent launch.  No
+ * counterpart in the reference, which runs one curve per call with
+ * power-of-two padding (src/secp256k1_ecdsa.rs:25-44); per-item semantics are
+ * those of the per-curve calls above.
+ * curves: n tags (SIGOPS_SECP256K1 / SECP256R1 / ED25519); sigs n*64; msgs
+ * n*32; pks n*32 (read for ed25519 items only); out n*64 (ECDSA: key bytes;
+ * ed25519: byte 0 = valid, rest zero); out_status n (may be NULL). */
+int sigops_verify_mixed(sigops_ctx* ctx, const uint8_t* curves, const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks, size_t n,
+                        uint8_t* out, uint8_t* out_status);
+
+/* Same over device buffers (16-byte aligned) on `stream`; no host sync.
+ * Uses context-owned scratch sized by sigops_reserve (grown on demand, which
+ * allocates: reserve first when capturing into a CUDA graph). */
+int sigops_verify_mixed_device(sigops_ctx* ctx, const uint8_t* d_curves, const uint8_t* d_sigs, const uint8_t* d_msgs, const uint8_t* d_pks,
+                               size_t n, uint8_t* d_out, uint8_t* d_status, void* stream);
+
+/* Size the context's batched-engine scratch for batches of up to n items. */
+int sigops_reserve(sigops_ctx* ctx, size_t n);
+
+/* A CUDA graph of one batched step over fixed device buffers: the scratch
+ * reset, the classify kernel and the persistent kernel, replayed by
+ * sigops_mixed_plan_launch.  The plan uses the context's scratch: do not run
+ * two plans or mixed calls of one context concurrently. */
+int sigops_mixed_plan_create(sigops_ctx* ctx, const uint8_t* d_curves, const uint8_t* d_sigs, const uint8_t* d_msgs, const uint8_t* d_pks,
+                             size_t n, uint8_t* d_out, uint8_t* d_status, sigops_plan** plan);
+int sigops_mixed_plan_launch(sigops_plan* plan, void* stream);
+void sigops_mixed_plan_destroy(sigops_plan* plan);
+
+/* Threads per block of the persistent kernel (128 or 256). */
+int sigops_set_batched_block(sigops_ctx* ctx, int block);
+
+/* ------------------------------------------- synthetic workload signing */
+
+/* Sign on the device to generate benchmark / test inputs (no counterpart on
+ * the reference's path, whose tests sign on the CPU with fuel-crypto / p256 /
+ * ed25519-dalek).  ECDSA: secret and nonce 32 bytes big-endian per item;
+ * writes fuel-encoded low-s signatures (n*64), public keys (n*64) and a status
+ * byte (0 ok, 1 the secret/nonce pair cannot sign).  ed25519: RFC 8032 from
+ * 32-byte seeds; writes signatures (n*64) and keys (n*32). */
+int sigops_workload_sign_ecdsa(sigops_ctx* ctx, int curve, const uint8_t* d_secrets, const uint8_t* d_nonces, const uint8_t* d_msgs, size_t n,
+                               uint8_t* d_sigs, uint8_t* d_pubkeys, uint8_t* d_status, void* stream);
+int sigops_workload_sign_ed25519(sigops_ctx* ctx, const uint8_t* d_seeds, const uint8_t* d_msgs, size_t n, uint8_t* d_sigs, uint8_t* d_pks,
+                                 void* stream);
 
 /* Wait for the context's stream and report device-side errors since the last
  * call (SIGOPS_E_TIMEDOUT if a bounded wait expired). */

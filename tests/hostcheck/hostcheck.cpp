@@ -96,3 +96,22 @@ void hc_sha512_96(const uint8_t* in, uint8_t* out) {
 }
 
 }  // extern "C"
+
+#include "../../wgpu-sigops_gb300/csrc/sign.cuh"
+
+extern "C" int hc_ecdsa_sign(int curve, const uint8_t* d, const uint8_t* k, const uint8_t* msg, uint8_t* sig, uint8_t* pub) {
+  init();
+  uint32_t dw[8], kw[8], m[8], s[16], p[16];
+  memcpy(dw, d, 32); memcpy(kw, k, 32); memcpy(m, msg, 32);
+  int st = curve == 0 ? ecdsa_sign<K1Traits>(dw, kw, m, g_k1, s, p) : ecdsa_sign<R1Traits>(dw, kw, m, g_r1, s, p);
+  memcpy(sig, s, 64); memcpy(pub, p, 64);
+  return st;
+}
+
+extern "C" void hc_ed_sign(const uint8_t* seed, const uint8_t* msg, uint8_t* sig, uint8_t* pk) {
+  init();
+  uint32_t sd[8], m[8], s[16], p[8];
+  memcpy(sd, seed, 32); memcpy(m, msg, 32);
+  ed25519_sign(sd, m, g_ed, s, p);
+  memcpy(sig, s, 64); memcpy(pk, p, 32);
+}

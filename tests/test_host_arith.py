@@ -137,3 +137,20 @@ def test_bases_bit_identical(hc, curve):
         buf = (ctypes.c_uint32 * len(exp))()
         assert hc.hc_bases(curve, L, buf) == len(exp)
         assert list(buf) == exp
+
+
+def test_signers_match_oracle(hc):
+    rng = random.Random(9)
+    for i in range(12):
+        m = rng.randbytes(32)
+        for cid, c in ((0, o.SECP256K1), (1, o.SECP256R1)):
+            d, k = rng.randrange(1, c.n), rng.randrange(1, c.n)
+            sig, pub = ctypes.create_string_buffer(64), ctypes.create_string_buffer(64)
+            assert hc.hc_ecdsa_sign(cid, d.to_bytes(32, "big"), k.to_bytes(32, "big"), m, sig, pub) == 0
+            assert sig.raw == o.ecdsa_sign_fuel(c, d, m, k=k)
+            assert pub.raw == o.ws_public_key(c, d)
+        seed = rng.randbytes(32)
+        sig, pk = ctypes.create_string_buffer(64), ctypes.create_string_buffer(32)
+        hc.hc_ed_sign(seed, m, sig, pk)
+        assert sig.raw == o.ed25519_sign(seed, m)
+        assert pk.raw == o.ed25519_keypair(seed)[2]

@@ -16,9 +16,13 @@
 #if defined(__CUDACC__)
 #define SG_HD __host__ __device__ __forceinline__
 #define SG_DEV __device__ __forceinline__
+// once-per-signature routines (exponentiation chains, scalar multiplication):
+// compiled once and called, which keeps kernels small enough to compile fast
+#define SG_NOINL __host__ __device__ __noinline__
 #else
 #define SG_HD inline
 #define SG_DEV inline
+#define SG_NOINL inline
 #endif
 
 namespace sg {

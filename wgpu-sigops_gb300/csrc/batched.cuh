@@ -1,0 +1,149 @@
+// Batched mixed-curve engine: one persistent launch verifies a batch that
+// mixes secp256k1 recovery, P-256 recovery and ed25519 verification.
+//
+// The reference runs one curve per call and pads every batch to a power of two
+// (src/secp256k1_ecdsa.rs:25-44); it has no mixed-curve path.  Here:
+//   1. classify_kernel buckets item indices by curve (warp-aggregated atomics
+//      into per-curve index lists);
+//   2. batched_kernel runs a persistent grid: each warp repeatedly takes the
+//      next 32-item tile from a global counter; tiles never straddle curves, so
+//      the curve dispatch is warp-uniform and no lane idles on another curve's
+//      code.  All three generator tables are staged into shared memory by bulk
+//      (TMA) copies completing on one mbarrier.
+// Scratch (global memory beyond inputs and outputs): Scratch below.
+#pragma once
+#include "kernels.cuh"
+
+namespace sg {
+
+constexpr int BATCH_TILE = 32;  // items per warp work unit
+constexpr uint32_t QUEUE_MAX_SPINS = 1u << 20;
+
+struct Scratch {
+  uint32_t count[3];    // items per curve (classify)
+  uint32_t next_tile;   // work-stealing counter (batched)
+  uint32_t tiles_done;  // completed tiles (diagnostic)
+  uint32_t pad[3];
+};
+
+// Mixed output record: ECDSA key bytes, or for ed25519 byte 0 = valid.
+struct MixedIO {
+  const uint8_t* curves;  // n tags (0/1/2)
+  const uint8_t* sigs;    // n*64
+  const uint8_t* msgs;    // n*32
+  const uint8_t* pks;     // n*32 (read for ed25519 items only)
+  uint8_t* out;           // n*64
+  uint8_t* status;        // n
+  size_t n;
+};
+
+__global__ void classify_kernel(const uint8_t* __restrict__ curves, size_t n, uint32_t* __restrict__ idx, Scratch* sc) {
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  const unsigned lane = threadIdx.x & 31u;
+  for (size_t base = (size_t)blockIdx.x * blockDim.x; base < n; base += stride) {
+    size_t i = base + threadIdx.x;
+    int c = i < n ? curves[i] : -1;
+    if (c > 2) c = -1;  // unknown tags are skipped (host validates)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      unsigned m = __ballot_sync(0xffffffffu, c == k);
+      if (!m) continue;
+      uint32_t off = 0;
+      int leader = __ffs(m) - 1;
+      if ((int)lane == leader) off = atomicAdd(&sc->count[k], (uint32_t)__popc(m));
+      off = __shfl_sync(0xffffffffu, off, leader);
+      if (c == k) idx[(size_t)k * n + off + __popc(m & ((1u << lane) - 1u))] = (uint32_t)i;
+    }
+  }
+}
+
+struct BatchTables {
+  const uint32_t* k1;
+  const uint32_t* r1;
+  const uint32_t* ed;
+};
+
+// all three tables into shared memory with bulk copies on one mbarrier
+__device__ __forceinline__ bool stage_three(uint32_t* sk1, uint32_t* sr1, uint32_t* sed, const BatchTables& t, uint64_t* bar, uint32_t* err) {
+  const uint32_t b = smem_addr(bar);
+  const uint32_t bk = ECDSA_GTAB * 64, be = ED_GTAB * 96;
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b) : "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(2 * bk + be) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_addr(sk1)), "l"(t.k1),
+                 "r"(bk), "r"(b)
+                 : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_addr(sr1)), "l"(t.r1),
+                 "r"(bk), "r"(b)
+                 : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_addr(sed)), "l"(t.ed),
+                 "r"(be), "r"(b)
+                 : "memory");
+  }
+  uint32_t done = 0;
+  for (uint32_t i = 0; i < STAGE_MAX_POLLS && !done; ++i) {
+    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n selp.u32 %0, 1, 0, p;\n}\n"
+                 : "=r"(done)
+                 : "r"(b)
+                 : "memory");
+  }
+  if (!done) {
+    atomicOr(err, DEV_ERR_STAGE_TIMEOUT);
+    return false;
+  }
+  return true;
+}
+
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK) batched_kernel(MixedIO io, const uint32_t* __restrict__ idx, BatchTables tabs, Scratch* sc,
+                                                        uint32_t* err) {
+  __shared__ __align__(128) uint32_t tk1[ECDSA_GTAB * 16];
+  __shared__ __align__(128) uint32_t tr1[ECDSA_GTAB * 16];
+  __shared__ __align__(128) uint32_t ted[ED_GTAB * 24];
+  __shared__ __align__(8) uint64_t bar;
+  if (!stage_three(tk1, tr1, ted, tabs, &bar, err)) return;
+
+  const uint32_t n1 = sc->count[0], n2 = sc->count[1], n3 = sc->count[2];
+  const uint32_t t1 = (n1 + BATCH_TILE - 1) / BATCH_TILE, t2 = (n2 + BATCH_TILE - 1) / BATCH_TILE, t3 = (n3 + BATCH_TILE - 1) / BATCH_TILE;
+  const uint32_t total = t1 + t2 + t3;
+  const unsigned lane = threadIdx.x & 31u;
+  for (;;) {
+    uint32_t tile = 0;
+    if (lane == 0) tile = atomicAdd(&sc->next_tile, 1u);
+    tile = __shfl_sync(0xffffffffu, tile, 0);
+    if (tile >= total) break;
+    int curve;
+    uint32_t first, cnt;
+    if (tile < t1) { curve = 0; first = tile * BATCH_TILE; cnt = n1; }
+    else if (tile < t1 + t2) { curve = 1; first = (tile - t1) * BATCH_TILE; cnt = n2; }
+    else { curve = 2; first = (tile - t1 - t2) * BATCH_TILE; cnt = n3; }
+    const uint32_t slot = first + lane;
+    if (slot < cnt) {
+      const size_t i = idx[(size_t)curve * io.n + slot];
+      uint32_t s[16], m[8], o[16];
+      load_words(io.sigs, i, 16, s);
+      load_words(io.msgs, i, 8, m);
+      uint8_t st;
+      if (curve == 0) {
+        st = ecdsa_recover<K1Traits>(s, m, tk1, o);
+      } else if (curve == 1) {
+        st = ecdsa_recover<R1Traits>(s, m, tr1, o);
+      } else {
+        uint32_t p[8];
+        load_words(io.pks, i, 8, p);
+        st = ed25519_verify(s, m, p, ted);
+#pragma unroll
+        for (int k = 0; k < 16; ++k) o[k] = 0;
+        o[0] = st == ST_OK;
+      }
+      store_words(io.out, i, 16, o);
+      io.status[i] = st;
+    }
+  }
+}
+
+}  // namespace sg

@@ -116,24 +116,6 @@ struct FpK1 {
   SG_HD static u256 zero() { return u256_zero(); }
   SG_HD static u256 from_int(const u256& x) { return reduce_once(x, P()); }  // x < 2^256
   SG_HD static u256 to_int(const u256& a) { return a; }
-  SG_HD static u256 mul_small(const u256& a, uint32_t k) {  // k < 2^32
-    uint32_t t[16];
-    t[0] = mul_lo(a.w[0], k);
-    t[1] = mad_hi_cc(a.w[0], k, mul_lo(a.w[1], k));
-    // build the 9-limb product, then fold through the generic reducer
-    uint32_t lo[8], hi[8];
-#pragma unroll
-    for (int j = 0; j < 8; ++j) { lo[j] = mul_lo(a.w[j], k); hi[j] = mul_hi(a.w[j], k); }
-    t[0] = lo[0];
-    t[1] = add_cc(lo[1], hi[0]);
-#pragma unroll
-    for (int j = 2; j < 8; ++j) t[j] = addc_cc(lo[j], hi[j - 1]);
-    t[8] = addc(hi[7], 0u);
-#pragma unroll
-    for (int j = 9; j < 16; ++j) t[j] = 0;
-    return reduce(t);
-  }
-
   SG_HD static u256 sqr_n(u256 a, int n) {
 #pragma unroll 1
     for (int i = 0; i < n; ++i) a = sqr(a);
@@ -141,7 +123,7 @@ struct FpK1 {
   }
 
   // x2 .. x223: a^(2^k - 1) blocks shared by the inverse and the square root
-  SG_HD static void blocks(const u256& a, u256& x2, u256& x22, u256& x223) {
+  SG_HD static void blocks(const u256 a, u256& x2, u256& x22, u256& x223) {
     x2 = mul(sqr(a), a);
     u256 x3 = mul(sqr(x2), a);
     u256 x6 = mul(sqr_n(x3, 3), x3);
@@ -156,7 +138,7 @@ struct FpK1 {
   }
 
   // a^(p-2): 255 squarings, 15 multiplications
-  SG_HD static u256 inv(const u256& a) {
+  SG_NOINL static u256 inv(const u256 a) {
     u256 x2, x22, t;
     blocks(a, x2, x22, t);
     t = mul(sqr_n(t, 23), x22);
@@ -167,7 +149,7 @@ struct FpK1 {
   }
 
   // a^((p+1)/4): 253 squarings, 13 multiplications
-  SG_HD static u256 sqrt_candidate(const u256& a) {
+  SG_NOINL static u256 sqrt_candidate(const u256 a) {
     u256 x2, x22, t;
     blocks(a, x2, x22, t);
     t = mul(sqr_n(t, 23), x22);
@@ -243,7 +225,7 @@ struct FpEd {
   }
 
   // z^(2^250 - 1) and z^11 (the shared prefix of the inverse and the p58 power)
-  SG_HD static void pow250(const u256& z, u256& z2_250_0, u256& z11) {
+  SG_HD static void pow250(const u256 z, u256& z2_250_0, u256& z11) {
     u256 z2 = sqr(z);
     u256 z9 = mul(sqr_n(z2, 2), z);
     z11 = mul(z9, z2);
@@ -258,14 +240,14 @@ struct FpEd {
   }
 
   // z^(p-2) = z^(2^255 - 21)
-  SG_HD static u256 inv(const u256& z) {
+  SG_NOINL static u256 inv(const u256 z) {
     u256 t, z11;
     pow250(z, t, z11);
     return mul(sqr_n(t, 5), z11);
   }
 
   // z^((p-5)/8) = z^(2^252 - 3)
-  SG_HD static u256 pow_p58(const u256& z) {
+  SG_NOINL static u256 pow_p58(const u256 z) {
     u256 t, z11;
     pow250(z, t, z11);
     return mul(sqr_n(t, 2), z);
@@ -351,7 +333,7 @@ struct Mont {
     return a;
   }
   // a^e for a constant exponent given as 8 little-endian words, 4-bit window
-  SG_HD static u256 pow_const(const u256& a, const uint32_t* e) {
+  SG_HD static u256 pow_const(const u256 a, const uint32_t* e) {
     u256 tab[16];
     tab[0] = one();
     tab[1] = a;
@@ -367,7 +349,7 @@ struct Mont {
     return r;
   }
   // Fermat inverse in the Montgomery domain
-  SG_HD static u256 inv(const u256& a) {
+  SG_NOINL static u256 inv(const u256 a) {
     uint32_t e[8];
     u256 m2 = C::N_MINUS_2();
 #pragma unroll
@@ -422,7 +404,7 @@ struct FpR1 : Mont<R1BaseC> {
   SG_HD static u256 curve_b() { return SG_U256(0x29c4bddfu, 0xd89cdf62u, 0x78843090u, 0xacf005cdu, 0xf7212ed6u, 0xe5a220abu, 0x04874834u, 0xdc30061du); }
 
   // x2, x4, x8, x16, x32 blocks: a^(2^k - 1)
-  SG_HD static void blocks(const u256& a, u256& x2, u256& x4, u256& x8, u256& x16, u256& x32) {
+  SG_HD static void blocks(const u256 a, u256& x2, u256& x4, u256& x8, u256& x16, u256& x32) {
     x2 = mul(sqr(a), a);
     x4 = mul(sqr_n(x2, 2), x2);
     x8 = mul(sqr_n(x4, 4), x4);
@@ -431,7 +413,7 @@ struct FpR1 : Mont<R1BaseC> {
   }
 
   // a^(p-2), p-2 = ones[255..224] 0^31 1 0^96 ones[95..2] 0 1 : 255 S + 13 M
-  SG_HD static u256 inv(const u256& a) {
+  SG_NOINL static u256 inv(const u256 a) {
     u256 x2, x4, x8, x16, x32;
     blocks(a, x2, x4, x8, x16, x32);
     u256 t = mul(sqr_n(x32, 32), a);
@@ -447,7 +429,7 @@ struct FpR1 : Mont<R1BaseC> {
   }
 
   // a^((p+1)/4) = a^(2^254 - 2^222 + 2^190 + 2^94): 253 S + 7 M
-  SG_HD static u256 sqrt_candidate(const u256& a) {
+  SG_NOINL static u256 sqrt_candidate(const u256 a) {
     u256 x2, x4, x8, x16, x32;
     blocks(a, x2, x4, x8, x16, x32);
     u256 t = mul(sqr_n(x32, 32), a);

@@ -90,7 +90,19 @@ struct sigops_ctx {
   size_t d_cap = 0;
   uint8_t* h_buf = nullptr;  // pinned staging
   size_t h_cap = 0;
+  // batched engine
+  void* d_scratch = nullptr;  // Scratch record
+  uint32_t* d_idx = nullptr;  // 3 * idx_cap per-curve index lists
+  size_t idx_cap = 0;
+  int batched_block = 256;
+  int batched_grid = 0;
   std::mutex mu;
+};
+
+struct sigops_plan {
+  sigops_ctx* ctx = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
 };
 
 namespace {
@@ -112,6 +124,52 @@ int ensure_buffers(sigops_ctx* c, size_t bytes) {
     c->h_cap = bytes;
   }
   return SIGOPS_OK;
+}
+
+int ensure_device(sigops_ctx* c, size_t bytes) {
+  bytes = (bytes + 255) & ~(size_t)255;
+  if (bytes <= c->d_cap) return SIGOPS_OK;
+  if (c->d_buf) cudaFree(c->d_buf);
+  c->d_buf = nullptr;
+  c->d_cap = 0;
+  if (cudaMalloc(&c->d_buf, bytes) != cudaSuccess) return fail(SIGOPS_E_NOMEM, "cudaMalloc(%zu) failed", bytes);
+  c->d_cap = bytes;
+  return SIGOPS_OK;
+}
+
+bool is_pinned(const void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeHost;
+}
+
+int ensure_idx(sigops_ctx* c, size_t n) {
+  if (n <= c->idx_cap) return SIGOPS_OK;
+  if (c->d_idx) cudaFree(c->d_idx);
+  c->d_idx = nullptr;
+  c->idx_cap = 0;
+  if (cudaMalloc(&c->d_idx, 3 * n * sizeof(uint32_t)) != cudaSuccess) return fail(SIGOPS_E_NOMEM, "cudaMalloc(index lists, %zu)", n);
+  c->idx_cap = n;
+  return SIGOPS_OK;
+}
+
+int set_batched_block(sigops_ctx* c, int block) {
+  int bps = batched_max_blocks_per_sm(block);
+  if (bps <= 0) return fail(SIGOPS_E_INVAL, "unsupported batched block size %d", block);
+  c->batched_block = block;
+  c->batched_grid = c->num_sms * bps;
+  return SIGOPS_OK;
+}
+
+cudaError_t launch_mixed(sigops_ctx* c, const uint8_t* curves, const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks, size_t n,
+                         uint8_t* out, uint8_t* status, cudaStream_t s) {
+  size_t cg = (n + 255) / 256;
+  int classify_grid = (int)(cg < (size_t)c->num_sms * 8 ? cg : (size_t)c->num_sms * 8);
+  return launch_batched(curves, sigs, msgs, pks, n, out, status, c->d_idx, c->d_scratch, c->d_gtab[0], c->d_gtab[1], c->d_gtab[2], c->d_err,
+                        c->batched_grid, c->batched_block, classify_grid, s);
 }
 
 int check_device_errors(sigops_ctx* c) {
@@ -233,6 +291,11 @@ sigops_ctx* sigops_create(int device) {
     c->grid[k] = c->num_sms * (bps > 0 ? bps : 1);
   }
   if ((e = cudaMalloc(&c->d_err, sizeof(uint32_t))) != cudaSuccess) return bail("cudaMalloc(err)", e);
+  if ((e = cudaMalloc(&c->d_scratch, batched_scratch_bytes())) != cudaSuccess) return bail("cudaMalloc(scratch)", e);
+  if (set_batched_block(c, 256) != SIGOPS_OK) {
+    sigops_destroy(c);
+    return nullptr;
+  }
   if ((e = cudaMemset(c->d_err, 0, sizeof(uint32_t))) != cudaSuccess) return bail("memset", e);
   return c;
 }
@@ -244,6 +307,8 @@ void sigops_destroy(sigops_ctx* c) {
   for (int k = 0; k < 3; ++k)
     if (c->d_gtab[k]) cudaFree(c->d_gtab[k]);
   if (c->d_err) cudaFree(c->d_err);
+  if (c->d_scratch) cudaFree(c->d_scratch);
+  if (c->d_idx) cudaFree(c->d_idx);
   if (c->d_buf) cudaFree(c->d_buf);
   if (c->h_buf) cudaFreeHost(c->h_buf);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -336,6 +401,156 @@ int sigops_plain_device(sigops_ctx* ctx, int curve, const uint8_t* d_sigs, const
   return SIGOPS_OK;
 }
 
+int sigops_reserve(sigops_ctx* ctx, size_t n) {
+  sigops_ctx* c = resolve(ctx);
+  if (!c) return SIGOPS_E_NODEV;
+  std::lock_guard<std::mutex> g(c->mu);
+  SG_CUDA(cudaSetDevice(c->device));
+  return ensure_idx(c, n);
+}
+
+int sigops_verify_mixed_device(sigops_ctx* ctx, const uint8_t* d_curves, const uint8_t* d_sigs, const uint8_t* d_msgs, const uint8_t* d_pks,
+                               size_t n, uint8_t* d_out, uint8_t* d_status, void* stream) {
+  if (n == 0) return SIGOPS_OK;
+  auto misaligned = [](const void* p) { return ((uintptr_t)p & 15u) != 0; };
+  if (!d_curves || !d_sigs || !d_msgs || !d_pks || !d_out || !d_status) return fail(SIGOPS_E_INVAL, "null device buffer");
+  if (misaligned(d_sigs) || misaligned(d_msgs) || misaligned(d_pks) || misaligned(d_out))
+    return fail(SIGOPS_E_INVAL, "device buffers must be 16-byte aligned");
+  sigops_ctx* c = resolve(ctx);
+  if (!c) return SIGOPS_E_NODEV;
+  std::lock_guard<std::mutex> g(c->mu);
+  SG_CUDA(cudaSetDevice(c->device));
+  int rc = ensure_idx(c, n);
+  if (rc) return rc;
+  SG_CUDA(launch_mixed(c, d_curves, d_sigs, d_msgs, d_pks, n, d_out, d_status, stream ? (cudaStream_t)stream : c->stream));
+  return SIGOPS_OK;
+}
+
+int sigops_verify_mixed(sigops_ctx* ctx, const uint8_t* curves, const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks, size_t n,
+                        uint8_t* out, uint8_t* out_status) {
+  if (n == 0) return SIGOPS_OK;
+  if (!curves || !sigs || !msgs || !pks || !out) return fail(SIGOPS_E_INVAL, "null buffer");
+  for (size_t i = 0; i < n; ++i)
+    if (curves[i] > 2) return fail(SIGOPS_E_INVAL, "item %zu has unknown curve tag %u", i, (unsigned)curves[i]);
+  sigops_ctx* c = resolve(ctx);
+  if (!c) return SIGOPS_E_NODEV;
+  std::lock_guard<std::mutex> g(c->mu);
+  SG_CUDA(cudaSetDevice(c->device));
+  auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+  const size_t o_sig = 0, o_msg = al(n * 64), o_pk = o_msg + al(n * 32), o_cur = o_pk + al(n * 32), o_out = o_cur + al(n),
+               o_st = o_out + al(n * 64), total = o_st + al(n);
+  // caller buffers that are page-locked go straight to / from the device
+  const bool pinned = is_pinned(sigs) && is_pinned(msgs) && is_pinned(pks) && is_pinned(curves) && is_pinned(out) &&
+                      (!out_status || is_pinned(out_status));
+  int rc = pinned ? ensure_device(c, total) : ensure_buffers(c, total);
+  if (rc) return rc;
+  rc = ensure_idx(c, n);
+  if (rc) return rc;
+  if (pinned) {
+    SG_CUDA(cudaMemcpyAsync(c->d_buf + o_sig, sigs, n * 64, cudaMemcpyHostToDevice, c->stream));
+    SG_CUDA(cudaMemcpyAsync(c->d_buf + o_msg, msgs, n * 32, cudaMemcpyHostToDevice, c->stream));
+    SG_CUDA(cudaMemcpyAsync(c->d_buf + o_pk, pks, n * 32, cudaMemcpyHostToDevice, c->stream));
+    SG_CUDA(cudaMemcpyAsync(c->d_buf + o_cur, curves, n, cudaMemcpyHostToDevice, c->stream));
+  } else {
+    memcpy(c->h_buf + o_sig, sigs, n * 64);
+    memcpy(c->h_buf + o_msg, msgs, n * 32);
+    memcpy(c->h_buf + o_pk, pks, n * 32);
+    memcpy(c->h_buf + o_cur, curves, n);
+    SG_CUDA(cudaMemcpyAsync(c->d_buf, c->h_buf, o_out, cudaMemcpyHostToDevice, c->stream));
+  }
+  SG_CUDA(launch_mixed(c, c->d_buf + o_cur, c->d_buf + o_sig, c->d_buf + o_msg, c->d_buf + o_pk, n, c->d_buf + o_out, c->d_buf + o_st,
+                       c->stream));
+  if (pinned) {
+    SG_CUDA(cudaMemcpyAsync(out, c->d_buf + o_out, n * 64, cudaMemcpyDeviceToHost, c->stream));
+    if (out_status) SG_CUDA(cudaMemcpyAsync(out_status, c->d_buf + o_st, n, cudaMemcpyDeviceToHost, c->stream));
+    return check_device_errors(c);
+  }
+  SG_CUDA(cudaMemcpyAsync(c->h_buf + o_out, c->d_buf + o_out, total - o_out, cudaMemcpyDeviceToHost, c->stream));
+  rc = check_device_errors(c);
+  if (rc) return rc;
+  memcpy(out, c->h_buf + o_out, n * 64);
+  if (out_status) memcpy(out_status, c->h_buf + o_st, n);
+  return SIGOPS_OK;
+}
+
+int sigops_mixed_plan_create(sigops_ctx* ctx, const uint8_t* d_curves, const uint8_t* d_sigs, const uint8_t* d_msgs, const uint8_t* d_pks,
+                             size_t n, uint8_t* d_out, uint8_t* d_status, sigops_plan** plan_out) {
+  if (!plan_out || n == 0) return fail(SIGOPS_E_INVAL, "plan needs n > 0 and an output pointer");
+  sigops_ctx* c = resolve(ctx);
+  if (!c) return SIGOPS_E_NODEV;
+  std::lock_guard<std::mutex> g(c->mu);
+  SG_CUDA(cudaSetDevice(c->device));
+  int rc = ensure_idx(c, n);
+  if (rc) return rc;
+  sigops_plan* p = new sigops_plan();
+  p->ctx = c;
+  cudaStream_t cs;
+  SG_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+  cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess) {
+    cudaError_t le = launch_mixed(c, d_curves, d_sigs, d_msgs, d_pks, n, d_out, d_status, cs);
+    e = cudaStreamEndCapture(cs, &p->graph);
+    if (le != cudaSuccess) e = le;
+  }
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&p->exec, p->graph, 0);
+  cudaStreamDestroy(cs);
+  if (e != cudaSuccess) {
+    if (p->graph) cudaGraphDestroy(p->graph);
+    delete p;
+    return fail(SIGOPS_E_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
+  }
+  *plan_out = p;
+  return SIGOPS_OK;
+}
+
+int sigops_mixed_plan_launch(sigops_plan* p, void* stream) {
+  if (!p) return fail(SIGOPS_E_INVAL, "null plan");
+  SG_CUDA(cudaSetDevice(p->ctx->device));
+  SG_CUDA(cudaGraphLaunch(p->exec, stream ? (cudaStream_t)stream : p->ctx->stream));
+  return SIGOPS_OK;
+}
+
+void sigops_mixed_plan_destroy(sigops_plan* p) {
+  if (!p) return;
+  cudaSetDevice(p->ctx->device);
+  if (p->exec) cudaGraphExecDestroy(p->exec);
+  if (p->graph) cudaGraphDestroy(p->graph);
+  delete p;
+}
+
+int sigops_set_batched_block(sigops_ctx* ctx, int block) {
+  sigops_ctx* c = resolve(ctx);
+  if (!c) return SIGOPS_E_NODEV;
+  std::lock_guard<std::mutex> g(c->mu);
+  return set_batched_block(c, block);
+}
+
+int sigops_workload_sign_ecdsa(sigops_ctx* ctx, int curve, const uint8_t* d_secrets, const uint8_t* d_nonces, const uint8_t* d_msgs, size_t n,
+                               uint8_t* d_sigs, uint8_t* d_pubkeys, uint8_t* d_status, void* stream) {
+  if (curve != SIGOPS_SECP256K1 && curve != SIGOPS_SECP256R1) return fail(SIGOPS_E_INVAL, "ECDSA curve expected");
+  if (n == 0) return SIGOPS_OK;
+  if (!d_secrets || !d_nonces || !d_msgs || !d_sigs || !d_pubkeys || !d_status) return fail(SIGOPS_E_INVAL, "null device buffer");
+  sigops_ctx* c = resolve(ctx);
+  if (!c) return SIGOPS_E_NODEV;
+  std::lock_guard<std::mutex> g(c->mu);
+  SG_CUDA(cudaSetDevice(c->device));
+  SG_CUDA(launch_sign_ecdsa(curve, d_secrets, d_nonces, d_msgs, n, c->d_gtab[curve], d_sigs, d_pubkeys, d_status, c->d_err, c->grid[curve],
+                            stream ? (cudaStream_t)stream : c->stream));
+  return SIGOPS_OK;
+}
+
+int sigops_workload_sign_ed25519(sigops_ctx* ctx, const uint8_t* d_seeds, const uint8_t* d_msgs, size_t n, uint8_t* d_sigs, uint8_t* d_pks,
+                                 void* stream) {
+  if (n == 0) return SIGOPS_OK;
+  if (!d_seeds || !d_msgs || !d_sigs || !d_pks) return fail(SIGOPS_E_INVAL, "null device buffer");
+  sigops_ctx* c = resolve(ctx);
+  if (!c) return SIGOPS_E_NODEV;
+  std::lock_guard<std::mutex> g(c->mu);
+  SG_CUDA(cudaSetDevice(c->device));
+  SG_CUDA(launch_sign_ed(d_seeds, d_msgs, n, c->d_gtab[2], d_sigs, d_pks, c->d_err, c->grid[2], stream ? (cudaStream_t)stream : c->stream));
+  return SIGOPS_OK;
+}
+
 int sigops_sync(sigops_ctx* ctx) {
   sigops_ctx* c = resolve(ctx);
   if (!c) return SIGOPS_E_NODEV;
@@ -376,6 +591,7 @@ int sigops_probe_imad(sigops_ctx* ctx, double* rate) {
 int sigops_device_info(sigops_ctx* ctx, int* num_sms, int* g1, int* g2, int* g3) {
   sigops_ctx* c = resolve(ctx);
   if (!c) return SIGOPS_E_NODEV;
+  (void)0;
   if (num_sms) *num_sms = c->num_sms;
   if (g1) *g1 = c->grid[0];
   if (g2) *g2 = c->grid[1];

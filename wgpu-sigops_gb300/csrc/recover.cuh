@@ -74,7 +74,7 @@ SG_HD APoint load_apoint(const uint32_t* t, uint32_t idx) {
 // u1 * G + u2 * R, signed fixed windows, one shared doubling chain.
 // gtab: multiples 1..ECDSA_GTAB of G, affine, field representation.
 template <class T>
-SG_HD JPoint ecdsa_lincomb(const u256& u1, const u256& u2, const APoint& R, const uint32_t* gtab) {
+SG_NOINL JPoint ecdsa_lincomb(const u256 u1, const u256 u2, const APoint R, const uint32_t* gtab) {
   using W = Weier<typename T::F, T::A_M3>;
   constexpr int NR = 1 << (ECDSA_WR - 1);
   JPoint tab[NR];
@@ -170,12 +170,8 @@ SG_HD EAffNiels load_eniels(const uint32_t* t, uint32_t idx) {
   return a;
 }
 
-// k = SHA-512(R || A || M) mod l  (src/wgsl/ed25519_reduce_fr.wgsl:88-125)
-SG_HD u256 ed_challenge(const uint32_t sig[16], const uint32_t pk[8], const uint32_t msg[8]) {
-  uint32_t m[24], h[16];
-#pragma unroll
-  for (int k = 0; k < 8; ++k) { m[k] = sig[k]; m[8 + k] = pk[k]; m[16 + k] = msg[k]; }
-  sha512_96(m, h);
+// 64-byte little-endian digest mod l (src/wgsl/ed25519_reduce_fr.wgsl:88-125)
+SG_HD u256 reduce512_mod_l(const uint32_t h[16]) {
   u256 lo, hi;
 #pragma unroll
   for (int k = 0; k < 8; ++k) { lo.w[k] = h[k]; hi.w[k] = h[8 + k]; }
@@ -185,8 +181,18 @@ SG_HD u256 ed_challenge(const uint32_t sig[16], const uint32_t pk[8], const uint
   return ScEd::to_int(t);
 }
 
+// k = SHA-512(R || A || M) mod l
+SG_HD u256 ed_challenge(const uint32_t sig[16], const uint32_t pk[8], const uint32_t msg[8]) {
+  uint32_t m[24], h[16];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) { m[k] = sig[k]; m[8 + k] = pk[k]; m[16 + k] = msg[k]; }
+  sha512_96(m, h);
+  return reduce512_mod_l(h);
+}
+
 // [s]B + [k](-A), signed fixed windows; btab: multiples 1..ED_GTAB of B (affine Niels)
-SG_HD EPoint ed_lincomb(const u256& s, const u256& k, const EPoint& negA, const uint32_t* btab) {
+template <int = 0>
+SG_NOINL EPoint ed_lincomb(const u256 s, const u256 k, const EPoint negA, const uint32_t* btab) {
   constexpr int NR = 1 << (ED_WR - 1);
   ENiels tab[NR];
   EPoint cur = negA;
@@ -251,7 +257,7 @@ SG_HD uint8_t ed25519_verify(const uint32_t sig[16], const uint32_t msg[8], cons
   negA.Y = A.Y;
   negA.Z = A.Z;
   negA.T = FpEd::neg(A.T);
-  EPoint Rp = ed_lincomb(s, k, negA, btab);
+  EPoint Rp = ed_lincomb<>(s, k, negA, btab);
   u256 enc = Edw::compress(Rp);
   return u256_eq(enc, renc) ? ST_OK : ST_MISMATCH;
 }

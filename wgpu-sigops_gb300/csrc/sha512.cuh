@@ -1,4 +1,5 @@
-// SHA-512 of the 96-byte ed25519 challenge preimage R || A || M (one block).
+// One-block SHA-512: the 96-byte ed25519 challenge preimage R || A || M, and
+// the 32- and 64-byte inputs of RFC 8032 signing (workload generation).
 //
 // Replaces src/wgsl/sha512.wgsl:1-194 (`sha512_96`, 64-bit words emulated as
 // vec2<u32>); here 64-bit words are native and the 80 rounds are unrolled with
@@ -12,9 +13,12 @@ namespace sg {
 
 SG_HD uint64_t rotr64(uint64_t x, int n) { return (x >> n) | (x << (64 - n)); }
 
-// m: the 96 input bytes as 24 little-endian u32 words (as loaded from memory).
+// One-block SHA-512 of NB bytes (NB a multiple of 8, at most 104).
+// m: the input bytes as NB/4 little-endian u32 words (as loaded from memory).
 // out: the 64-byte digest as 16 little-endian u32 words (digest byte order).
-SG_HD void sha512_96(const uint32_t m[24], uint32_t out[16]) {
+template <int NB>
+SG_HD void sha512_fixed(const uint32_t* m, uint32_t out[16]) {
+  static_assert(NB % 8 == 0 && NB <= 104, "one-block input");
   const uint64_t K[80] = {
     0x428a2f98d728ae22ull, 0x7137449123ef65cdull, 0xb5c0fbcfec4d3b2full, 0xe9b5dba58189dbbcull,
     0x3956c25bf348b538ull, 0x59f111f1b605d019ull, 0x923f82a4af194f9bull, 0xab1c5ed5da6d8118ull,
@@ -39,16 +43,19 @@ SG_HD void sha512_96(const uint32_t m[24], uint32_t out[16]) {
   };
   uint64_t w[16];
 #pragma unroll
-  for (int i = 0; i < 12; ++i) {
-    uint32_t hi = m[2 * i], lo = m[2 * i + 1];
-    hi = (hi >> 24) | ((hi >> 8) & 0xff00u) | ((hi << 8) & 0xff0000u) | (hi << 24);
-    lo = (lo >> 24) | ((lo >> 8) & 0xff00u) | ((lo << 8) & 0xff0000u) | (lo << 24);
-    w[i] = ((uint64_t)hi << 32) | lo;
+  for (int i = 0; i < 16; ++i) {
+    if (i < NB / 8) {
+      uint32_t hi = m[2 * i], lo = m[2 * i + 1];
+      hi = (hi >> 24) | ((hi >> 8) & 0xff00u) | ((hi << 8) & 0xff0000u) | (hi << 24);
+      lo = (lo >> 24) | ((lo >> 8) & 0xff00u) | ((lo << 8) & 0xff0000u) | (lo << 24);
+      w[i] = ((uint64_t)hi << 32) | lo;
+    } else if (i == NB / 8) {
+      w[i] = 0x8000000000000000ull;
+    } else {
+      w[i] = 0;
+    }
   }
-  w[12] = 0x8000000000000000ull;
-  w[13] = 0;
-  w[14] = 0;
-  w[15] = 768;
+  w[15] = (uint64_t)NB * 8;
   const uint64_t H0[8] = { 0x6a09e667f3bcc908ull, 0xbb67ae8584caa73bull, 0x3c6ef372fe94f82bull, 0xa54ff53a5f1d36f1ull, 0x510e527fade682d1ull, 0x9b05688c2b3e6c1full, 0x1f83d9abfb41bd6bull, 0x5be0cd19137e2179ull };
   uint64_t a = H0[0], b = H0[1], c = H0[2], d = H0[3], e = H0[4], f = H0[5], g = H0[6], h = H0[7];
 #pragma unroll
@@ -80,5 +87,8 @@ SG_HD void sha512_96(const uint32_t m[24], uint32_t out[16]) {
     out[2 * i + 1] = (lo >> 24) | ((lo >> 8) & 0xff00u) | ((lo << 8) & 0xff0000u) | (lo << 24);
   }
 }
+
+// the ed25519 challenge preimage R || A || M
+SG_HD void sha512_96(const uint32_t m[24], uint32_t out[16]) { sha512_fixed<96>(m, out); }
 
 }  // namespace sg

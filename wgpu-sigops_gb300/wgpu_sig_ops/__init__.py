@@ -13,4 +13,4 @@ class ShaderFailureError(RuntimeError):
     """Raised when a batch call fails as a whole (src/lib.rs:12-14)."""
 
 
-from . import ed25519_eddsa, precompute, secp256k1_ecdsa, secp256r1_ecdsa  # noqa: E402,F401
+from . import batch, ed25519_eddsa, precompute, secp256k1_ecdsa, secp256r1_ecdsa  # noqa: E402,F401

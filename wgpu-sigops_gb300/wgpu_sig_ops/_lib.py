@@ -49,6 +49,15 @@ SIGNATURES = {
     "sigops_ed25519_ecverify": (ctypes.c_int, [_vp, _vp, _vp, _vp, _sz, _u32p, _sz, ctypes.c_uint32, _vp, _vp]),
     "sigops_ed25519_ecverify_single": (ctypes.c_int, [_vp, _vp, _vp, _vp, _sz, ctypes.c_uint32, _vp, _vp]),
     "sigops_plain_device": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp, _vp, _sz, _vp, _vp, _vp]),
+    "sigops_verify_mixed": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _sz, _vp, _vp]),
+    "sigops_verify_mixed_device": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _sz, _vp, _vp, _vp]),
+    "sigops_reserve": (ctypes.c_int, [_vp, _sz]),
+    "sigops_mixed_plan_create": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _sz, _vp, _vp, ctypes.POINTER(_vp)]),
+    "sigops_mixed_plan_launch": (ctypes.c_int, [_vp, _vp]),
+    "sigops_mixed_plan_destroy": (None, [_vp]),
+    "sigops_set_batched_block": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "sigops_workload_sign_ecdsa": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp, _vp, _sz, _vp, _vp, _vp, _vp]),
+    "sigops_workload_sign_ed25519": (ctypes.c_int, [_vp, _vp, _vp, _sz, _vp, _vp, _vp]),
     "sigops_sync": (ctypes.c_int, [_vp]),
     "sigops_probe_imad": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_double)]),
     "sigops_device_info": (ctypes.c_int, [_vp] + [ctypes.POINTER(ctypes.c_int)] * 4),
