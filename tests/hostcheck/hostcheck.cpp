@@ -115,3 +115,11 @@ extern "C" void hc_ed_sign(const uint8_t* seed, const uint8_t* msg, uint8_t* sig
   ed25519_sign(sd, m, g_ed, s, p);
   memcpy(sig, s, 64); memcpy(pk, p, 32);
 }
+
+extern "C" void hc_sqr_wide(const uint8_t* a, uint8_t* out64) {
+  uint32_t t[16];
+  u256 x;
+  memcpy(x.w, a, 32);
+  sqr_wide(t, x);
+  memcpy(out64, t, 64);
+}

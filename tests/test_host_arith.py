@@ -46,6 +46,16 @@ def test_mul_wide(hc):
         assert int.from_bytes(out.raw, "little") == a * b
 
 
+def test_sqr_wide(hc):
+    rng = random.Random(6)
+    cases = [2**256 - 1, 0, 1, 2**255, 2**32 - 1] + [rng.getrandbits(256) for _ in range(500)]
+    cases += [sum(rng.choice([0, 0xFFFFFFFF]) << (32 * k) for k in range(8)) for _ in range(100)]
+    for a in cases:
+        out = ctypes.create_string_buffer(64)
+        hc.hc_sqr_wide(le(a), out)
+        assert int.from_bytes(out.raw, "little") == a * a, hex(a)
+
+
 @pytest.mark.parametrize("field", range(6))
 @pytest.mark.parametrize("op", range(5))
 def test_field_ops(hc, field, op):

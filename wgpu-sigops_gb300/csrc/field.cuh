@@ -108,7 +108,7 @@ struct FpK1 {
   }
 
   SG_HD static u256 mul(const u256& a, const u256& b) { uint32_t t[16]; mul_wide(t, a, b); return reduce(t); }
-  SG_HD static u256 sqr(const u256& a) { uint32_t t[16]; mul_wide(t, a, a); return reduce(t); }
+  SG_HD static u256 sqr(const u256& a) { uint32_t t[16]; sqr_wide(t, a); return reduce(t); }
   SG_HD static u256 add(const u256& a, const u256& b) { return mod_add(a, b, P()); }
   SG_HD static u256 sub(const u256& a, const u256& b) { return mod_sub(a, b, P()); }
   SG_HD static u256 neg(const u256& a) { return mod_neg(a, P()); }
@@ -206,7 +206,7 @@ struct FpEd {
   }
 
   SG_HD static u256 mul(const u256& a, const u256& b) { uint32_t t[16]; mul_wide(t, a, b); return reduce(t); }
-  SG_HD static u256 sqr(const u256& a) { uint32_t t[16]; mul_wide(t, a, a); return reduce(t); }
+  SG_HD static u256 sqr(const u256& a) { uint32_t t[16]; sqr_wide(t, a); return reduce(t); }
   SG_HD static u256 add(const u256& a, const u256& b) { return mod_add(a, b, P()); }
   SG_HD static u256 sub(const u256& a, const u256& b) { return mod_sub(a, b, P()); }
   SG_HD static u256 neg(const u256& a) { return mod_neg(a, P()); }
