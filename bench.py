@@ -53,7 +53,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU-baseline sample duration")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--block", type=int, default=0, help="batched kernel block size (0 = library default)")
+    ap.add_argument("--variant", type=int, default=-1, help="batched kernel launch variant (-1 = library default)")
+    ap.add_argument("--plain-variant", type=int, default=-1, help="plain kernels launch variant (-1 = library default)")
     return ap.parse_args()
 
 
@@ -264,8 +265,11 @@ def main():
     from wgpu_sig_ops._lib import check, lib
 
     ctx = w.Context(dist.local)
-    if args.block:
-        check(lib.sigops_set_batched_block(ctx.ptr, args.block), "block")
+    if args.variant >= 0:
+        check(lib.sigops_set_variant(ctx.ptr, 3, args.variant), "variant")
+    if args.plain_variant >= 0:
+        for k in range(3):
+            check(lib.sigops_set_variant(ctx.ptr, k, args.plain_variant), "plain variant")
     info = ctx.device_info()
     imad_peak = max(ctx.probe_imad() for _ in range(3))
 
@@ -333,6 +337,13 @@ def main():
                                           st.data_ptr(), stream.cuda_stream), "plain")
 
     ms_p = timed(plain_step, max(3, args.steps // 2), 1)
+    per_curve = {}
+    for c, m, s_, mm, p, o, st, _ in parts:
+        def one(c=c, m=m, s_=s_, mm=mm, p=p, o=o, st=st):
+            check(lib.sigops_plain_device(ctx.ptr, c, s_.data_ptr(), mm.data_ptr(), p.data_ptr() if c == 2 else None, m, o.data_ptr(),
+                                          st.data_ptr(), stream.cuda_stream), "plain")
+        t = statistics.mean(timed(one, 3, 1))
+        per_curve[["secp256k1", "secp256r1", "ed25519"][c]] = {"n": m, "ms": t, "sigs_per_s": m / (t * 1e-3)}
     check(lib.sigops_sync(ctx.ptr), "plain run")
     plain_mismatch = 0
     for c, m, s, mm, p, o, st, sel in parts:
@@ -396,7 +407,7 @@ def main():
                    "parallelism": f"replicas x{dist.world} (weak scaling, no collective)"},
         "selfcheck": selfcheck,
         "plain": {"ms_per_step": plain_ms, "value": dist.sum(n) / (plain_ms * 1e-3), "batched_over_plain": plain_ms / ms_step,
-                  "outputs_equal_batched": plain_mismatch == 0},
+                  "outputs_equal_batched": plain_mismatch == 0, "per_curve": per_curve},
         "roofline": {"bound": "imad", "achieved": achieved / 1e12, "peak": imad_peak / 1e12, "unit": "TIMAD/s",
                      "frac": achieved / imad_peak, "traffic": traffic,
                      "peak_source": "measured in-process: mad.lo.u32 probe (MEASURED_PEAKS.json has no integer figure)",

@@ -171,8 +171,13 @@ int sigops_mixed_plan_create(sigops_ctx* ctx, const uint8_t* d_curves, const uin
 int sigops_mixed_plan_launch(sigops_plan* plan, void* stream);
 void sigops_mixed_plan_destroy(sigops_plan* plan);
 
-/* Threads per block of the persistent kernel (128 or 256). */
-int sigops_set_batched_block(sigops_ctx* ctx, int block);
+/* Launch-shape variants (the autotuner's search space).  kernel 0..2: the
+ * plain kernel of SIGOPS_SECP256K1 / SECP256R1 / ED25519, variant 0 = one
+ * 256-thread block per SM, 1 = two (register budget 128); kernel 3: the
+ * batched kernel, variant 0 = 256 threads x 1 block per SM, 1 = 256 x 2,
+ * 2 = 128 x 4.  sigops_get_variant also reports the grid and block used. */
+int sigops_set_variant(sigops_ctx* ctx, int kernel, int variant);
+int sigops_get_variant(sigops_ctx* ctx, int kernel, int* variant, int* grid, int* block);
 
 /* ------------------------------------------- synthetic workload signing */
 

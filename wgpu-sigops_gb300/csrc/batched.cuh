@@ -98,8 +98,8 @@ __device__ __forceinline__ bool stage_three(uint32_t* sk1, uint32_t* sr1, uint32
   return true;
 }
 
-template <int BLOCK>
-__global__ void __launch_bounds__(BLOCK) batched_kernel(MixedIO io, const uint32_t* __restrict__ idx, BatchTables tabs, Scratch* sc,
+template <int BLOCK, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB) batched_kernel(MixedIO io, const uint32_t* __restrict__ idx, BatchTables tabs, Scratch* sc,
                                                         uint32_t* err) {
   __shared__ __align__(128) uint32_t tk1[ECDSA_GTAB * 16];
   __shared__ __align__(128) uint32_t tr1[ECDSA_GTAB * 16];

@@ -197,8 +197,10 @@ struct Edw {
   using F = FpEd;
   SG_HD static EPoint identity() { EPoint r; r.X = F::zero(); r.Y = F::one(); r.Z = F::one(); r.T = F::zero(); return r; }
 
-  // dbl-2008-hwcd with a = -1: 4M + 4S
-  SG_HD static EPoint dbl(const EPoint& p) {
+  // dbl-2008-hwcd with a = -1: 4M + 4S; with need_t false the T coordinate
+  // is left stale (3M + 4S): only valid when the next operation is a doubling,
+  // which never reads T
+  SG_HD static EPoint dbl(const EPoint& p, bool need_t = true) {
     u256 A = F::sqr(p.X);
     u256 B = F::sqr(p.Y);
     u256 C = F::sqr(p.Z);
@@ -211,7 +213,7 @@ struct Edw {
     EPoint r;
     r.X = F::mul(E, Fv);
     r.Y = F::mul(G, H);
-    r.T = F::mul(E, H);
+    r.T = need_t ? F::mul(E, H) : p.T;
     r.Z = F::mul(Fv, G);
     return r;
   }

@@ -3,7 +3,7 @@
 //
 //  * FpK1  p = 2^256 - 2^32 - 977   special-form fold (2^256 = 2^32 + 977)
 //  * FpEd  p = 2^255 - 19           special-form fold (2^256 = 38)
-//  * FpR1  p = NIST P-256           Montgomery form, R = 2^256 (n0' = 1)
+//  * FpR1  p = NIST P-256           NIST fast reduction (signed word columns)
 //  * Mont<...> generic Montgomery (CIOS) for the scalar fields mod n and mod l
 //
 // The reference does all of this with 13-bit limbs: Barrett `ff_mul`
@@ -382,26 +382,78 @@ struct EdScalarC {
   static constexpr uint32_t NINV = 0x12547e1bu;
 };
 
-struct R1BaseC {
-  SG_HD static u256 N() { return SG_U256(0xffffffffu, 0xffffffffu, 0xffffffffu, 0x00000000u, 0x00000000u, 0x00000000u, 0x00000001u, 0xffffffffu); }
-  SG_HD static u256 R2() { return SG_U256(0x00000003u, 0x00000000u, 0xffffffffu, 0xfffffffbu, 0xfffffffeu, 0xffffffffu, 0xfffffffdu, 0x00000004u); }
-  SG_HD static u256 ONE_MONT() { return SG_U256(0x00000001u, 0x00000000u, 0x00000000u, 0xffffffffu, 0xffffffffu, 0xffffffffu, 0xfffffffeu, 0x00000000u); }
-  SG_HD static u256 N_MINUS_2() { return SG_U256(0xfffffffdu, 0xffffffffu, 0xffffffffu, 0x00000000u, 0x00000000u, 0x00000000u, 0x00000001u, 0xffffffffu); }
-  static constexpr uint32_t NINV = 0x1u;
-};
-
 using ScK1 = Mont<K1ScalarC>;
 using ScR1 = Mont<R1ScalarC>;
 using ScEd = Mont<EdScalarC>;
 
 // ---------------------------------------------------------------------------
-// P-256 base field: Montgomery form with addition chains for inverse / sqrt
+// P-256 base field: the NIST fast reduction (FIPS 186-4 D.2.3) on the 512-bit
+// product.  p = 2^256 - 2^224 + 2^192 + 2^96 - 1, so each result word is a
+// signed sum of product words (s1 + 2 s2 + 2 s3 + s4 + s5 - s6 - s7 - s8 - s9);
+// the sums run in 64-bit columns, then the signed top carry t (|t| <= 6) is
+// folded twice with 2^256 = 2^224 - 2^192 - 2^96 + 1.  No multiplications in
+// the reduction: it runs on the integer ALU while the products use IMAD.
 // ---------------------------------------------------------------------------
-struct FpR1 : Mont<R1BaseC> {
-  using B = Mont<R1BaseC>;
-  SG_HD static u256 P() { return R1BaseC::N(); }
-  SG_HD static u256 from_int(const u256& x) { return B::from_int(reduce_once(x, P())); }
-  SG_HD static u256 curve_b() { return SG_U256(0x29c4bddfu, 0xd89cdf62u, 0x78843090u, 0xacf005cdu, 0xf7212ed6u, 0xe5a220abu, 0x04874834u, 0xdc30061du); }
+struct FpR1 {
+  SG_HD static u256 P() { return SG_U256(0xffffffffu, 0xffffffffu, 0xffffffffu, 0x00000000u, 0x00000000u, 0x00000000u, 0x00000001u, 0xffffffffu); }
+
+  // value = w + top * 2^256  ->  w + top * (2^224 - 2^192 - 2^96 + 1)
+  SG_HD static void fold(uint32_t w[8], int64_t& top) {
+    int64_t v = (int64_t)w[0] + top;
+    w[0] = (uint32_t)v; v >>= 32;
+    v += w[1]; w[1] = (uint32_t)v; v >>= 32;
+    v += w[2]; w[2] = (uint32_t)v; v >>= 32;
+    v += (int64_t)w[3] - top; w[3] = (uint32_t)v; v >>= 32;
+    v += w[4]; w[4] = (uint32_t)v; v >>= 32;
+    v += w[5]; w[5] = (uint32_t)v; v >>= 32;
+    v += (int64_t)w[6] - top; w[6] = (uint32_t)v; v >>= 32;
+    v += (int64_t)w[7] + top; w[7] = (uint32_t)v; v >>= 32;
+    top = v;
+  }
+
+  SG_HD static u256 reduce(const uint32_t c[16]) {
+    typedef int64_t I;
+    I t[8];
+    t[0] = (I)c[0] + c[8] + c[9] - c[11] - c[12] - c[13] - c[14];
+    t[1] = (I)c[1] + c[9] + c[10] - c[12] - c[13] - c[14] - c[15];
+    t[2] = (I)c[2] + c[10] + c[11] - c[13] - c[14] - c[15];
+    t[3] = (I)c[3] + 2 * (I)c[11] + 2 * (I)c[12] + c[13] - c[15] - c[8] - c[9];
+    t[4] = (I)c[4] + 2 * (I)c[12] + 2 * (I)c[13] + c[14] - c[9] - c[10];
+    t[5] = (I)c[5] + 2 * (I)c[13] + 2 * (I)c[14] + c[15] - c[10] - c[11];
+    t[6] = (I)c[6] + 3 * (I)c[14] + 2 * (I)c[15] + c[13] - c[8] - c[9];
+    t[7] = (I)c[7] + 3 * (I)c[15] + c[8] - c[10] - c[11] - c[12] - c[13];
+    uint32_t w[8];
+    I v = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      v += t[k];
+      w[k] = (uint32_t)v;
+      v >>= 32;
+    }
+    fold(w, v);  // |v| <= 6 -> v in {-1, 0, 1}
+    fold(w, v);  // -> v == 0, value in [0, 2^256)
+    u256 r;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) r.w[k] = w[k];
+    return reduce_once(r, P());
+  }
+
+  SG_HD static u256 mul(const u256& a, const u256& b) { uint32_t t[16]; mul_wide(t, a, b); return reduce(t); }
+  SG_HD static u256 sqr(const u256& a) { uint32_t t[16]; sqr_wide(t, a); return reduce(t); }
+  SG_HD static u256 add(const u256& a, const u256& b) { return mod_add(a, b, P()); }
+  SG_HD static u256 sub(const u256& a, const u256& b) { return mod_sub(a, b, P()); }
+  SG_HD static u256 neg(const u256& a) { return mod_neg(a, P()); }
+  SG_HD static u256 one() { return u256_small(1); }
+  SG_HD static u256 zero() { return u256_zero(); }
+  SG_HD static u256 from_int(const u256& x) { return reduce_once(x, P()); }  // x < 2^256
+  SG_HD static u256 to_int(const u256& a) { return a; }
+  SG_HD static u256 curve_b() { return SG_U256(0x27d2604bu, 0x3bce3c3eu, 0xcc53b0f6u, 0x651d06b0u, 0x769886bcu, 0xb3ebbd55u, 0xaa3a93e7u, 0x5ac635d8u); }
+
+  SG_HD static u256 sqr_n(u256 a, int n) {
+#pragma unroll 1
+    for (int i = 0; i < n; ++i) a = sqr(a);
+    return a;
+  }
 
   // x2, x4, x8, x16, x32 blocks: a^(2^k - 1)
   SG_HD static void blocks(const u256 a, u256& x2, u256& x4, u256& x8, u256& x16, u256& x32) {

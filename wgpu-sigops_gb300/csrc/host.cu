@@ -83,7 +83,8 @@ struct sigops_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   int num_sms = 0;
-  int grid[3] = {0, 0, 0};
+  int grid[3] = {0, 0, 0};     // plain kernels: blocks per launch, per curve
+  int variant[3] = {0, 0, 0};  // plain kernel variant per curve
   uint32_t* d_gtab[3] = {nullptr, nullptr, nullptr};
   uint32_t* d_err = nullptr;
   uint8_t* d_buf = nullptr;  // inputs then outputs of host-buffer calls
@@ -94,7 +95,7 @@ struct sigops_ctx {
   void* d_scratch = nullptr;  // Scratch record
   uint32_t* d_idx = nullptr;  // 3 * idx_cap per-curve index lists
   size_t idx_cap = 0;
-  int batched_block = 256;
+  int batched_variant = 0;
   int batched_grid = 0;
   std::mutex mu;
 };
@@ -156,12 +157,25 @@ int ensure_idx(sigops_ctx* c, size_t n) {
   return SIGOPS_OK;
 }
 
-int set_batched_block(sigops_ctx* c, int block) {
-  int bps = batched_max_blocks_per_sm(block);
-  if (bps <= 0) return fail(SIGOPS_E_INVAL, "unsupported batched block size %d", block);
-  c->batched_block = block;
-  c->batched_grid = c->num_sms * bps;
-  return SIGOPS_OK;
+// kernel 0..2: plain kernel of that curve; 3: batched engine
+int set_variant(sigops_ctx* c, int kernel, int variant) {
+  if (kernel >= 0 && kernel < 3) {
+    if (variant < 0 || variant >= PLAIN_VARIANTS) return fail(SIGOPS_E_INVAL, "plain variant %d out of range", variant);
+    int bps = plain_max_blocks_per_sm(kernel, variant);
+    if (bps <= 0) return fail(SIGOPS_E_CUDA, "plain kernel %d variant %d cannot launch", kernel, variant);
+    c->variant[kernel] = variant;
+    c->grid[kernel] = c->num_sms * bps;
+    return SIGOPS_OK;
+  }
+  if (kernel == 3) {
+    if (variant < 0 || variant >= BATCHED_VARIANTS) return fail(SIGOPS_E_INVAL, "batched variant %d out of range", variant);
+    int bps = batched_max_blocks_per_sm(variant);
+    if (bps <= 0) return fail(SIGOPS_E_CUDA, "batched variant %d cannot launch", variant);
+    c->batched_variant = variant;
+    c->batched_grid = c->num_sms * bps;
+    return SIGOPS_OK;
+  }
+  return fail(SIGOPS_E_INVAL, "kernel id %d out of range", kernel);
 }
 
 cudaError_t launch_mixed(sigops_ctx* c, const uint8_t* curves, const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks, size_t n,
@@ -169,7 +183,7 @@ cudaError_t launch_mixed(sigops_ctx* c, const uint8_t* curves, const uint8_t* si
   size_t cg = (n + 255) / 256;
   int classify_grid = (int)(cg < (size_t)c->num_sms * 8 ? cg : (size_t)c->num_sms * 8);
   return launch_batched(curves, sigs, msgs, pks, n, out, status, c->d_idx, c->d_scratch, c->d_gtab[0], c->d_gtab[1], c->d_gtab[2], c->d_err,
-                        c->batched_grid, c->batched_block, classify_grid, s);
+                        c->batched_grid, c->batched_variant, classify_grid, s);
 }
 
 int check_device_errors(sigops_ctx* c) {
@@ -228,7 +242,7 @@ int run_host_call(sigops_ctx* ctx, int curve, const uint8_t* sigs, const uint8_t
   if (curve == SIGOPS_ED25519) memcpy(c->h_buf + l.pk, pks, n * 32);
   SG_CUDA(cudaMemcpyAsync(c->d_buf, c->h_buf, l.out, cudaMemcpyHostToDevice, c->stream));
   SG_CUDA(launch_plain(curve, c->d_buf + l.sig, c->d_buf + l.msg, c->d_buf + l.pk, n, c->d_gtab[curve], c->d_buf + l.out,
-                       c->d_buf + l.status, c->d_err, c->grid[curve], c->stream));
+                       c->d_buf + l.status, c->d_err, c->grid[curve], c->variant[curve], c->stream));
   SG_CUDA(cudaMemcpyAsync(c->h_buf + l.out, c->d_buf + l.out, l.total - l.out, cudaMemcpyDeviceToHost, c->stream));
   rc = check_device_errors(c);
   if (rc) return rc;
@@ -287,12 +301,14 @@ sigops_ctx* sigops_create(int device) {
     const auto& t = host_tables().gtab[k];
     if ((e = cudaMalloc(&c->d_gtab[k], t.size() * 4)) != cudaSuccess) return bail("cudaMalloc(table)", e);
     if ((e = cudaMemcpy(c->d_gtab[k], t.data(), t.size() * 4, cudaMemcpyHostToDevice)) != cudaSuccess) return bail("table upload", e);
-    int bps = plain_max_blocks_per_sm(k);
-    c->grid[k] = c->num_sms * (bps > 0 ? bps : 1);
+    if (set_variant(c, k, 0) != SIGOPS_OK) {
+      sigops_destroy(c);
+      return nullptr;
+    }
   }
   if ((e = cudaMalloc(&c->d_err, sizeof(uint32_t))) != cudaSuccess) return bail("cudaMalloc(err)", e);
   if ((e = cudaMalloc(&c->d_scratch, batched_scratch_bytes())) != cudaSuccess) return bail("cudaMalloc(scratch)", e);
-  if (set_batched_block(c, 256) != SIGOPS_OK) {
+  if (set_variant(c, 3, 0) != SIGOPS_OK) {
     sigops_destroy(c);
     return nullptr;
   }
@@ -397,7 +413,7 @@ int sigops_plain_device(sigops_ctx* ctx, int curve, const uint8_t* d_sigs, const
   std::lock_guard<std::mutex> g(c->mu);
   SG_CUDA(cudaSetDevice(c->device));
   cudaStream_t s = stream ? (cudaStream_t)stream : c->stream;
-  SG_CUDA(launch_plain(curve, d_sigs, d_msgs, d_pks, n, c->d_gtab[curve], d_out, d_status, c->d_err, c->grid[curve], s));
+  SG_CUDA(launch_plain(curve, d_sigs, d_msgs, d_pks, n, c->d_gtab[curve], d_out, d_status, c->d_err, c->grid[curve], c->variant[curve], s));
   return SIGOPS_OK;
 }
 
@@ -518,11 +534,30 @@ void sigops_mixed_plan_destroy(sigops_plan* p) {
   delete p;
 }
 
-int sigops_set_batched_block(sigops_ctx* ctx, int block) {
+int sigops_set_variant(sigops_ctx* ctx, int kernel, int variant) {
   sigops_ctx* c = resolve(ctx);
   if (!c) return SIGOPS_E_NODEV;
   std::lock_guard<std::mutex> g(c->mu);
-  return set_batched_block(c, block);
+  SG_CUDA(cudaSetDevice(c->device));
+  return set_variant(c, kernel, variant);
+}
+
+int sigops_get_variant(sigops_ctx* ctx, int kernel, int* variant, int* grid, int* block) {
+  sigops_ctx* c = resolve(ctx);
+  if (!c) return SIGOPS_E_NODEV;
+  if (kernel >= 0 && kernel < 3) {
+    if (variant) *variant = c->variant[kernel];
+    if (grid) *grid = c->grid[kernel];
+    if (block) *block = PLAIN_BLOCK;
+    return SIGOPS_OK;
+  }
+  if (kernel == 3) {
+    if (variant) *variant = c->batched_variant;
+    if (grid) *grid = c->batched_grid;
+    if (block) *block = batched_variant_block(c->batched_variant);
+    return SIGOPS_OK;
+  }
+  return fail(SIGOPS_E_INVAL, "kernel id %d out of range", kernel);
 }
 
 int sigops_workload_sign_ecdsa(sigops_ctx* ctx, int curve, const uint8_t* d_secrets, const uint8_t* d_nonces, const uint8_t* d_msgs, size_t n,

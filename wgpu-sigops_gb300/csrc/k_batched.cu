@@ -1,26 +1,32 @@
-// Batched mixed-curve engine: kernel instantiations and launchers.
+// Batched mixed-curve engine: classify kernel, variant dispatch.
 #include "batched.cuh"
 
 namespace sg {
 
-template <int BLOCK>
-static int occ() {
-  int b = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, batched_kernel<BLOCK>, BLOCK, 0);
-  return b;
-}
+int batched_occupancy_0();
+int batched_occupancy_1();
+int batched_occupancy_2();
+cudaError_t batched_launch_0(const MixedIO&, const uint32_t*, const BatchTables&, Scratch*, uint32_t*, int, cudaStream_t);
+cudaError_t batched_launch_1(const MixedIO&, const uint32_t*, const BatchTables&, Scratch*, uint32_t*, int, cudaStream_t);
+cudaError_t batched_launch_2(const MixedIO&, const uint32_t*, const BatchTables&, Scratch*, uint32_t*, int, cudaStream_t);
 
-int batched_max_blocks_per_sm(int block) {
-  switch (block) {
-    case 128: return occ<128>();
-    case 256: return occ<256>();
+// variants: 0 = 256 threads x 1 block/SM, 1 = 256 x 2, 2 = 128 x 4
+static const int kBlock[BATCHED_VARIANTS] = {256, 256, 128};
+
+int batched_variant_block(int v) { return (v >= 0 && v < BATCHED_VARIANTS) ? kBlock[v] : 0; }
+
+int batched_max_blocks_per_sm(int v) {
+  switch (v) {
+    case 0: return batched_occupancy_0();
+    case 1: return batched_occupancy_1();
+    case 2: return batched_occupancy_2();
     default: return 0;
   }
 }
 
 cudaError_t launch_batched(const uint8_t* curves, const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks, size_t n, uint8_t* out,
                            uint8_t* status, uint32_t* idx, void* scratch, const uint32_t* gk1, const uint32_t* gr1, const uint32_t* ged,
-                           uint32_t* err, int grid, int block, int classify_grid, cudaStream_t stream) {
+                           uint32_t* err, int grid, int variant, int classify_grid, cudaStream_t stream) {
   if (n == 0) return cudaSuccess;
   Scratch* sc = (Scratch*)scratch;
   cudaError_t e = cudaMemsetAsync(sc, 0, sizeof(Scratch), stream);
@@ -28,12 +34,12 @@ cudaError_t launch_batched(const uint8_t* curves, const uint8_t* sigs, const uin
   classify_kernel<<<classify_grid, 256, 0, stream>>>(curves, n, idx, sc);
   MixedIO io{curves, sigs, msgs, pks, out, status, n};
   BatchTables t{gk1, gr1, ged};
-  switch (block) {
-    case 128: batched_kernel<128><<<grid, 128, 0, stream>>>(io, idx, t, sc, err); break;
-    case 256: batched_kernel<256><<<grid, 256, 0, stream>>>(io, idx, t, sc, err); break;
+  switch (variant) {
+    case 0: return batched_launch_0(io, idx, t, sc, err, grid, stream);
+    case 1: return batched_launch_1(io, idx, t, sc, err, grid, stream);
+    case 2: return batched_launch_2(io, idx, t, sc, err, grid, stream);
     default: return cudaErrorInvalidValue;
   }
-  return cudaGetLastError();
 }
 
 size_t batched_scratch_bytes() { return sizeof(Scratch); }

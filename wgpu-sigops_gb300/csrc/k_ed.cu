@@ -3,7 +3,8 @@
 
 namespace sg {
 
-__global__ void __launch_bounds__(PLAIN_BLOCK) ed_plain_kernel(const uint8_t* __restrict__ sigs, const uint8_t* __restrict__ msgs,
+template <int MINB>
+__global__ void __launch_bounds__(PLAIN_BLOCK, MINB) ed_plain_kernel(const uint8_t* __restrict__ sigs, const uint8_t* __restrict__ msgs,
                                                                 const uint8_t* __restrict__ pks, size_t n, const uint32_t* __restrict__ btab,
                                                                 uint8_t* __restrict__ valid, uint8_t* __restrict__ status, uint32_t* err) {
   __shared__ __align__(128) uint32_t tab[ED_GTAB * 24];
@@ -22,14 +23,20 @@ __global__ void __launch_bounds__(PLAIN_BLOCK) ed_plain_kernel(const uint8_t* __
 }
 
 cudaError_t launch_plain_ed(const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks, size_t n, const uint32_t* btab, uint8_t* valid,
-                            uint8_t* status, uint32_t* err, int grid, cudaStream_t stream) {
-  ed_plain_kernel<<<grid, PLAIN_BLOCK, 0, stream>>>(sigs, msgs, pks, n, btab, valid, status, err);
+                            uint8_t* status, uint32_t* err, int grid, int variant, cudaStream_t stream) {
+  if (variant == 1)
+    ed_plain_kernel<2><<<grid, PLAIN_BLOCK, 0, stream>>>(sigs, msgs, pks, n, btab, valid, status, err);
+  else
+    ed_plain_kernel<1><<<grid, PLAIN_BLOCK, 0, stream>>>(sigs, msgs, pks, n, btab, valid, status, err);
   return cudaGetLastError();
 }
 
-int occupancy_plain_ed() {
+int occupancy_plain_ed(int variant) {
   int b = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, ed_plain_kernel, PLAIN_BLOCK, 0);
+  if (variant == 1)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, ed_plain_kernel<2>, PLAIN_BLOCK, 0);
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, ed_plain_kernel<1>, PLAIN_BLOCK, 0);
   return b;
 }
 

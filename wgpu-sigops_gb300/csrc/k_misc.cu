@@ -81,21 +81,21 @@ __global__ void imad_probe_kernel(uint32_t* out, uint32_t iters, uint32_t seed) 
 // launchers
 // ---------------------------------------------------------------------------
 cudaError_t launch_plain(int curve, const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks, size_t n, const uint32_t* gtab,
-                         uint8_t* out, uint8_t* status, uint32_t* err, int grid, cudaStream_t stream) {
+                         uint8_t* out, uint8_t* status, uint32_t* err, int grid, int variant, cudaStream_t stream) {
   if (n == 0) return cudaSuccess;
   switch (curve) {
-    case CURVE_SECP256K1: return launch_plain_k1(sigs, msgs, n, gtab, out, status, err, grid, stream);
-    case CURVE_SECP256R1: return launch_plain_r1(sigs, msgs, n, gtab, out, status, err, grid, stream);
-    case CURVE_ED25519: return launch_plain_ed(sigs, msgs, pks, n, gtab, out, status, err, grid, stream);
+    case CURVE_SECP256K1: return launch_plain_k1(sigs, msgs, n, gtab, out, status, err, grid, variant, stream);
+    case CURVE_SECP256R1: return launch_plain_r1(sigs, msgs, n, gtab, out, status, err, grid, variant, stream);
+    case CURVE_ED25519: return launch_plain_ed(sigs, msgs, pks, n, gtab, out, status, err, grid, variant, stream);
     default: return cudaErrorInvalidValue;
   }
 }
 
-int plain_max_blocks_per_sm(int curve) {
+int plain_max_blocks_per_sm(int curve, int variant) {
   switch (curve) {
-    case CURVE_SECP256K1: return occupancy_plain_k1();
-    case CURVE_SECP256R1: return occupancy_plain_r1();
-    case CURVE_ED25519: return occupancy_plain_ed();
+    case CURVE_SECP256K1: return occupancy_plain_k1(variant);
+    case CURVE_SECP256R1: return occupancy_plain_r1(variant);
+    case CURVE_ED25519: return occupancy_plain_ed(variant);
     default: return 0;
   }
 }

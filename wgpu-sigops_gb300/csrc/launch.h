@@ -12,27 +12,32 @@ constexpr int PLAIN_BLOCK = 256;
 enum : uint32_t { DEV_ERR_STAGE_TIMEOUT = 1u, DEV_ERR_MISALIGNED = 2u, DEV_ERR_QUEUE_TIMEOUT = 4u };
 
 cudaError_t launch_plain(int curve, const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks, size_t n, const uint32_t* gtab,
-                         uint8_t* out, uint8_t* status, uint32_t* err, int grid, cudaStream_t stream);
-int plain_max_blocks_per_sm(int curve);
+                         uint8_t* out, uint8_t* status, uint32_t* err, int grid, int variant, cudaStream_t stream);
+int plain_max_blocks_per_sm(int curve, int variant);
+// plain kernel variants: 0 = one 256-thread block per SM, 1 = two (128 registers)
+constexpr int PLAIN_VARIANTS = 2;
 cudaError_t launch_plain_k1(const uint8_t* sigs, const uint8_t* msgs, size_t n, const uint32_t* gtab, uint8_t* out, uint8_t* status,
-                            uint32_t* err, int grid, cudaStream_t stream);
+                            uint32_t* err, int grid, int variant, cudaStream_t stream);
 cudaError_t launch_plain_r1(const uint8_t* sigs, const uint8_t* msgs, size_t n, const uint32_t* gtab, uint8_t* out, uint8_t* status,
-                            uint32_t* err, int grid, cudaStream_t stream);
+                            uint32_t* err, int grid, int variant, cudaStream_t stream);
 cudaError_t launch_plain_ed(const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks, size_t n, const uint32_t* btab, uint8_t* valid,
-                            uint8_t* status, uint32_t* err, int grid, cudaStream_t stream);
-int occupancy_plain_k1();
-int occupancy_plain_r1();
-int occupancy_plain_ed();
+                            uint8_t* status, uint32_t* err, int grid, int variant, cudaStream_t stream);
+int occupancy_plain_k1(int variant);
+int occupancy_plain_r1(int variant);
+int occupancy_plain_ed(int variant);
 cudaError_t launch_sign_ecdsa(int curve, const uint8_t* secrets, const uint8_t* nonces, const uint8_t* msgs, size_t n, const uint32_t* gtab,
                               uint8_t* sigs, uint8_t* pubs, uint8_t* status, uint32_t* err, int grid, cudaStream_t stream);
 cudaError_t launch_sign_ed(const uint8_t* seeds, const uint8_t* msgs, size_t n, const uint32_t* btab, uint8_t* sigs, uint8_t* pks,
                            uint32_t* err, int grid, cudaStream_t stream);
-// batched mixed-curve engine: scratch = Scratch record + 3*n u32 index lists
-int batched_max_blocks_per_sm(int block);
+// batched mixed-curve engine: scratch = Scratch record + 3*n u32 index lists.
+// variants: 0 = 256 threads x 1 block/SM, 1 = 256 x 2, 2 = 128 x 4
+constexpr int BATCHED_VARIANTS = 3;
+int batched_variant_block(int variant);
+int batched_max_blocks_per_sm(int variant);
 size_t batched_scratch_bytes();
 cudaError_t launch_batched(const uint8_t* curves, const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks, size_t n, uint8_t* out,
                            uint8_t* status, uint32_t* idx, void* scratch, const uint32_t* gk1, const uint32_t* gr1, const uint32_t* ged,
-                           uint32_t* err, int grid, int block, int classify_grid, cudaStream_t stream);
+                           uint32_t* err, int grid, int variant, int classify_grid, cudaStream_t stream);
 cudaError_t launch_field_test(int field, int op, const void* a, const void* b, void* out, int n, cudaStream_t stream);
 cudaError_t launch_sha512_test(const void* in, void* out, int n, cudaStream_t stream);
 cudaError_t launch_imad_probe(uint32_t* out, uint32_t iters, int grid, int block, cudaStream_t stream);

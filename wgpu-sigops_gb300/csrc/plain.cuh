@@ -13,8 +13,8 @@
 
 namespace sg {
 
-template <class T>
-__global__ void __launch_bounds__(PLAIN_BLOCK) ecdsa_plain_kernel(const uint8_t* __restrict__ sigs, const uint8_t* __restrict__ msgs,
+template <class T, int MINB>
+__global__ void __launch_bounds__(PLAIN_BLOCK, MINB) ecdsa_plain_kernel(const uint8_t* __restrict__ sigs, const uint8_t* __restrict__ msgs,
                                                                    size_t n, const uint32_t* __restrict__ gtab, uint8_t* __restrict__ out,
                                                                    uint8_t* __restrict__ status, uint32_t* err) {
   __shared__ __align__(128) uint32_t tab[ECDSA_GTAB * 16];

@@ -212,7 +212,7 @@ SG_NOINL EPoint ed_lincomb(const u256 s, const u256 k, const EPoint negA, const 
   EPoint acc = Edw::identity();
 #pragma unroll 1
   for (int pos = TOP; pos >= 0; --pos) {
-    acc = Edw::dbl(acc);
+    acc = Edw::dbl(acc, pos % ED_WR == 0 || pos % ED_WG == 0);
     if (pos % ED_WR == 0) {
       bool neg;
       uint32_t d = booth_digit(k, pos / ED_WR, ED_WR, neg);

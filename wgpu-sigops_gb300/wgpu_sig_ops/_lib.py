@@ -55,7 +55,8 @@ SIGNATURES = {
     "sigops_mixed_plan_create": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _sz, _vp, _vp, ctypes.POINTER(_vp)]),
     "sigops_mixed_plan_launch": (ctypes.c_int, [_vp, _vp]),
     "sigops_mixed_plan_destroy": (None, [_vp]),
-    "sigops_set_batched_block": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "sigops_set_variant": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int]),
+    "sigops_get_variant": (ctypes.c_int, [_vp, ctypes.c_int] + [ctypes.POINTER(ctypes.c_int)] * 3),
     "sigops_workload_sign_ecdsa": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp, _vp, _sz, _vp, _vp, _vp, _vp]),
     "sigops_workload_sign_ed25519": (ctypes.c_int, [_vp, _vp, _vp, _sz, _vp, _vp, _vp]),
     "sigops_sync": (ctypes.c_int, [_vp]),
