@@ -37,26 +37,6 @@ struct MixedIO {
   size_t n;
 };
 
-__global__ void classify_kernel(const uint8_t* __restrict__ curves, size_t n, uint32_t* __restrict__ idx, Scratch* sc) {
-  const size_t stride = (size_t)gridDim.x * blockDim.x;
-  const unsigned lane = threadIdx.x & 31u;
-  for (size_t base = (size_t)blockIdx.x * blockDim.x; base < n; base += stride) {
-    size_t i = base + threadIdx.x;
-    int c = i < n ? curves[i] : -1;
-    if (c > 2) c = -1;  // unknown tags are skipped (host validates)
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      unsigned m = __ballot_sync(0xffffffffu, c == k);
-      if (!m) continue;
-      uint32_t off = 0;
-      int leader = __ffs(m) - 1;
-      if ((int)lane == leader) off = atomicAdd(&sc->count[k], (uint32_t)__popc(m));
-      off = __shfl_sync(0xffffffffu, off, leader);
-      if (c == k) idx[(size_t)k * n + off + __popc(m & ((1u << lane) - 1u))] = (uint32_t)i;
-    }
-  }
-}
-
 struct BatchTables {
   const uint32_t* k1;
   const uint32_t* r1;
