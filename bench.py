@@ -53,6 +53,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU-baseline sample duration")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--serving-seconds", type=float, default=5.0, help="seconds per serving load level (0 = skip serving)")
     ap.add_argument("--variant", type=int, default=-1, help="batched kernel launch variant (-1 = library default)")
     ap.add_argument("--plain-variant", type=int, default=-1, help="plain kernels launch variant (-1 = library default)")
     return ap.parse_args()
@@ -391,6 +392,14 @@ def main():
             t = json.load(f)
         traffic = t.get("dram_bytes_per_sig", 0) * n if t.get("dram_bytes_per_sig") else None
 
+    serving = None
+    if args.serving_seconds > 0:
+        from wgpu_sig_ops import serving as sv
+
+        serving = sv.measure(ctx, W, seconds=args.serving_seconds)
+        serving["workload"] = ("Poisson arrivals of single-curve requests, sizes log-uniform in 1..2048, 40/30/30 curves, "
+                               "items drawn from the mixed batch; latency = submit to results in host memory")
+
     cpu = None
     if not args.no_cpu_baseline and dist.rank == 0:
         cpu = cpu_baseline(W, out, status, args.cpu_seconds)
@@ -413,6 +422,7 @@ def main():
                      "peak_source": "measured in-process: mad.lo.u32 probe (MEASURED_PEAKS.json has no integer figure)",
                      "work_model": "256 IMAD per 256-bit field multiply; 1.201e6 IMAD per ECDSA recovery, 0.912e6 per ed25519 verify"},
         "e2e": e2e,
+        "serving": serving,
         "cpu_baseline": cpu,
         "gpu_launches": 2 * args.steps,
         "clocks": clk,

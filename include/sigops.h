@@ -64,6 +64,7 @@ extern "C" {
 
 typedef struct sigops_ctx sigops_ctx;
 typedef struct sigops_plan sigops_plan;
+typedef struct sigops_server sigops_server;
 
 /* ---------------------------------------------------------------- context */
 
@@ -178,6 +179,43 @@ void sigops_mixed_plan_destroy(sigops_plan* plan);
  * 2 = 128 x 4.  sigops_get_variant also reports the grid and block used. */
 int sigops_set_variant(sigops_ctx* ctx, int kernel, int variant);
 int sigops_get_variant(sigops_ctx* ctx, int kernel, int* variant, int* grid, int* block);
+
+/* ------------------------------------------------------- serving loop */
+
+/* A continuous-batching server over one context (no counterpart in the
+ * reference).  A dispatcher thread keeps `slots` batches in flight (each with
+ * its own stream, pinned staging, device buffers and scratch); requests that
+ * arrive while others run are packed into the next free slot.  slot_items = 0
+ * sizes slots from free device memory (hbm_fraction of cudaMemGetInfo's free
+ * bytes, default 0.25), capped at 65,536 items.  Returns NULL on failure. */
+sigops_server* sigops_server_create(sigops_ctx* ctx, int slots, size_t slot_items, double hbm_fraction);
+void sigops_server_destroy(sigops_server* server);
+size_t sigops_server_slot_items(sigops_server* server);
+
+/* Queue one request of n items.  curves: n tags, or NULL with uniform_curve
+ * set for a single-curve request; pks may be NULL for ECDSA-only requests.
+ * All buffers stay owned by the caller and must remain valid until
+ * sigops_server_wait returns for the handle; out receives n*64 bytes (mixed
+ * record layout), status n bytes (may be NULL).  Admission: SIGOPS_E_RANGE if
+ * n exceeds the slot size, SIGOPS_E_BUSY if the queue bound (from device
+ * memory) would be exceeded. */
+int sigops_server_submit(sigops_server* server, const uint8_t* curves, int uniform_curve, const uint8_t* sigs, const uint8_t* msgs,
+                         const uint8_t* pks, size_t n, uint8_t* out, uint8_t* status, uint64_t* handle);
+
+/* Wait for a request (timeout_ms < 0: no limit).  SIGOPS_OK when its results
+ * are in place (latency_ms: submit to results, may be NULL), SIGOPS_E_TIMEDOUT
+ * if still running, SIGOPS_E_INVAL for an unknown handle. */
+int sigops_server_wait(sigops_server* server, uint64_t handle, int timeout_ms, double* latency_ms);
+
+int sigops_server_stats(sigops_server* server, uint64_t* launches, uint64_t* requests_done, uint64_t* items_done, size_t* queued_items);
+
+/* Open-loop load generator: request i covers pool items
+ * [offset[i], offset[i] + count[i]) and is submitted arrival_s[i] seconds after
+ * the start (non-decreasing); outputs go to the same item positions of out /
+ * status.  Fills latency_ms[i] (-1 when refused) and the wall time. */
+int sigops_server_run_load(sigops_server* server, const uint8_t* curves, const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks,
+                           const uint64_t* offset, const uint32_t* count, const double* arrival_s, size_t nreq, uint8_t* out,
+                           uint8_t* status, double* latency_ms, double* wall_s);
 
 /* ------------------------------------------- synthetic workload signing */
 

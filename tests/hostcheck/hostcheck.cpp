@@ -7,12 +7,12 @@
 
 using namespace sg;
 
-static uint32_t g_k1[ECDSA_GTAB * 16], g_r1[ECDSA_GTAB * 16], g_ed[ED_GTAB * 24];
+static uint32_t g_k1[2 * ECDSA_GTAB * 16], g_r1[ECDSA_GTAB * 16], g_ed[ED_GTAB * 24];
 static bool g_init = false;
 
 static void init() {
   if (g_init) return;
-  build_weier_gtab<K1Traits>(k1_gx(), k1_gy(), g_k1);
+  build_k1_glv_gtab(g_k1);
   build_weier_gtab<R1Traits>(r1_gx(), r1_gy(), g_r1);
   build_ed_btab(g_ed);
   g_init = true;
@@ -27,7 +27,7 @@ int hc_bases(int curve, uint32_t L, uint32_t* out) { return build_bases(curve, L
 
 void hc_gtab(int curve, uint32_t* out) {
   init();
-  if (curve == 0) memcpy(out, g_k1, sizeof g_k1);
+  if (curve == 0) memcpy(out, g_k1, ECDSA_GTAB * 64);
   else if (curve == 1) memcpy(out, g_r1, sizeof g_r1);
   else memcpy(out, g_ed, sizeof g_ed);
 }
@@ -122,4 +122,13 @@ extern "C" void hc_sqr_wide(const uint8_t* a, uint8_t* out64) {
   memcpy(x.w, a, 32);
   sqr_wide(t, x);
   memcpy(out64, t, 64);
+}
+
+extern "C" int hc_k1_recover_glv(const uint8_t* sig, const uint8_t* msg, uint8_t* out) {
+  init();
+  uint32_t s[16], m[8], o[16];
+  memcpy(s, sig, 64); memcpy(m, msg, 32);
+  int st = ecdsa_recover<K1Traits, true>(s, m, g_k1, o);
+  memcpy(out, o, 64);
+  return st;
 }

@@ -77,9 +77,10 @@ def test_sha512(hc):
         assert out.raw.hex() == v["out"]
 
 
-@pytest.mark.parametrize("curve", ["secp256k1", "secp256r1"])
+@pytest.mark.parametrize("curve", ["secp256k1", "secp256k1_glv", "secp256r1"])
 def test_ecdsa_golden(hc, curve):
-    fn = hc.hc_k1_recover if curve == "secp256k1" else hc.hc_r1_recover
+    fn = {"secp256k1": hc.hc_k1_recover, "secp256k1_glv": hc.hc_k1_recover_glv, "secp256r1": hc.hc_r1_recover}[curve]
+    curve = curve.replace("_glv", "")
     for v in G[curve] + G[curve + "_edge"]:
         out = ctypes.create_string_buffer(64)
         st = fn(bytes.fromhex(v["sig"]), bytes.fromhex(v["msg"]), out)
@@ -160,3 +161,17 @@ def test_signers_match_oracle(hc):
         hc.hc_ed_sign(seed, m, sig, pk)
         assert sig.raw == o.ed25519_sign(seed, m)
         assert pk.raw == o.ed25519_keypair(seed)[2]
+
+
+def test_k1_glv_vs_oracle(hc):
+    """GLV path (batched engine) on random signatures, scalar edge cases and the
+    Strauss edge case of the reference's tests."""
+    rng = random.Random(31)
+    c = o.SECP256K1
+    for i in range(60):
+        d = rng.randrange(1, c.n) if i > 3 else [1, 2, c.n - 1, c.n // 2][i]
+        msg = rng.randbytes(32) if i % 5 else (c.n - 1).to_bytes(32, "big")
+        sig = o.ecdsa_sign_fuel(c, d, msg, k=rng.randrange(1, c.n))
+        out = ctypes.create_string_buffer(64)
+        st = hc.hc_k1_recover_glv(sig, msg, out)
+        assert (st, out.raw) == o.ecdsa_recover(c, sig, msg)[0:1] + (o.ecdsa_recover(c, sig, msg)[1] or bytes(64),)

@@ -46,16 +46,16 @@ struct BatchTables {
 // all three tables into shared memory with bulk copies on one mbarrier
 __device__ __forceinline__ bool stage_three(uint32_t* sk1, uint32_t* sr1, uint32_t* sed, const BatchTables& t, uint64_t* bar, uint32_t* err) {
   const uint32_t b = smem_addr(bar);
-  const uint32_t bk = ECDSA_GTAB * 64, be = ED_GTAB * 96;
+  const uint32_t bk = ECDSA_GTAB * 64, bk2 = 2 * ECDSA_GTAB * 64, be = ED_GTAB * 96;
   if (threadIdx.x == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b) : "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(2 * bk + be) : "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(bk2 + bk + be) : "memory");
     asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_addr(sk1)), "l"(t.k1),
-                 "r"(bk), "r"(b)
+                 "r"(bk2), "r"(b)
                  : "memory");
     asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_addr(sr1)), "l"(t.r1),
                  "r"(bk), "r"(b)
@@ -81,7 +81,7 @@ __device__ __forceinline__ bool stage_three(uint32_t* sk1, uint32_t* sr1, uint32
 template <int BLOCK, int MINB>
 __global__ void __launch_bounds__(BLOCK, MINB) batched_kernel(MixedIO io, const uint32_t* __restrict__ idx, BatchTables tabs, Scratch* sc,
                                                         uint32_t* err) {
-  __shared__ __align__(128) uint32_t tk1[ECDSA_GTAB * 16];
+  __shared__ __align__(128) uint32_t tk1[2 * ECDSA_GTAB * 16];  // G and 2^128 G multiples (GLV)
   __shared__ __align__(128) uint32_t tr1[ECDSA_GTAB * 16];
   __shared__ __align__(128) uint32_t ted[ED_GTAB * 24];
   __shared__ __align__(8) uint64_t bar;
@@ -109,7 +109,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) batched_kernel(MixedIO io, const 
       load_words(io.msgs, i, 8, m);
       uint8_t st;
       if (curve == 0) {
-        st = ecdsa_recover<K1Traits>(s, m, tk1, o);
+        st = ecdsa_recover<K1Traits, true>(s, m, tk1, o);
       } else if (curve == 1) {
         st = ecdsa_recover<R1Traits>(s, m, tr1, o);
       } else {

@@ -51,10 +51,10 @@ struct HostTables {
   void build() {
     std::lock_guard<std::mutex> g(mu);
     if (built) return;
-    gtab[CURVE_SECP256K1].resize(ECDSA_GTAB * 16);
+    gtab[CURVE_SECP256K1].resize(2 * ECDSA_GTAB * 16);  // G multiples, then 2^128 G multiples (GLV)
     gtab[CURVE_SECP256R1].resize(ECDSA_GTAB * 16);
     gtab[CURVE_ED25519].resize(ED_GTAB * 24);
-    build_weier_gtab<K1Traits>(k1_gx(), k1_gy(), gtab[CURVE_SECP256K1].data());
+    build_k1_glv_gtab(gtab[CURVE_SECP256K1].data());
     build_weier_gtab<R1Traits>(r1_gx(), r1_gy(), gtab[CURVE_SECP256R1].data());
     build_ed_btab(gtab[CURVE_ED25519].data());
     built = true;
@@ -257,6 +257,19 @@ int check_table_arg(int curve, const uint32_t* table, size_t len, uint32_t L) {
 }
 
 }  // namespace
+
+namespace sg {
+int ctx_view(sigops_ctx* c, CtxView* v) {
+  if (!c || !v) return SIGOPS_E_INVAL;
+  v->device = c->device;
+  v->num_sms = c->num_sms;
+  for (int k = 0; k < 3; ++k) v->gtab[k] = c->d_gtab[k];
+  v->d_err = c->d_err;
+  v->batched_grid = c->batched_grid;
+  v->batched_variant = c->batched_variant;
+  return SIGOPS_OK;
+}
+}  // namespace sg
 
 extern "C" {
 

@@ -4,6 +4,8 @@
 #include <stddef.h>
 #include <stdint.h>
 
+struct sigops_ctx;
+
 namespace sg {
 
 constexpr int PLAIN_BLOCK = 256;
@@ -38,6 +40,17 @@ size_t batched_scratch_bytes();
 cudaError_t launch_batched(const uint8_t* curves, const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks, size_t n, uint8_t* out,
                            uint8_t* status, uint32_t* idx, void* scratch, const uint32_t* gk1, const uint32_t* gr1, const uint32_t* ged,
                            uint32_t* err, int grid, int variant, int classify_grid, cudaStream_t stream);
+// what the serving loop needs from a context (host.cu)
+struct CtxView {
+  int device;
+  int num_sms;
+  const uint32_t* gtab[3];
+  uint32_t* d_err;
+  int batched_grid;
+  int batched_variant;
+};
+int ctx_view(sigops_ctx* c, CtxView* v);
+
 cudaError_t launch_field_test(int field, int op, const void* a, const void* b, void* out, int n, cudaStream_t stream);
 cudaError_t launch_sha512_test(const void* in, void* out, int n, cudaStream_t stream);
 cudaError_t launch_imad_probe(uint32_t* out, uint32_t iters, int grid, int block, cudaStream_t stream);

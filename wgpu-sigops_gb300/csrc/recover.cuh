@@ -112,12 +112,133 @@ SG_NOINL JPoint ecdsa_lincomb(const u256 u1, const u256 u2, const APoint R, cons
   return acc;
 }
 
+// ---------------------------------------------------------------------------
+// secp256k1 with the GLV endomorphism phi(x, y) = (beta x, y) = lambda (x, y):
+// u2 R = k1 R + k2 phi(R) with |k1|, |k2| < 2^128 and u1 G = a G + b (2^128 G)
+// (a, b the two 128-bit halves of u1), so the shared doubling chain is ~133
+// doublings instead of ~260.  Decomposition constants as in the reference's
+// src/curve_algos/secp256k1_curve.rs:47-71 (Babai rounding with g1, g2 scaled
+// by 2^384); the CPU model of GLV is src/curve_algos/secp256k1_mul.rs:38-94.
+// gtab2: multiples 1..64 of G followed by multiples 1..64 of 2^128 G.
+// ---------------------------------------------------------------------------
+struct K1Glv {
+  SG_HD static u256 LAMBDA_MONT() { return SG_U256(0xc9926c9eu, 0xf07deb3du, 0x83c6944cu, 0x2c93e7adu, 0x52697d91u, 0x73a96606u, 0x8558d639u, 0x53284017u); }
+  SG_HD static u256 BETA() { return SG_U256(0x719501eeu, 0xc1396c28u, 0x12f58995u, 0x9cf04975u, 0xac3434e9u, 0x6e64479eu, 0x657c0710u, 0x7ae96a2bu); }
+  SG_HD static u256 G1() { return SG_U256(0x45dbb031u, 0xe893209au, 0x71e8ca7fu, 0x3daa8a14u, 0x9284eb15u, 0xe86c90e4u, 0xa7d46bcdu, 0x3086d221u); }
+  SG_HD static u256 G2() { return SG_U256(0x8ac47f71u, 0x1571b4aeu, 0x9df506c6u, 0x221208acu, 0x0abfe4c4u, 0x6f547fa9u, 0x010e8828u, 0xe4437ed6u); }
+  SG_HD static u256 MINUS_B1() { return SG_U256(0x0abfe4c3u, 0x6f547fa9u, 0x010e8828u, 0xe4437ed6u, 0u, 0u, 0u, 0u); }
+  SG_HD static u256 B2() { return SG_U256(0x9284eb15u, 0xe86c90e4u, 0xa7d46bcdu, 0x3086d221u, 0u, 0u, 0u, 0u); }
+  SG_HD static u256 HALF_N() { return SG_U256(0x681b20a0u, 0xdfe92f46u, 0x57a4501du, 0x5d576e73u, 0xffffffffu, 0xffffffffu, 0xffffffffu, 0x7fffffffu); }
+
+  // round(k * g / 2^384) for k < 2^256, g < 2^256: bits 384..511 plus bit 383
+  SG_HD static u256 mul_shift384(const u256& k, const u256& g) {
+    uint32_t t[16];
+    mul_wide(t, k, g);
+    u256 r = u256_zero();
+    r.w[0] = add_cc(t[12], t[11] >> 31);
+    r.w[1] = addc_cc(t[13], 0u);
+    r.w[2] = addc_cc(t[14], 0u);
+    r.w[3] = addc_cc(t[15], 0u);
+    r.w[4] = addc(0u, 0u);
+    return r;
+  }
+
+  // product of two values below 2^129, reduced mod n (fits 256 bits + reduce_once)
+  SG_HD static u256 mul_small_mod_n(const u256& a, const u256& b) {
+    uint32_t t[16];
+    mul_wide(t, a, b);
+    u256 r;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) r.w[k] = t[k];
+    return reduce_once(r, K1ScalarC::N());
+  }
+
+  // k = k1 + k2 lambda (mod n); returns |k1|, |k2| and their signs
+  SG_HD static void split(const u256& k, u256& k1, bool& neg1, u256& k2, bool& neg2) {
+    const u256 N = K1ScalarC::N();
+    u256 c1 = mul_shift384(k, G1());
+    u256 c2 = mul_shift384(k, G2());
+    u256 r2 = mod_sub(mul_small_mod_n(c1, MINUS_B1()), mul_small_mod_n(c2, B2()), N);
+    u256 r1 = mod_sub(k, ScK1::mul(r2, LAMBDA_MONT()), N);  // Montgomery: r2 * (lambda R) / R
+    u256 t;
+    neg1 = u256_gte(HALF_N(), r1) == false;
+    u256_sub(t, N, r1);
+    k1 = neg1 ? t : r1;
+    neg2 = u256_gte(HALF_N(), r2) == false;
+    u256_sub(t, N, r2);
+    k2 = neg2 ? t : r2;
+  }
+};
+
+template <int = 0>
+SG_NOINL JPoint k1_glv_lincomb(const u256 u1, const u256 u2, const APoint R, const uint32_t* gtab2) {
+  using F = FpK1;
+  using W = Weier<F, false>;
+  constexpr int NR = 1 << (ECDSA_WR - 1);
+  u256 k1, k2;
+  bool neg1, neg2;
+  K1Glv::split(u2, k1, neg1, k2, neg2);
+  APoint R1 = neg1 ? W::neg(R) : R;
+  JPoint tab[NR];
+  tab[0] = W::from_affine(R1);
+  tab[1] = W::dbl(tab[0]);
+#pragma unroll 1
+  for (int k = 2; k < NR; ++k) tab[k] = W::madd(tab[k - 1], R1);
+  // phi(+-R) multiples: (beta X, +-Y, Z); k2's sign relative to k1's
+  const bool flip2 = neg1 != neg2;
+  const u256 beta = K1Glv::BETA();
+  u256 a = u1, b = u256_zero();
+#pragma unroll
+  for (int k = 0; k < 4; ++k) { b.w[k] = u1.w[4 + k]; a.w[4 + k] = 0; }
+
+  constexpr int JR = (130 + ECDSA_WR - 1) / ECDSA_WR;  // windows for a 129-bit magnitude
+  constexpr int JG = (129 + ECDSA_WG - 1) / ECDSA_WG;  // windows for a 128-bit half
+  constexpr int TOP = (JR * ECDSA_WR > JG * ECDSA_WG ? JR * ECDSA_WR : JG * ECDSA_WG) - 1;
+  JPoint acc = W::infinity();
+#pragma unroll 1
+  for (int pos = TOP; pos >= 0; --pos) {
+    acc = W::dbl(acc);
+    if (pos % ECDSA_WR == 0) {
+      bool ng;
+      uint32_t d = booth_digit(k1, pos / ECDSA_WR, ECDSA_WR, ng);
+      if (d) {
+        JPoint e = tab[d - 1];
+        if (ng) e = W::neg(e);
+        acc = W::add(acc, e);
+      }
+      d = booth_digit(k2, pos / ECDSA_WR, ECDSA_WR, ng);
+      if (d) {
+        JPoint e = tab[d - 1];
+        e.X = F::mul(e.X, beta);
+        if (ng != flip2) e = W::neg(e);
+        acc = W::add(acc, e);
+      }
+    }
+    if (pos % ECDSA_WG == 0) {
+      bool ng;
+      uint32_t d = booth_digit(a, pos / ECDSA_WG, ECDSA_WG, ng);
+      if (d) {
+        APoint e = load_apoint(gtab2, d - 1);
+        if (ng) e = W::neg(e);
+        acc = W::madd(acc, e);
+      }
+      d = booth_digit(b, pos / ECDSA_WG, ECDSA_WG, ng);
+      if (d) {
+        APoint e = load_apoint(gtab2, ECDSA_GTAB + d - 1);
+        if (ng) e = W::neg(e);
+        acc = W::madd(acc, e);
+      }
+    }
+  }
+  return acc;
+}
+
 // Recover the signer's key from a fuel-encoded signature (recovery parity in
 // bit 7 of s[0]); follows the reference's one-kernel path
 // (src/wgsl/secp256k1_ecdsa.wgsl:87-130, src/wgsl/secp256r1_ecdsa.wgsl:87-130)
 // with the validity rules of libsecp256k1 / p256 recovery: r, s in [1, n-1],
 // z = msg mod n, a checked square root for R.y, Q != infinity.
-template <class T>
+template <class T, bool GLV = false>
 SG_HD uint8_t ecdsa_recover(const uint32_t sig[16], const uint32_t msg[8], const uint32_t* gtab, uint32_t out[16]) {
   using F = typename T::F;
   using S = typename T::S;
@@ -151,7 +272,9 @@ SG_HD uint8_t ecdsa_recover(const uint32_t sig[16], const uint32_t msg[8], const
   u256 u2 = S::mul(s, rinv_m);
   u256 u1 = S::neg(S::mul(z, rinv_m));
 
-  JPoint Q = ecdsa_lincomb<T>(u1, u2, R, gtab);
+  JPoint Q;
+  if constexpr (GLV) Q = k1_glv_lincomb<>(u1, u2, R, gtab);
+  else Q = ecdsa_lincomb<T>(u1, u2, R, gtab);
   if (W::is_inf(Q)) return ST_INFINITY;
   APoint a = W::to_affine(Q);
   u256_to_be_words(F::to_int(a.x), out);

@@ -66,6 +66,20 @@ inline void build_weier_gtab(const u256& gx, const u256& gy, uint32_t* out) {
     }
 }
 
+// secp256k1 GLV table: multiples 1..64 of G, then multiples 1..64 of 2^128 G
+inline void build_k1_glv_gtab(uint32_t* out) {
+  using F = FpK1;
+  using W = Weier<F, false>;
+  build_weier_gtab<K1Traits>(k1_gx(), k1_gy(), out);
+  APoint g;
+  g.x = k1_gx();
+  g.y = k1_gy();
+  JPoint h = W::from_affine(g);
+  for (int i = 0; i < 128; ++i) h = W::dbl(h);
+  APoint ha = W::to_affine(h);
+  build_weier_gtab<K1Traits>(F::to_int(ha.x), F::to_int(ha.y), out + ECDSA_GTAB * 16);
+}
+
 // kernel table for ed25519: ED_GTAB entries of 24 words (y+x, y-x, 2d*x*y)
 inline void build_ed_btab(uint32_t* out) {
   u256 xs[ED_GTAB], ys[ED_GTAB];

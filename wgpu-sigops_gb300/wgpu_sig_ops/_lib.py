@@ -59,6 +59,14 @@ SIGNATURES = {
     "sigops_get_variant": (ctypes.c_int, [_vp, ctypes.c_int] + [ctypes.POINTER(ctypes.c_int)] * 3),
     "sigops_workload_sign_ecdsa": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp, _vp, _sz, _vp, _vp, _vp, _vp]),
     "sigops_workload_sign_ed25519": (ctypes.c_int, [_vp, _vp, _vp, _sz, _vp, _vp, _vp]),
+    "sigops_server_create": (_vp, [_vp, ctypes.c_int, _sz, ctypes.c_double]),
+    "sigops_server_destroy": (None, [_vp]),
+    "sigops_server_slot_items": (_sz, [_vp]),
+    "sigops_server_submit": (ctypes.c_int, [_vp, _vp, ctypes.c_int, _vp, _vp, _vp, _sz, _vp, _vp, ctypes.POINTER(ctypes.c_uint64)]),
+    "sigops_server_wait": (ctypes.c_int, [_vp, ctypes.c_uint64, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
+    "sigops_server_stats": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64),
+                                           ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(_sz)]),
+    "sigops_server_run_load": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp, _vp, _vp, ctypes.POINTER(ctypes.c_double)]),
     "sigops_sync": (ctypes.c_int, [_vp]),
     "sigops_probe_imad": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_double)]),
     "sigops_device_info": (ctypes.c_int, [_vp] + [ctypes.POINTER(ctypes.c_int)] * 4),
