@@ -136,8 +136,12 @@ void pack_and_launch(sigops_server* s, Slot& sl) {
   cudaMemcpyAsync(sl.d + L.pk, sl.h + L.pk, n * 32, cudaMemcpyHostToDevice, sl.stream);
   size_t cg = (n + 255) / 256;
   int classify_grid = (int)std::min(cg, (size_t)s->cv.num_sms * 8);
+  // grid sized to the batch (one item per thread up to a full persistent grid):
+  // small batches occupy few SMs, so launches from other slots run beside them
+  const int block = sg::batched_variant_block(s->cv.batched_variant);
+  const int grid = (int)std::min<size_t>((size_t)s->cv.batched_grid, (n + block - 1) / block);
   cudaError_t e = sg::launch_batched(sl.d + L.cur, sl.d + L.sig, sl.d + L.msg, sl.d + L.pk, n, sl.d + L.out, sl.d + L.st, sl.d_idx,
-                                     sl.d_scratch, s->cv.gtab[0], s->cv.gtab[1], s->cv.gtab[2], s->cv.d_err, s->cv.batched_grid,
+                                     sl.d_scratch, s->cv.gtab[0], s->cv.gtab[1], s->cv.gtab[2], s->cv.d_err, grid,
                                      s->cv.batched_variant, classify_grid, sl.stream);
   cudaMemcpyAsync(sl.h + L.out, sl.d + L.out, n * 64, cudaMemcpyDeviceToHost, sl.stream);
   cudaMemcpyAsync(sl.h + L.st, sl.d + L.st, n, cudaMemcpyDeviceToHost, sl.stream);
@@ -210,7 +214,7 @@ extern "C" {
 sigops_server* sigops_server_create(sigops_ctx* ctx, int nslots, size_t slot_items, double hbm_fraction) {
   sg::CtxView v;
   if (!ctx || sg::ctx_view(ctx, &v) != SIGOPS_OK) return nullptr;
-  if (nslots <= 0) nslots = 3;
+  if (nslots <= 0) nslots = 8;
   if (nslots > 16) nslots = 16;
   if (hbm_fraction <= 0 || hbm_fraction > 0.9) hbm_fraction = 0.25;
   cudaSetDevice(v.device);
@@ -218,7 +222,7 @@ sigops_server* sigops_server_create(sigops_ctx* ctx, int nslots, size_t slot_ite
   if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return nullptr;
   const size_t per_item = 1 + 64 + 32 + 32 + 64 + 1 + 3 * 4;
   size_t budget_items = (size_t)(free_b * hbm_fraction) / per_item;
-  if (slot_items == 0) slot_items = std::min<size_t>(budget_items / nslots, 1u << 16);
+  if (slot_items == 0) slot_items = std::min<size_t>(budget_items / nslots, 1u << 14);
   if (slot_items == 0 || slot_items * nslots > budget_items) return nullptr;
   sigops_server* s = new sigops_server();
   s->ctx = ctx;

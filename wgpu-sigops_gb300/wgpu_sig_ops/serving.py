@@ -21,7 +21,7 @@ _dblp = ctypes.POINTER(ctypes.c_double)
 
 
 class Server:
-    def __init__(self, ctx, slots: int = 3, slot_items: int = 0, hbm_fraction: float = 0.25):
+    def __init__(self, ctx, slots: int = 8, slot_items: int = 0, hbm_fraction: float = 0.25):
         self.ctx = ctx
         self.ptr = lib.sigops_server_create(ctx.ptr, slots, slot_items, hbm_fraction)
         if not self.ptr:
@@ -129,7 +129,7 @@ def request_stream(regions: dict, rate_rps: float, seconds: float, seed: int, ma
     return offsets, sizes.astype(np.uint32), arrivals
 
 
-def measure(ctx, W, loads=(0.25, 0.5, 0.75, 0.9), seconds: float = 10.0, seed: int = 5001, slots: int = 3,
+def measure(ctx, W, loads=(0.25, 0.5, 0.75, 0.9), seconds: float = 10.0, seed: int = 5001, slots: int = 8,
             slot_items: int = 0, sat_items: int = 2_000_000) -> dict:
     """Saturation, then open-loop Poisson load levels; latency percentiles in ms."""
     pool, regions = curve_sorted_pool(W)
