@@ -185,9 +185,11 @@ int sigops_get_variant(sigops_ctx* ctx, int kernel, int* variant, int* grid, int
 /* A continuous-batching server over one context (no counterpart in the
  * reference).  A dispatcher thread keeps `slots` batches in flight (each with
  * its own stream, pinned staging, device buffers and scratch); requests that
- * arrive while others run are packed into the next free slot.  slot_items = 0
- * sizes slots from free device memory (hbm_fraction of cudaMemGetInfo's free
- * bytes, default 0.25), capped at 65,536 items.  Returns NULL on failure. */
+ * arrive while others run are packed into the next free slot; each launch's
+ * grid is sized to its batch, so small batches from several slots share the
+ * SMs.  slots <= 0 selects 8; slot_items = 0 sizes slots from free device
+ * memory (hbm_fraction of cudaMemGetInfo's free bytes, default 0.25), capped
+ * at 16,384 items.  Returns NULL on failure. */
 sigops_server* sigops_server_create(sigops_ctx* ctx, int slots, size_t slot_items, double hbm_fraction);
 void sigops_server_destroy(sigops_server* server);
 size_t sigops_server_slot_items(sigops_server* server);
