@@ -132,3 +132,27 @@ extern "C" int hc_k1_recover_glv(const uint8_t* sig, const uint8_t* msg, uint8_t
   memcpy(out, o, 64);
   return st;
 }
+
+#include "../../wgpu-sigops_gb300/csrc/inverse.cuh"
+
+// x^-1 mod M by divsteps; *batches_used = first batch after which g == 0
+extern "C" void hc_divstep_inv(const uint8_t* x, const uint8_t* m, uint32_t minv30, uint8_t* out, int* batches_used) {
+  u256 xv = load_le(x), mv = load_le(m);
+  store_le(divstep_inverse(xv, mv, minv30), out);
+  // count batches until g == 0
+  S30 M = s30_from_u256(mv), f = M, g = s30_from_u256(xv), d, e;
+  for (int i = 0; i < 9; ++i) { d.v[i] = 0; e.v[i] = 0; }
+  e.v[0] = 1;
+  int32_t delta = 1;
+  int used = -1;
+  for (int it = 0; it < 25; ++it) {
+    int32_t t[4];
+    delta = divsteps30(delta, (uint32_t)f.v[0] | ((uint32_t)f.v[1] << 30), (uint32_t)g.v[0] | ((uint32_t)g.v[1] << 30), t);
+    s30_update_de(d, e, t, M, minv30);
+    s30_update_fg(f, g, t);
+    bool zero = true;
+    for (int k = 0; k < 9; ++k) zero &= g.v[k] == 0;
+    if (zero && used < 0) used = it + 1;
+  }
+  *batches_used = used;
+}

@@ -175,3 +175,20 @@ def test_k1_glv_vs_oracle(hc):
         out = ctypes.create_string_buffer(64)
         st = hc.hc_k1_recover_glv(sig, msg, out)
         assert (st, out.raw) == o.ecdsa_recover(c, sig, msg)[0:1] + (o.ecdsa_recover(c, sig, msg)[1] or bytes(64),)
+
+
+@pytest.mark.parametrize("name", ["k1p", "k1n", "r1p", "r1n", "edp", "edl"])
+def test_divstep_inverse(hc, name):
+    """Bernstein-Yang divstep inverse (25 batches of 30): exact against pow(),
+    and every random input reaches g = 0 within the fixed batch count."""
+    M, minv = {"k1p": (o.SECP256K1.p, 0x2ddacacf), "k1n": (o.SECP256K1.n, 0x2a774ec1), "r1p": (o.SECP256R1.p, 0x3fffffff),
+               "r1n": (o.SECP256R1.n, 0x11ff43b1), "edp": (o.ED_P, 0x179435e5), "edl": (o.ED_L, 0x2dab81e5)}[name]
+    assert pow(M, -1, 2**30) == minv
+    rng = random.Random(hash(name) & 0xffff)
+    cases = [1, 2, 3, M - 1, M - 2, (M - 1) // 2, 2**255 % M, 2**128] + [rng.randrange(1, M) for _ in range(3000)]
+    for x in cases:
+        out = ctypes.create_string_buffer(32)
+        used = ctypes.c_int()
+        hc.hc_divstep_inv(x.to_bytes(32, "little"), M.to_bytes(32, "little"), minv, out, ctypes.byref(used))
+        assert int.from_bytes(out.raw, "little") == pow(x, -1, M)
+        assert 0 < used.value <= 25

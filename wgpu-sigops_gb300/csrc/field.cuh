@@ -11,11 +11,13 @@
 // square-and-multiply `modpow` (src/wgsl/mont.wgsl:80-99), binary-EEA
 // `ff_inverse` (src/wgsl/ff.wgsl:60-120) and the (p+1)/4 square root
 // (src/wgsl/secp256k1_curve.wgsl:12-21).  Here exponentiations use fixed
-// addition chains (255 squarings and 11-15 multiplications each) and the
-// scalar inverse uses Fermat with a 4-bit window, so no input can make a loop
-// run away (the reference's binary EEA never terminates for 0).
+// addition chains (253-255 squarings and 7-15 multiplications each) and the
+// inverses use a fixed count of Bernstein-Yang divsteps (inverse.cuh), each
+// verified by one multiplication with Fermat as the fallback, so no input can
+// make a loop run away (the reference's binary EEA never terminates for 0).
 #pragma once
 #include "arith.cuh"
+#include "inverse.cuh"
 
 namespace sg {
 
@@ -137,8 +139,14 @@ struct FpK1 {
     x223 = mul(sqr_n(x220, 3), x3);
   }
 
-  // a^(p-2): 255 squarings, 15 multiplications
+  // a^-1 by divsteps, verified; Fermat fallback
   SG_NOINL static u256 inv(const u256 a) {
+    u256 r = divstep_inverse(a, P(), 0x2ddacacfu);
+    return u256_eq(mul(a, r), one()) ? r : inv_fermat(a);
+  }
+
+  // a^(p-2): 255 squarings, 15 multiplications
+  SG_NOINL static u256 inv_fermat(const u256 a) {
     u256 x2, x22, t;
     blocks(a, x2, x22, t);
     t = mul(sqr_n(t, 23), x22);
@@ -239,8 +247,14 @@ struct FpEd {
     z2_250_0 = mul(sqr_n(z2_200_0, 50), z2_50_0);
   }
 
-  // z^(p-2) = z^(2^255 - 21)
+  // z^-1 by divsteps, verified; Fermat fallback
   SG_NOINL static u256 inv(const u256 z) {
+    u256 r = divstep_inverse(z, P(), 0x179435e5u);
+    return u256_eq(mul(z, r), one()) ? r : inv_fermat(z);
+  }
+
+  // z^(p-2) = z^(2^255 - 21)
+  SG_NOINL static u256 inv_fermat(const u256 z) {
     u256 t, z11;
     pow250(z, t, z11);
     return mul(sqr_n(t, 5), z11);
@@ -348,6 +362,13 @@ struct Mont {
     }
     return r;
   }
+  // x^-1 for a plain integer 0 < x < N: divsteps, verified; Fermat fallback
+  SG_NOINL static u256 inv_int(const u256 x) {
+    u256 r = divstep_inverse(x, C::N(), C::MINV30);
+    if (u256_eq(mul(from_int(x), r), u256_small(1))) return r;
+    return to_int(inv(from_int(x)));
+  }
+
   // Fermat inverse in the Montgomery domain
   SG_NOINL static u256 inv(const u256 a) {
     uint32_t e[8];
@@ -364,6 +385,7 @@ struct K1ScalarC {
   SG_HD static u256 ONE_MONT() { return SG_U256(0x2fc9bebfu, 0x402da173u, 0x50b75fc4u, 0x45512319u, 0x00000001u, 0x00000000u, 0x00000000u, 0x00000000u); }
   SG_HD static u256 N_MINUS_2() { return SG_U256(0xd036413fu, 0xbfd25e8cu, 0xaf48a03bu, 0xbaaedce6u, 0xfffffffeu, 0xffffffffu, 0xffffffffu, 0xffffffffu); }
   static constexpr uint32_t NINV = 0x5588b13fu;
+  static constexpr uint32_t MINV30 = 0x2a774ec1u;
 };
 
 struct R1ScalarC {
@@ -372,6 +394,7 @@ struct R1ScalarC {
   SG_HD static u256 ONE_MONT() { return SG_U256(0x039cdaafu, 0x0c46353du, 0x58e8617bu, 0x43190552u, 0x00000000u, 0x00000000u, 0xffffffffu, 0x00000000u); }
   SG_HD static u256 N_MINUS_2() { return SG_U256(0xfc63254fu, 0xf3b9cac2u, 0xa7179e84u, 0xbce6faadu, 0xffffffffu, 0xffffffffu, 0x00000000u, 0xffffffffu); }
   static constexpr uint32_t NINV = 0xee00bc4fu;
+  static constexpr uint32_t MINV30 = 0x11ff43b1u;
 };
 
 struct EdScalarC {
@@ -380,6 +403,7 @@ struct EdScalarC {
   SG_HD static u256 ONE_MONT() { return SG_U256(0x8d98951du, 0xd6ec3174u, 0x737dcf70u, 0xc6ef5bf4u, 0xfffffffeu, 0xffffffffu, 0xffffffffu, 0x0fffffffu); }
   SG_HD static u256 N_MINUS_2() { return SG_U256(0x5cf5d3ebu, 0x5812631au, 0xa2f79cd6u, 0x14def9deu, 0x00000000u, 0x00000000u, 0x00000000u, 0x10000000u); }
   static constexpr uint32_t NINV = 0x12547e1bu;
+  static constexpr uint32_t MINV30 = 0x2dab81e5u;
 };
 
 using ScK1 = Mont<K1ScalarC>;
@@ -464,8 +488,14 @@ struct FpR1 {
     x32 = mul(sqr_n(x16, 16), x16);
   }
 
-  // a^(p-2), p-2 = ones[255..224] 0^31 1 0^96 ones[95..2] 0 1 : 255 S + 13 M
+  // a^-1 by divsteps, verified; Fermat fallback
   SG_NOINL static u256 inv(const u256 a) {
+    u256 r = divstep_inverse(a, P(), 0x3fffffffu);
+    return u256_eq(mul(a, r), one()) ? r : inv_fermat(a);
+  }
+
+  // a^(p-2), p-2 = ones[255..224] 0^31 1 0^96 ones[95..2] 0 1 : 255 S + 13 M
+  SG_NOINL static u256 inv_fermat(const u256 a) {
     u256 x2, x4, x8, x16, x32;
     blocks(a, x2, x4, x8, x16, x32);
     u256 t = mul(sqr_n(x32, 32), a);

@@ -268,7 +268,7 @@ SG_HD uint8_t ecdsa_recover(const uint32_t sig[16], const uint32_t msg[8], const
   R.y = y;
 
   // u1 = -z / r, u2 = s / r (mod n)
-  u256 rinv_m = S::inv(S::from_int(r));  // r^-1 in Montgomery form
+  u256 rinv_m = S::from_int(S::inv_int(r));  // r^-1 in Montgomery form
   u256 u2 = S::mul(s, rinv_m);
   u256 u1 = S::neg(S::mul(z, rinv_m));
 

@@ -27,7 +27,7 @@ SG_HD uint8_t ecdsa_sign(const uint32_t d_w[8], const uint32_t k_w[8], const uin
   u256 rx = F::to_int(R.x);
   uint32_t parity = F::to_int(R.y).w[0] & 1u;
   if (u256_is_zero(rx) || u256_gte(rx, N)) return 1;
-  u256 kinv_m = S::inv(S::from_int(k));
+  u256 kinv_m = S::from_int(S::inv_int(k));
   u256 t = S::add(z, S::mul(rx, S::from_int(d)));
   u256 s = S::mul(t, kinv_m);
   if (u256_is_zero(s)) return 1;
