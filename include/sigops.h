@@ -198,7 +198,8 @@ void sigops_mixed_plan_destroy(sigops_plan* plan);
  * plain kernel of SIGOPS_SECP256K1 / SECP256R1 / ED25519, variant 0 = one
  * 256-thread block per SM, 1 = two (register budget 128); kernel 3: the
  * batched kernel, variant 0 = 256 threads x 1 block per SM, 1 = 256 x 2,
- * 2 = 128 x 4.  sigops_get_variant also reports the grid and block used. */
+ * 2 = 128 x 4, 3 = 64-thread blocks (as many per SM as registers allow).
+ * sigops_get_variant also reports the grid and block used. */
 int sigops_set_variant(sigops_ctx* ctx, int kernel, int variant);
 int sigops_get_variant(sigops_ctx* ctx, int kernel, int* variant, int* grid, int* block);
 

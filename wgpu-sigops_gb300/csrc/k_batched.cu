@@ -26,12 +26,14 @@ __global__ void classify_kernel(const uint8_t* __restrict__ curves, size_t n, ui
 int batched_occupancy_0();
 int batched_occupancy_1();
 int batched_occupancy_2();
+int batched_occupancy_3();
 cudaError_t batched_launch_0(const MixedIO&, const uint32_t*, const BatchTables&, Scratch*, uint32_t*, int, cudaStream_t);
 cudaError_t batched_launch_1(const MixedIO&, const uint32_t*, const BatchTables&, Scratch*, uint32_t*, int, cudaStream_t);
 cudaError_t batched_launch_2(const MixedIO&, const uint32_t*, const BatchTables&, Scratch*, uint32_t*, int, cudaStream_t);
+cudaError_t batched_launch_3(const MixedIO&, const uint32_t*, const BatchTables&, Scratch*, uint32_t*, int, cudaStream_t);
 
-// variants: 0 = 256 threads x 1 block/SM, 1 = 256 x 2, 2 = 128 x 4
-static const int kBlock[BATCHED_VARIANTS] = {256, 256, 128};
+// variants: 0 = 256 threads x 1 block/SM, 1 = 256 x 2, 2 = 128 x 4, 3 = 64 threads
+static const int kBlock[BATCHED_VARIANTS] = {256, 256, 128, 64};
 
 int batched_variant_block(int v) { return (v >= 0 && v < BATCHED_VARIANTS) ? kBlock[v] : 0; }
 
@@ -40,6 +42,7 @@ int batched_max_blocks_per_sm(int v) {
     case 0: return batched_occupancy_0();
     case 1: return batched_occupancy_1();
     case 2: return batched_occupancy_2();
+    case 3: return batched_occupancy_3();
     default: return 0;
   }
 }
@@ -58,6 +61,7 @@ cudaError_t launch_batched(const uint8_t* curves, const uint8_t* sigs, const uin
     case 0: return batched_launch_0(io, idx, t, sc, err, grid, stream);
     case 1: return batched_launch_1(io, idx, t, sc, err, grid, stream);
     case 2: return batched_launch_2(io, idx, t, sc, err, grid, stream);
+    case 3: return batched_launch_3(io, idx, t, sc, err, grid, stream);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -32,8 +32,8 @@ cudaError_t launch_sign_ecdsa(int curve, const uint8_t* secrets, const uint8_t* 
 cudaError_t launch_sign_ed(const uint8_t* seeds, const uint8_t* msgs, size_t n, const uint32_t* btab, uint8_t* sigs, uint8_t* pks,
                            uint32_t* err, int grid, cudaStream_t stream);
 // batched mixed-curve engine: scratch = Scratch record + 3*n u32 index lists.
-// variants: 0 = 256 threads x 1 block/SM, 1 = 256 x 2, 2 = 128 x 4
-constexpr int BATCHED_VARIANTS = 3;
+// variants: 0 = 256 threads x 1 block/SM, 1 = 256 x 2, 2 = 128 x 4, 3 = 64 threads
+constexpr int BATCHED_VARIANTS = 4;
 int batched_variant_block(int variant);
 int batched_max_blocks_per_sm(int variant);
 size_t batched_scratch_bytes();
