@@ -56,6 +56,7 @@ def parse():
     ap.add_argument("--serving-seconds", type=float, default=5.0, help="seconds per serving load level (0 = skip serving)")
     ap.add_argument("--variant", type=int, default=-1, help="batched kernel launch variant (-1 = library default)")
     ap.add_argument("--plain-variant", type=int, default=-1, help="plain kernels launch variant (-1 = library default)")
+    ap.add_argument("--no-autotune", action="store_true", help="skip the autotuner (launch variants as set)")
     return ap.parse_args()
 
 
@@ -271,7 +272,11 @@ def main():
     if args.plain_variant >= 0:
         for k in range(3):
             check(lib.sigops_set_variant(ctx.ptr, k, args.plain_variant), "plain variant")
+    tune = None
+    if not args.no_autotune and args.variant < 0 and args.plain_variant < 0:
+        tune = ctx.autotune()
     info = ctx.device_info()
+    info["variants"] = ctx.variants()
     imad_peak = max(ctx.probe_imad() for _ in range(3))
 
     t_gen = time.perf_counter()
@@ -427,6 +432,7 @@ def main():
         "gpu_launches": 2 * args.steps,
         "clocks": clk,
         "workload_gen_s": t_gen,
+        "autotune": tune,
     }
     print(json.dumps(line), flush=True)
 

@@ -203,6 +203,14 @@ void sigops_mixed_plan_destroy(sigops_plan* plan);
 int sigops_set_variant(sigops_ctx* ctx, int kernel, int variant);
 int sigops_get_variant(sigops_ctx* ctx, int kernel, int* variant, int* grid, int* block);
 
+/* Autotuner: signs a probe batch (probe_items, 0 = 4 waves of the device) with
+ * the 40/30/30 curve mix on the device, times every variant of the batched
+ * kernel and of each plain kernel (best of three after a warm-up), and selects
+ * the fastest.  report (may be NULL) receives a JSON summary of the timings.
+ * When SIGOPS_TUNE_CACHE names a file, the choice is stored there per device
+ * model and sigops_create applies it. */
+int sigops_autotune(sigops_ctx* ctx, size_t probe_items, char* report, size_t report_cap);
+
 /* ------------------------------------------------------- serving loop */
 
 /* A continuous-batching server over one context (no counterpart in the

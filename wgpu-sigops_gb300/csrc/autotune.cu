@@ -1,0 +1,228 @@
+// Autotuner: picks the fastest launch variant of each kernel on this device.
+//
+// No counterpart in the reference (its launch shape is fixed at 256-thread
+// workgroups, src/benchmarks/mod.rs:10-53).  A probe batch with the 40/30/30
+// curve mix is signed on the device (valid signatures, so every item runs the
+// full path), then each variant of the batched kernel and of each curve's
+// plain kernel is timed with CUDA events (one warm-up, best of three) and the
+// fastest is selected.  The search space is the compiled variants: block shape
+// (64 / 128 / 256 threads) and register budget (one or two blocks per SM).
+// Window widths are fixed at compile time (5 bits for the per-signature point,
+// 7 for the generator tables), chosen by the operation-count model.
+//
+// Results can be kept in a cache file (SIGOPS_TUNE_CACHE, one line per device
+// name and SM count) that sigops_create reads back.
+#include <cuda_runtime.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/sigops.h"
+#include "launch.h"
+
+namespace {
+
+uint64_t splitmix(uint64_t& s) {
+  uint64_t z = (s += 0x9e3779b97f4a7c15ull);
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+
+void fill_random(std::vector<uint8_t>& v, uint64_t& s) {
+  for (size_t i = 0; i < v.size(); i += 8) {
+    uint64_t r = splitmix(s);
+    for (size_t k = 0; k < 8 && i + k < v.size(); ++k) v[i + k] = (uint8_t)(r >> (8 * k));
+  }
+}
+
+struct DevBuf {
+  uint8_t* p = nullptr;
+  ~DevBuf() {
+    if (p) cudaFree(p);
+  }
+};
+
+std::string cache_key(int device) {
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return "";
+  char buf[300];
+  snprintf(buf, sizeof buf, "%s|sm%d|%s", prop.name, prop.multiProcessorCount, sigops_version());
+  return buf;
+}
+
+std::mutex g_cache_mu;
+
+}  // namespace
+
+namespace sg {
+
+// read a cached tuning for this device: fills variants[4]; false if none
+bool tune_cache_lookup(int device, int variants[4]) {
+  const char* path = getenv("SIGOPS_TUNE_CACHE");
+  if (!path || !*path) return false;
+  std::lock_guard<std::mutex> g(g_cache_mu);
+  FILE* f = fopen(path, "r");
+  if (!f) return false;
+  std::string key = cache_key(device);
+  char line[512];
+  bool found = false;
+  while (fgets(line, sizeof line, f)) {
+    char* tab = strchr(line, '\t');
+    if (!tab) continue;
+    *tab = 0;
+    if (key == line && sscanf(tab + 1, "%d %d %d %d", &variants[0], &variants[1], &variants[2], &variants[3]) == 4) found = true;
+  }
+  fclose(f);
+  return found;
+}
+
+static void tune_cache_store(int device, const int variants[4]) {
+  const char* path = getenv("SIGOPS_TUNE_CACHE");
+  if (!path || !*path) return;
+  std::lock_guard<std::mutex> g(g_cache_mu);
+  std::string key = cache_key(device);
+  std::vector<std::string> keep;
+  if (FILE* f = fopen(path, "r")) {
+    char line[512];
+    while (fgets(line, sizeof line, f)) {
+      std::string s(line);
+      if (s.compare(0, key.size() + 1, key + "\t") != 0) keep.push_back(s);
+    }
+    fclose(f);
+  }
+  if (FILE* f = fopen(path, "w")) {
+    for (auto& s : keep) fputs(s.c_str(), f);
+    fprintf(f, "%s\t%d %d %d %d\n", key.c_str(), variants[0], variants[1], variants[2], variants[3]);
+    fclose(f);
+  }
+}
+
+}  // namespace sg
+
+extern "C" int sigops_autotune(sigops_ctx* ctx, size_t probe_items, char* report, size_t report_cap) {
+  sg::CtxView v;
+  if (!ctx || sg::ctx_view(ctx, &v) != SIGOPS_OK) return SIGOPS_E_INVAL;
+  if (probe_items == 0) probe_items = (size_t)v.num_sms * 256 * 4;
+  const size_t n = probe_items;
+  cudaSetDevice(v.device);
+  // probe batch: 40/30/30 by position
+  const size_t n1 = n * 4 / 10, n2 = n * 3 / 10, n3 = n - n1 - n2;
+  std::vector<uint8_t> curves(n), secrets(n * 32), nonces(n * 32), msgs(n * 32), seeds(n * 32);
+  uint64_t s = 0x5349474f5053ull;
+  fill_random(secrets, s);
+  fill_random(nonces, s);
+  fill_random(msgs, s);
+  fill_random(seeds, s);
+  for (size_t i = 0; i < n; ++i) curves[i] = i < n1 ? 0 : (i < n1 + n2 ? 1 : 2);
+  DevBuf d;
+  const size_t o_cur = 0, o_sec = 256 * ((n + 255) / 256), o_non = o_sec + n * 32, o_msg = o_non + n * 32, o_seed = o_msg + n * 32,
+               o_sig = o_seed + n * 32, o_pub = o_sig + n * 64, o_pk = o_pub + n * 64, o_out = o_pk + n * 32, o_st = o_out + n * 64,
+               o_idx = o_st + 256 * ((n + 255) / 256), o_scr = o_idx + 3 * n * 4, total = o_scr + 256;
+  if (cudaMalloc(&d.p, total) != cudaSuccess) return SIGOPS_E_NOMEM;
+  cudaStream_t st;
+  if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return SIGOPS_E_CUDA;
+  cudaMemcpyAsync(d.p + o_cur, curves.data(), n, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(d.p + o_sec, secrets.data(), n * 32, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(d.p + o_non, nonces.data(), n * 32, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(d.p + o_msg, msgs.data(), n * 32, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(d.p + o_seed, seeds.data(), n * 32, cudaMemcpyHostToDevice, st);
+  cudaMemsetAsync(d.p + o_pk, 0, n * 32, st);
+  const int sign_grid = v.num_sms * 2;
+  sg::launch_sign_ecdsa(0, d.p + o_sec, d.p + o_non, d.p + o_msg, n1, v.gtab[0], d.p + o_sig, d.p + o_pub, d.p + o_st, v.d_err, sign_grid, st);
+  sg::launch_sign_ecdsa(1, d.p + o_sec + n1 * 32, d.p + o_non + n1 * 32, d.p + o_msg + n1 * 32, n2, v.gtab[1], d.p + o_sig + n1 * 64,
+                        d.p + o_pub + n1 * 64, d.p + o_st + n1, v.d_err, sign_grid, st);
+  sg::launch_sign_ed(d.p + o_seed + (n1 + n2) * 32, d.p + o_msg + (n1 + n2) * 32, n3, v.gtab[2], d.p + o_sig + (n1 + n2) * 64,
+                     d.p + o_pk + (n1 + n2) * 32, v.d_err, sign_grid, st);
+  if (cudaStreamSynchronize(st) != cudaSuccess) {
+    cudaStreamDestroy(st);
+    return SIGOPS_E_CUDA;
+  }
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  auto time_it = [&](auto&& launch) -> float {
+    launch();
+    float best = 1e30f;
+    for (int r = 0; r < 3; ++r) {
+      cudaEventRecord(e0, st);
+      launch();
+      cudaEventRecord(e1, st);
+      cudaEventSynchronize(e1);
+      float ms = 0;
+      cudaEventElapsedTime(&ms, e0, e1);
+      best = std::min(best, ms);
+    }
+    return cudaGetLastError() == cudaSuccess ? best : 1e30f;
+  };
+  std::string rep = "{";
+  int chosen[4] = {0, 0, 0, 0};
+  // batched engine
+  {
+    float best = 1e30f;
+    rep += "\"batched\": {";
+    for (int var = 0; var < sg::BATCHED_VARIANTS; ++var) {
+      int bps = sg::batched_max_blocks_per_sm(var);
+      if (bps <= 0) continue;
+      const int grid = v.num_sms * bps;
+      size_t cg = (n + 255) / 256;
+      int classify_grid = (int)std::min(cg, (size_t)v.num_sms * 8);
+      float ms = time_it([&] {
+        sg::launch_batched(d.p + o_cur, d.p + o_sig, d.p + o_msg, d.p + o_pk, n, d.p + o_out, d.p + o_st, (uint32_t*)(d.p + o_idx),
+                           d.p + o_scr, v.gtab[0], v.gtab[1], v.gtab[2], v.d_err, grid, var, classify_grid, st);
+      });
+      char b[96];
+      snprintf(b, sizeof b, "%s\"%d\": %.3f", var ? ", " : "", var, ms);
+      rep += b;
+      if (ms < best) {
+        best = ms;
+        chosen[3] = var;
+      }
+    }
+    rep += "}";
+  }
+  // plain kernels per curve
+  const size_t off[3] = {0, n1, n1 + n2}, cnt[3] = {n1, n2, n3};
+  for (int c = 0; c < 3; ++c) {
+    float best = 1e30f;
+    char b[96];
+    snprintf(b, sizeof b, ", \"plain_%d\": {", c);
+    rep += b;
+    for (int var = 0; var < sg::PLAIN_VARIANTS; ++var) {
+      int bps = sg::plain_max_blocks_per_sm(c, var);
+      if (bps <= 0) continue;
+      const int grid = v.num_sms * bps;
+      float ms = time_it([&] {
+        sg::launch_plain(c, d.p + o_sig + off[c] * 64, d.p + o_msg + off[c] * 32, d.p + o_pk + off[c] * 32, cnt[c], v.gtab[c],
+                         d.p + o_out, d.p + o_st, v.d_err, grid, var, st);
+      });
+      snprintf(b, sizeof b, "%s\"%d\": %.3f", var ? ", " : "", var, ms);
+      rep += b;
+      if (ms < best) {
+        best = ms;
+        chosen[c] = var;
+      }
+    }
+    rep += "}";
+  }
+  char b[160];
+  snprintf(b, sizeof b, ", \"chosen\": [%d, %d, %d, %d], \"probe_items\": %zu}", chosen[0], chosen[1], chosen[2], chosen[3], n);
+  rep += b;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaStreamDestroy(st);
+  for (int k = 0; k < 4; ++k) {
+    int rc = sigops_set_variant(ctx, k, chosen[k]);
+    if (rc != SIGOPS_OK) return rc;
+  }
+  sg::tune_cache_store(v.device, chosen);
+  if (report && report_cap) {
+    strncpy(report, rep.c_str(), report_cap - 1);
+    report[report_cap - 1] = 0;
+  }
+  return SIGOPS_OK;
+}

@@ -1,5 +1,8 @@
 // Prime fields for the three curves, 8 x 32-bit limbs, values kept canonical
-// (in [0, p)) after every operation.
+// (in [0, p)) after every operation.  The base-field multiply and square are
+// called functions, not inlined: the hot loops then fit the instruction cache
+// (inlining them everywhere measured 4% slower overall, 19% on ed25519, and
+// took six times longer to compile).
 //
 //  * FpK1  p = 2^256 - 2^32 - 977   special-form fold (2^256 = 2^32 + 977)
 //  * FpEd  p = 2^255 - 19           special-form fold (2^256 = 38)
@@ -109,8 +112,8 @@ struct FpK1 {
     return reduce_once(r, P());
   }
 
-  SG_HD static u256 mul(const u256& a, const u256& b) { uint32_t t[16]; mul_wide(t, a, b); return reduce(t); }
-  SG_HD static u256 sqr(const u256& a) { uint32_t t[16]; sqr_wide(t, a); return reduce(t); }
+  SG_NOINL static u256 mul(const u256 a, const u256 b) { uint32_t t[16]; mul_wide(t, a, b); return reduce(t); }
+  SG_NOINL static u256 sqr(const u256 a) { uint32_t t[16]; sqr_wide(t, a); return reduce(t); }
   SG_HD static u256 add(const u256& a, const u256& b) { return mod_add(a, b, P()); }
   SG_HD static u256 sub(const u256& a, const u256& b) { return mod_sub(a, b, P()); }
   SG_HD static u256 neg(const u256& a) { return mod_neg(a, P()); }
@@ -213,8 +216,8 @@ struct FpEd {
     return canon(r);
   }
 
-  SG_HD static u256 mul(const u256& a, const u256& b) { uint32_t t[16]; mul_wide(t, a, b); return reduce(t); }
-  SG_HD static u256 sqr(const u256& a) { uint32_t t[16]; sqr_wide(t, a); return reduce(t); }
+  SG_NOINL static u256 mul(const u256 a, const u256 b) { uint32_t t[16]; mul_wide(t, a, b); return reduce(t); }
+  SG_NOINL static u256 sqr(const u256 a) { uint32_t t[16]; sqr_wide(t, a); return reduce(t); }
   SG_HD static u256 add(const u256& a, const u256& b) { return mod_add(a, b, P()); }
   SG_HD static u256 sub(const u256& a, const u256& b) { return mod_sub(a, b, P()); }
   SG_HD static u256 neg(const u256& a) { return mod_neg(a, P()); }
@@ -462,8 +465,8 @@ struct FpR1 {
     return reduce_once(r, P());
   }
 
-  SG_HD static u256 mul(const u256& a, const u256& b) { uint32_t t[16]; mul_wide(t, a, b); return reduce(t); }
-  SG_HD static u256 sqr(const u256& a) { uint32_t t[16]; sqr_wide(t, a); return reduce(t); }
+  SG_NOINL static u256 mul(const u256 a, const u256 b) { uint32_t t[16]; mul_wide(t, a, b); return reduce(t); }
+  SG_NOINL static u256 sqr(const u256 a) { uint32_t t[16]; sqr_wide(t, a); return reduce(t); }
   SG_HD static u256 add(const u256& a, const u256& b) { return mod_add(a, b, P()); }
   SG_HD static u256 sub(const u256& a, const u256& b) { return mod_sub(a, b, P()); }
   SG_HD static u256 neg(const u256& a) { return mod_neg(a, P()); }

@@ -325,6 +325,9 @@ sigops_ctx* sigops_create(int device) {
     sigops_destroy(c);
     return nullptr;
   }
+  int tuned[4];
+  if (tune_cache_lookup(device, tuned))  // a previous sigops_autotune on this device model
+    for (int k = 0; k < 4; ++k) set_variant(c, k, tuned[k]);
   if ((e = cudaMemset(c->d_err, 0, sizeof(uint32_t))) != cudaSuccess) return bail("memset", e);
   return c;
 }

@@ -50,6 +50,9 @@ struct CtxView {
   int batched_variant;
 };
 int ctx_view(sigops_ctx* c, CtxView* v);
+// cached autotuner choice for this device (autotune.cu): variants of the three
+// plain kernels and the batched kernel; false when there is none
+bool tune_cache_lookup(int device, int variants[4]);
 
 cudaError_t launch_field_test(int field, int op, const void* a, const void* b, void* out, int n, cudaStream_t stream);
 cudaError_t launch_sha512_test(const void* in, void* out, int n, cudaStream_t stream);

@@ -83,7 +83,7 @@ struct sigops_server {
   sg::CtxView cv{};
   std::vector<Slot> slots;
   size_t cap = 0;          // items per slot
-  int variant = 3;         // batched-kernel launch variant: 64-thread blocks spread a small batch over many SMs
+  int variant = 0;         // batched-kernel launch variant (256-thread blocks; 64-thread blocks cut saturation by a third)
   int grid_cap = 0;        // blocks of that variant the device holds at once
   size_t queue_bound = 0;  // max queued (not yet launched) items
   Layout lay{};
@@ -138,9 +138,8 @@ void pack_and_launch(sigops_server* s, Slot& sl) {
   cudaMemcpyAsync(sl.d + L.pk, sl.h + L.pk, n * 32, cudaMemcpyHostToDevice, sl.stream);
   size_t cg = (n + 255) / 256;
   int classify_grid = (int)std::min(cg, (size_t)s->cv.num_sms * 8);
-  // grid sized to the batch (one item per thread up to a full persistent grid)
-  // with small blocks: a light batch spreads over many SMs and schedulers, and
-  // launches from other slots run beside it
+  // grid sized to the batch (one item per thread up to a full persistent grid):
+  // a light batch occupies few SMs and launches from other slots run beside it
   const int block = sg::batched_variant_block(s->variant);
   const int grid = (int)std::min<size_t>((size_t)s->grid_cap, (n + block - 1) / block);
   cudaError_t e = sg::launch_batched(sl.d + L.cur, sl.d + L.sig, sl.d + L.msg, sl.d + L.pk, n, sl.d + L.out, sl.d + L.st, sl.d_idx,
@@ -233,7 +232,7 @@ sigops_server* sigops_server_create(sigops_ctx* ctx, int nslots, size_t slot_ite
   s->cap = slot_items;
   s->queue_bound = std::max<size_t>(slot_items * 64, budget_items);
   s->lay = layout(slot_items);
-  s->variant = 3;
+  s->variant = 0;
   const int bps = sg::batched_max_blocks_per_sm(s->variant);
   s->grid_cap = v.num_sms * (bps > 0 ? bps : 1);
   s->slots.resize(nslots);

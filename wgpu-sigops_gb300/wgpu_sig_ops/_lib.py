@@ -58,6 +58,7 @@ SIGNATURES = {
     "sigops_mixed_plan_destroy": (None, [_vp]),
     "sigops_set_variant": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int]),
     "sigops_get_variant": (ctypes.c_int, [_vp, ctypes.c_int] + [ctypes.POINTER(ctypes.c_int)] * 3),
+    "sigops_autotune": (ctypes.c_int, [_vp, _sz, ctypes.c_char_p, _sz]),
     "sigops_workload_sign_ecdsa": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp, _vp, _sz, _vp, _vp, _vp, _vp]),
     "sigops_workload_sign_ed25519": (ctypes.c_int, [_vp, _vp, _vp, _sz, _vp, _vp, _vp]),
     "sigops_server_create": (_vp, [_vp, ctypes.c_int, _sz, ctypes.c_double]),

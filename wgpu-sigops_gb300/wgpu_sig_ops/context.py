@@ -40,6 +40,22 @@ class Context:
         check(lib.sigops_probe_imad(self.ptr, ctypes.byref(v)), "sigops_probe_imad")
         return v.value
 
+    def autotune(self, probe_items: int = 0) -> dict:
+        """Time every launch variant on a device-signed probe batch and keep the fastest."""
+        import json
+
+        buf = ctypes.create_string_buffer(4096)
+        check(lib.sigops_autotune(self.ptr, probe_items, buf, len(buf)), "sigops_autotune")
+        return json.loads(buf.value.decode())
+
+    def variants(self) -> dict:
+        out = {}
+        for k, name in enumerate(("plain_secp256k1", "plain_secp256r1", "plain_ed25519", "batched")):
+            v, g, b = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+            check(lib.sigops_get_variant(self.ptr, k, ctypes.byref(v), ctypes.byref(g), ctypes.byref(b)), "sigops_get_variant")
+            out[name] = {"variant": v.value, "grid": g.value, "block": b.value}
+        return out
+
     def device_info(self) -> dict:
         vals = [ctypes.c_int() for _ in range(4)]
         check(lib.sigops_device_info(self.ptr, *[ctypes.byref(v) for v in vals]), "sigops_device_info")
