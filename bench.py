@@ -12,10 +12,11 @@ One JSON line on stdout (rank 0).  Keys beyond the common contract:
   plain        the plain per-curve kernels over the same batch (split by curve
                before timing): ms_per_step, sigs/s, batched/plain ratio
   selfcheck    every output checked against the outcome the generator knows
-  roofline     IMAD-pipe roofline of the batched kernel: algorithmic IMAD per
-               signature (256 per 256-bit field multiply; 1.201e6 per ECDSA
-               recovery, 0.912e6 per ed25519 verification) x sigs/s against the
-               IMAD rate measured in-process by a dependency-free mad.lo probe
+  roofline     multiply-pipe roofline of the batched engine: 32-bit multiply
+               instructions per signature of each path (profiles/work_model.json,
+               counted by the host build of the kernel source) x sigs/s, against
+               the rate of the same instruction form (mad.lo.cc / madc.hi.cc
+               carry-chain rows) measured in-process
   cpu_baseline the C restatement of the reference's CPU path (oracle port)
                on a bounded sample of the same batch, all host threads; its
                outputs are compared bit for bit with the GPU's on that sample
@@ -37,7 +38,6 @@ sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "wgpu-sigops_gb300"))
 
 METRIC = "sigs/sec on 1 GB300, batched vs plain kernel (bit-exact); serving p50/p99 ms"
-IMAD_PER_SIG = {0: 1.201e6, 1: 1.201e6, 2: 0.912e6}  # frozen work model
 WORKLOAD_DESC = ("mixed-curve batch: 1,048,576 signatures, 40% secp256k1 recover / 30% secp256r1 recover / "
                  "30% ed25519 verify, single-curve requests log-uniform in 1..4096 interleaved, 2% tampered")
 
@@ -277,7 +277,11 @@ def main():
         tune = ctx.autotune()
     info = ctx.device_info()
     info["variants"] = ctx.variants()
-    imad_peak = max(ctx.probe_imad() for _ in range(3))
+    mul_forms = {name: max(ctx.probe_mul(form) for _ in range(3)) for form, name in enumerate(("mad.lo", "mad.hi", "lo/hi chain", "mad.wide"))}
+    mul_peak = mul_forms["lo/hi chain"]
+    with open(os.path.join(ROOT, "profiles", "work_model.json")) as f:
+        wm = json.load(f)
+    split = info["variants"]["batched"]["variant"] >= 4
 
     t_gen = time.perf_counter()
     order, sizes = request_order(args.n, args.seed + dist.rank)
@@ -387,7 +391,8 @@ def main():
     ms_step = dist.max(statistics.mean(ms_b))
     value = dist.sum(n) / (ms_step * 1e-3)
     plain_ms = dist.max(statistics.mean(ms_p))
-    work = sum(IMAD_PER_SIG[c] * counts[c] for c in counts)
+    # the batched engine runs secp256k1 with the GLV split
+    work = wm["secp256k1_glv"] * counts[0] + wm["secp256r1"] * counts[1] + wm["ed25519"] * counts[2]
     achieved = work / (ms_step * 1e-3)
 
     traffic = None
@@ -416,20 +421,26 @@ def main():
         "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
         "data": "synthetic (seeded PCG64 keys/nonces/seeds/messages; signed on the device; 2% tampered on the host)",
         "config": {"workload": WORKLOAD_DESC, "n": n, "mix": {"secp256k1": counts[0], "secp256r1": counts[1], "ed25519": counts[2]},
-                   "requests": int(len(W.requests)), "kernel": "batched persistent mixed-curve, CUDA graph",
+                   "requests": int(len(W.requests)), "kernel": ("batched: classify + three single-curve persistent kernels side by side, CUDA graph" if split
+                              else "batched: classify + fused persistent mixed-curve kernel, CUDA graph"),
                    "l2": "flushed between steps (256 MiB write outside the timed interval)", "grid": info,
                    "parallelism": f"replicas x{dist.world} (weak scaling, no collective)"},
         "selfcheck": selfcheck,
         "plain": {"ms_per_step": plain_ms, "value": dist.sum(n) / (plain_ms * 1e-3), "batched_over_plain": plain_ms / ms_step,
                   "outputs_equal_batched": plain_mismatch == 0, "per_curve": per_curve},
-        "roofline": {"bound": "imad", "achieved": achieved / 1e12, "peak": imad_peak / 1e12, "unit": "TIMAD/s",
-                     "frac": achieved / imad_peak, "traffic": traffic,
-                     "peak_source": "measured in-process: mad.lo.u32 probe (MEASURED_PEAKS.json has no integer figure)",
-                     "work_model": "256 IMAD per 256-bit field multiply; 1.201e6 IMAD per ECDSA recovery, 0.912e6 per ed25519 verify"},
+        "roofline": {"bound": "imad", "achieved": achieved / 1e12, "peak": mul_peak / 1e12, "unit": "Tmul32/s",
+                     "frac": achieved / mul_peak, "traffic": traffic,
+                     "peak_source": ("measured in-process: mad.lo.cc/madc.hi.cc carry-chain rows, the form the field "
+                                     "multiplications issue (MEASURED_PEAKS.json has no integer figure)"),
+                     "peak_forms_T_per_s": {k: v / 1e12 for k, v in mul_forms.items()},
+                     "work_model": ("32-bit multiply instructions per signature, counted by the host build of the kernel source: "
+                                    f"secp256k1 (GLV) {wm['secp256k1_glv']:.0f}, P-256 {wm['secp256r1']:.0f}, "
+                                    f"ed25519 {wm['ed25519']:.0f} (profiles/work_model.json)")},
         "e2e": e2e,
         "serving": serving,
         "cpu_baseline": cpu,
-        "gpu_launches": 2 * args.steps,
+        # per step: classify + the fused kernel, or classify + three single-curve kernels
+        "gpu_launches": (4 if split else 2) * args.steps,
         "clocks": clk,
         "workload_gen_s": t_gen,
         "autotune": tune,

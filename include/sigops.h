@@ -197,8 +197,12 @@ void sigops_mixed_plan_destroy(sigops_plan* plan);
 /* Launch-shape variants (the autotuner's search space).  kernel 0..2: the
  * plain kernel of SIGOPS_SECP256K1 / SECP256R1 / ED25519, variant 0 = one
  * 256-thread block per SM, 1 = two (register budget 128); kernel 3: the
- * batched kernel, variant 0 = 256 threads x 1 block per SM, 1 = 256 x 2,
- * 2 = 128 x 4, 3 = 64-thread blocks (as many per SM as registers allow).
+ * batched engine, variants 0..3 = the fused mixed-curve kernel at 256 threads
+ * x 1 block per SM, 256 x 2, 128 x 4, 64-thread blocks (as many per SM as
+ * registers allow); variants 4 + a + 3 b + 9 c (4..30) = three single-curve
+ * kernels run side by side on forked streams, secp256k1 at occupancy level a,
+ * P-256 at b, ed25519 at c (level 0 = 256 threads x 1 block per SM, 1 = 128
+ * threads x 3 blocks, register budget 170; 2 = 256 x 2, budget 128).
  * sigops_get_variant also reports the grid and block used. */
 int sigops_set_variant(sigops_ctx* ctx, int kernel, int variant);
 int sigops_get_variant(sigops_ctx* ctx, int kernel, int* variant, int* grid, int* block);
@@ -272,6 +276,12 @@ int sigops_sync(sigops_ctx* ctx);
 /* Measured 32-bit integer multiply-add throughput of this device (IMAD per
  * second), from a dependency-free mad.lo probe timed with CUDA events. */
 int sigops_probe_imad(sigops_ctx* ctx, double* imad_per_second);
+
+/* Measured multiply-instruction throughput (per second) of one instruction
+ * form: 0 = mad.lo.u32, 1 = mad.hi.u32, 2 = carry-chain rows alternating
+ * mad.lo.cc / madc.hi.cc (the form of the field multiplications), 3 =
+ * mad.wide.u32.  No counterpart in the reference; the roofline denominator. */
+int sigops_probe_mul(sigops_ctx* ctx, int form, double* per_second);
 
 /* Number of SMs and the plain kernels' grid (blocks) for `curve`. */
 int sigops_device_info(sigops_ctx* ctx, int* num_sms, int* plain_grid_k1, int* plain_grid_r1, int* plain_grid_ed);

@@ -63,6 +63,14 @@ void hc_mul_wide(const uint8_t* a, const uint8_t* b, uint8_t* out64) {
   memcpy(out64, t, 64);
 }
 
+// which = 0: schoolbook, 1: Karatsuba
+void hc_mul_wide_form(int which, const uint8_t* a, const uint8_t* b, uint8_t* out64) {
+  uint32_t t[16];
+  if (which) mul_wide_kara(t, load_le(a), load_le(b));
+  else mul_wide_school(t, load_le(a), load_le(b));
+  memcpy(out64, t, 64);
+}
+
 int hc_k1_recover(const uint8_t* sig, const uint8_t* msg, uint8_t* out) {
   init();
   uint32_t s[16], m[8], o[16];
@@ -114,6 +122,13 @@ extern "C" void hc_ed_sign(const uint8_t* seed, const uint8_t* msg, uint8_t* sig
   memcpy(sd, seed, 32); memcpy(m, msg, 32);
   ed25519_sign(sd, m, g_ed, s, p);
   memcpy(sig, s, 64); memcpy(pk, p, 32);
+}
+
+// multiply instructions counted since the last reset (this thread)
+extern "C" uint64_t hc_mulcount(int reset) {
+  const uint64_t c = mulcount_();
+  if (reset) mulcount_() = 0;
+  return c;
 }
 
 extern "C" void hc_sqr_wide(const uint8_t* a, uint8_t* out64) {

@@ -109,12 +109,29 @@ def test_matches_plain_kernels(w):
     assert (valid == out[sel, 0]).all() and (st == status[sel]).all()
 
 
-def test_graph_plan_replays(w):
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 17, 30, 4 + 2 + 3 * 1, 4 + 1 + 9 * 2])
+def test_every_launch_variant(w, variant):
+    """Fused (0..3) and single-curve (4..30) variants give the oracle's results,
+    on a mixed batch and on ragged ones that leave some curves empty."""
+    ctx = w.Context(0)
+    ctx.set_variant(3, variant)
+    assert ctx.variants()["batched"]["variant"] == variant
+    for n, seed in ((400, 61), (1, 62), (33, 63)):
+        items = random_items(n, seed=seed)
+        out, status = w.batch.verify_mixed(*zip(*items), ctx=ctx)
+        for k, (exp, st) in enumerate(oracle_mixed(items)):
+            assert out[k].tobytes() == exp and status[k] == st, (variant, n, k)
+    ctx.close()
+
+
+@pytest.mark.parametrize("variant", [0, 30])
+def test_graph_plan_replays(w, variant):
     import torch
 
     from wgpu_sig_ops._lib import check, lib
 
-    ctx = w.default_context()
+    ctx = w.Context(0)
+    ctx.set_variant(3, variant)
     items = random_items(200, seed=44)
     ref_out, ref_st = w.batch.verify_mixed(*zip(*items))
     cur, sig, msg, pk = zip(*items)
@@ -133,6 +150,7 @@ def test_graph_plan_replays(w):
         check(lib.sigops_sync(ctx.ptr), "sync")
         assert (d_out.cpu().numpy() == ref_out).all() and (d_st.cpu().numpy() == ref_st).all()
     plan.close()
+    ctx.close()
 
 
 def test_rejects_bad_curve_tag(w):

@@ -46,6 +46,24 @@ def test_mul_wide(hc):
         assert int.from_bytes(out.raw, "little") == a * b
 
 
+@pytest.mark.parametrize("form", [0, 1], ids=["schoolbook", "karatsuba"])
+def test_mul_wide_forms(hc, form):
+    """Both 512-bit product forms, including the sign cases of the Karatsuba
+    middle term (halves equal, a0 < a1 with b1 < b0, ...) and all-ones limbs."""
+    rng = random.Random(50 + form)
+    h = 2**128
+    cases = [(2**256 - 1, 2**256 - 1), (0, 0), (1, 2**256 - 1), (h, h), (h - 1, h), (h * 5 + 3, h * 3 + 5), (3 * h + 5, 5 * h + 3)]
+    for _ in range(400):
+        a1, a0, b1, b0 = (rng.choice([rng.getrandbits(128), 0, h - 1, rng.getrandbits(8)]) for _ in range(4))
+        cases.append((a1 * h + a0, b1 * h + b0))
+    cases += [(rng.getrandbits(256), rng.getrandbits(256)) for _ in range(400)]
+    hc.hc_mul_wide_form.argtypes = [ctypes.c_int, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p]
+    for a, b in cases:
+        out = ctypes.create_string_buffer(64)
+        hc.hc_mul_wide_form(form, le(a), le(b), out)
+        assert int.from_bytes(out.raw, "little") == a * b, (hex(a), hex(b))
+
+
 def test_sqr_wide(hc):
     rng = random.Random(6)
     cases = [2**256 - 1, 0, 1, 2**255, 2**32 - 1] + [rng.getrandbits(256) for _ in range(500)]

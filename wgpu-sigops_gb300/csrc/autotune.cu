@@ -142,6 +142,12 @@ extern "C" int sigops_autotune(sigops_ctx* ctx, size_t probe_items, char* report
     cudaStreamDestroy(st);
     return SIGOPS_E_CUDA;
   }
+  sg::ForkStreams fork;
+  if (sg::fork_streams_create(&fork) != cudaSuccess) {
+    sg::fork_streams_destroy(&fork);
+    cudaStreamDestroy(st);
+    return SIGOPS_E_CUDA;
+  }
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
@@ -173,7 +179,7 @@ extern "C" int sigops_autotune(sigops_ctx* ctx, size_t probe_items, char* report
       int classify_grid = (int)std::min(cg, (size_t)v.num_sms * 8);
       float ms = time_it([&] {
         sg::launch_batched(d.p + o_cur, d.p + o_sig, d.p + o_msg, d.p + o_pk, n, d.p + o_out, d.p + o_st, (uint32_t*)(d.p + o_idx),
-                           d.p + o_scr, v.gtab[0], v.gtab[1], v.gtab[2], v.d_err, grid, var, classify_grid, st);
+                           d.p + o_scr, v.gtab[0], v.gtab[1], v.gtab[2], v.d_err, grid, var, classify_grid, v.num_sms, &fork, st);
       });
       char b[96];
       snprintf(b, sizeof b, "%s\"%d\": %.3f", var ? ", " : "", var, ms);
@@ -214,6 +220,7 @@ extern "C" int sigops_autotune(sigops_ctx* ctx, size_t probe_items, char* report
   rep += b;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  sg::fork_streams_destroy(&fork);
   cudaStreamDestroy(st);
   for (int k = 0; k < 4; ++k) {
     int rc = sigops_set_variant(ctx, k, chosen[k]);

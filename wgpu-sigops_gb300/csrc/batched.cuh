@@ -1,5 +1,5 @@
-// Batched mixed-curve engine: one persistent launch verifies a batch that
-// mixes secp256k1 recovery, P-256 recovery and ed25519 verification.
+// Batched mixed-curve engine: verifies a batch that mixes secp256k1 recovery,
+// P-256 recovery and ed25519 verification.
 //
 // The reference runs one curve per call and pads every batch to a power of two
 // (src/secp256k1_ecdsa.rs:25-44); it has no mixed-curve path.  Here:
@@ -8,8 +8,12 @@
 //   2. batched_kernel runs a persistent grid: each warp repeatedly takes the
 //      next 32-item tile from a global counter; tiles never straddle curves, so
 //      the curve dispatch is warp-uniform and no lane idles on another curve's
-//      code.  All three generator tables are staged into shared memory by bulk
-//      (TMA) copies completing on one mbarrier.
+//      code.  The generator tables it needs are staged into shared memory by
+//      bulk (TMA) copies completing on one mbarrier.
+// The curve mask CM selects what one launch serves: CM_ALL is the fused
+// kernel (one queue over all three curves, registers sized for the largest
+// path); a single-curve mask gives a kernel with that curve's own register
+// budget, and the three are launched side by side on forked streams.
 // Scratch (global memory beyond inputs and outputs): Scratch below.
 #pragma once
 #include "kernels.cuh"
@@ -19,11 +23,14 @@ namespace sg {
 constexpr int BATCH_TILE = 32;  // items per warp work unit
 constexpr uint32_t QUEUE_MAX_SPINS = 1u << 20;
 
+// curve masks of batched_kernel
+constexpr int CM_K1 = 1, CM_R1 = 2, CM_ED = 4, CM_ALL = 7;
+
 struct Scratch {
-  uint32_t count[3];    // items per curve (classify)
-  uint32_t next_tile;   // work-stealing counter (batched)
-  uint32_t tiles_done;  // completed tiles (diagnostic)
-  uint32_t pad[3];
+  uint32_t count[3];            // items per curve (classify)
+  uint32_t next_tile;           // work-stealing counter of the fused kernel
+  uint32_t tiles_done;          // unused; keeps the record at 32 bytes
+  uint32_t next_curve_tile[3];  // work-stealing counters of the single-curve kernels
 };
 
 // Mixed output record: ECDSA key bytes, or for ed25519 byte 0 = valid.
@@ -43,10 +50,12 @@ struct BatchTables {
   const uint32_t* ed;
 };
 
-// all three tables into shared memory with bulk copies on one mbarrier
-__device__ __forceinline__ bool stage_three(uint32_t* sk1, uint32_t* sr1, uint32_t* sed, const BatchTables& t, uint64_t* bar, uint32_t* err) {
+// the tables a launch needs into shared memory, bulk copies on one mbarrier
+template <int CM>
+__device__ __forceinline__ bool stage_tables(uint32_t* sk1, uint32_t* sr1, uint32_t* sed, const BatchTables& t, uint64_t* bar, uint32_t* err) {
   const uint32_t b = smem_addr(bar);
-  const uint32_t bk = ECDSA_GTAB * 64, bk2 = 2 * ECDSA_GTAB * 64, be = ED_GTAB * 96;
+  constexpr uint32_t bk2 = (CM & CM_K1) ? 2 * ECDSA_GTAB * 64 : 0, bk = (CM & CM_R1) ? ECDSA_GTAB * 64 : 0,
+                     be = (CM & CM_ED) ? ED_GTAB * 96 : 0;
   if (threadIdx.x == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b) : "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -54,15 +63,18 @@ __device__ __forceinline__ bool stage_three(uint32_t* sk1, uint32_t* sr1, uint32
   __syncthreads();
   if (threadIdx.x == 0) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(bk2 + bk + be) : "memory");
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_addr(sk1)), "l"(t.k1),
-                 "r"(bk2), "r"(b)
-                 : "memory");
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_addr(sr1)), "l"(t.r1),
-                 "r"(bk), "r"(b)
-                 : "memory");
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_addr(sed)), "l"(t.ed),
-                 "r"(be), "r"(b)
-                 : "memory");
+    if (bk2)
+      asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_addr(sk1)),
+                   "l"(t.k1), "r"(bk2), "r"(b)
+                   : "memory");
+    if (bk)
+      asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_addr(sr1)),
+                   "l"(t.r1), "r"(bk), "r"(b)
+                   : "memory");
+    if (be)
+      asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_addr(sed)),
+                   "l"(t.ed), "r"(be), "r"(b)
+                   : "memory");
   }
   uint32_t done = 0;
   for (uint32_t i = 0; i < STAGE_MAX_POLLS && !done; ++i) {
@@ -78,22 +90,38 @@ __device__ __forceinline__ bool stage_three(uint32_t* sk1, uint32_t* sr1, uint32
   return true;
 }
 
-template <int BLOCK, int MINB>
+// ed25519 item of a batch: out byte 0 = valid, the rest zero
+__device__ __forceinline__ uint8_t ed_item(const MixedIO& io, size_t i, const uint32_t s[16], const uint32_t m[8], const uint32_t* ted,
+                                           uint32_t o[16]) {
+  uint32_t p[8];
+  load_words(io.pks, i, 8, p);
+  const uint8_t st = ed25519_verify(s, m, p, ted);
+#pragma unroll
+  for (int k = 0; k < 16; ++k) o[k] = 0;
+  o[0] = st == ST_OK;
+  return st;
+}
+
+template <int BLOCK, int MINB, int CM>
 __global__ void __launch_bounds__(BLOCK, MINB) batched_kernel(MixedIO io, const uint32_t* __restrict__ idx, BatchTables tabs, Scratch* sc,
                                                         uint32_t* err) {
-  __shared__ __align__(128) uint32_t tk1[2 * ECDSA_GTAB * 16];  // G and 2^128 G multiples (GLV)
-  __shared__ __align__(128) uint32_t tr1[ECDSA_GTAB * 16];
-  __shared__ __align__(128) uint32_t ted[ED_GTAB * 24];
+  __shared__ __align__(128) uint32_t tk1[(CM & CM_K1) ? 2 * ECDSA_GTAB * 16 : 4];  // G and 2^128 G multiples (GLV)
+  __shared__ __align__(128) uint32_t tr1[(CM & CM_R1) ? ECDSA_GTAB * 16 : 4];
+  __shared__ __align__(128) uint32_t ted[(CM & CM_ED) ? ED_GTAB * 24 : 4];
   __shared__ __align__(8) uint64_t bar;
-  if (!stage_three(tk1, tr1, ted, tabs, &bar, err)) return;
+  if (!stage_tables<CM>(tk1, tr1, ted, tabs, &bar, err)) return;
 
-  const uint32_t n1 = sc->count[0], n2 = sc->count[1], n3 = sc->count[2];
+  const uint32_t n1 = (CM & CM_K1) ? sc->count[0] : 0, n2 = (CM & CM_R1) ? sc->count[1] : 0, n3 = (CM & CM_ED) ? sc->count[2] : 0;
   const uint32_t t1 = (n1 + BATCH_TILE - 1) / BATCH_TILE, t2 = (n2 + BATCH_TILE - 1) / BATCH_TILE, t3 = (n3 + BATCH_TILE - 1) / BATCH_TILE;
   const uint32_t total = t1 + t2 + t3;
+  uint32_t* counter = CM == CM_K1 ? &sc->next_curve_tile[0]
+                      : CM == CM_R1 ? &sc->next_curve_tile[1]
+                      : CM == CM_ED ? &sc->next_curve_tile[2]
+                                    : &sc->next_tile;
   const unsigned lane = threadIdx.x & 31u;
   for (;;) {
     uint32_t tile = 0;
-    if (lane == 0) tile = atomicAdd(&sc->next_tile, 1u);
+    if (lane == 0) tile = atomicAdd(counter, 1u);
     tile = __shfl_sync(0xffffffffu, tile, 0);
     if (tile >= total) break;
     int curve;
@@ -108,17 +136,17 @@ __global__ void __launch_bounds__(BLOCK, MINB) batched_kernel(MixedIO io, const 
       load_words(io.sigs, i, 16, s);
       load_words(io.msgs, i, 8, m);
       uint8_t st;
-      if (curve == 0) {
+      if constexpr (CM == CM_K1) {
         st = ecdsa_recover<K1Traits, true>(s, m, tk1, o);
-      } else if (curve == 1) {
+      } else if constexpr (CM == CM_R1) {
         st = ecdsa_recover<R1Traits>(s, m, tr1, o);
+      } else if constexpr (CM == CM_ED) {
+        st = ed_item(io, i, s, m, ted, o);
       } else {
-        uint32_t p[8];
-        load_words(io.pks, i, 8, p);
-        st = ed25519_verify(s, m, p, ted);
-#pragma unroll
-        for (int k = 0; k < 16; ++k) o[k] = 0;
-        o[0] = st == ST_OK;
+        static_assert(CM == CM_ALL, "one curve or all three");
+        if (curve == 0) st = ecdsa_recover<K1Traits, true>(s, m, tk1, o);
+        else if (curve == 1) st = ecdsa_recover<R1Traits>(s, m, tr1, o);
+        else st = ed_item(io, i, s, m, ted, o);
       }
       store_words(io.out, i, 16, o);
       io.status[i] = st;

@@ -97,6 +97,7 @@ struct sigops_ctx {
   size_t idx_cap = 0;
   int batched_variant = 0;
   int batched_grid = 0;
+  ForkStreams fork{};  // side streams of the single-curve batched variants
   std::mutex mu;
 };
 
@@ -183,7 +184,7 @@ cudaError_t launch_mixed(sigops_ctx* c, const uint8_t* curves, const uint8_t* si
   size_t cg = (n + 255) / 256;
   int classify_grid = (int)(cg < (size_t)c->num_sms * 8 ? cg : (size_t)c->num_sms * 8);
   return launch_batched(curves, sigs, msgs, pks, n, out, status, c->d_idx, c->d_scratch, c->d_gtab[0], c->d_gtab[1], c->d_gtab[2], c->d_err,
-                        c->batched_grid, c->batched_variant, classify_grid, s);
+                        c->batched_grid, c->batched_variant, classify_grid, c->num_sms, &c->fork, s);
 }
 
 int check_device_errors(sigops_ctx* c) {
@@ -309,6 +310,7 @@ sigops_ctx* sigops_create(int device) {
   cudaError_t e;
   if ((e = cudaSetDevice(device)) != cudaSuccess) return bail("cudaSetDevice", e);
   if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess) return bail("cudaStreamCreate", e);
+  if ((e = fork_streams_create(&c->fork)) != cudaSuccess) return bail("side streams", e);
   if ((e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device)) != cudaSuccess) return bail("attr", e);
   for (int k = 0; k < 3; ++k) {
     const auto& t = host_tables().gtab[k];
@@ -344,6 +346,7 @@ void sigops_destroy(sigops_ctx* c) {
   if (c->d_buf) cudaFree(c->d_buf);
   if (c->h_buf) cudaFreeHost(c->h_buf);
   if (c->stream) cudaStreamDestroy(c->stream);
+  fork_streams_destroy(&c->fork);
   {
     std::lock_guard<std::mutex> g(g_default_mu);
     if (g_default == c) g_default = nullptr;
@@ -611,8 +614,8 @@ int sigops_sync(sigops_ctx* ctx) {
   return check_device_errors(c);
 }
 
-int sigops_probe_imad(sigops_ctx* ctx, double* rate) {
-  if (!rate) return fail(SIGOPS_E_INVAL, "null output");
+int sigops_probe_mul(sigops_ctx* ctx, int form, double* rate) {
+  if (!rate || form < 0 || form > 3) return fail(SIGOPS_E_INVAL, "bad probe form %d or null output", form);
   sigops_ctx* c = resolve(ctx);
   if (!c) return SIGOPS_E_NODEV;
   std::lock_guard<std::mutex> g(c->mu);
@@ -624,9 +627,9 @@ int sigops_probe_imad(sigops_ctx* ctx, double* rate) {
   cudaEvent_t a, b;
   SG_CUDA(cudaEventCreate(&a));
   SG_CUDA(cudaEventCreate(&b));
-  SG_CUDA(launch_imad_probe(d_out, 64, grid, block, c->stream));  // warm-up
+  SG_CUDA(launch_mul_probe(form, d_out, 16, grid, block, c->stream));  // warm-up
   SG_CUDA(cudaEventRecord(a, c->stream));
-  SG_CUDA(launch_imad_probe(d_out, iters, grid, block, c->stream));
+  SG_CUDA(launch_mul_probe(form, d_out, iters, grid, block, c->stream));
   SG_CUDA(cudaEventRecord(b, c->stream));
   SG_CUDA(cudaEventSynchronize(b));
   float ms = 0;
@@ -634,10 +637,12 @@ int sigops_probe_imad(sigops_ctx* ctx, double* rate) {
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   cudaFree(d_out);
-  double ops = (double)grid * block * iters * 8.0 * 16.0;
-  *rate = ops / (ms * 1e-3);
+  const double per_iter = form == 3 ? 8.0 * 8.0 : 8.0 * 16.0;
+  *rate = (double)grid * block * iters * per_iter / (ms * 1e-3);
   return SIGOPS_OK;
 }
+
+int sigops_probe_imad(sigops_ctx* ctx, double* rate) { return sigops_probe_mul(ctx, 0, rate); }
 
 int sigops_device_info(sigops_ctx* ctx, int* num_sms, int* g1, int* g2, int* g3) {
   sigops_ctx* c = resolve(ctx);

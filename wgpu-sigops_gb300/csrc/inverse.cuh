@@ -70,6 +70,7 @@ SG_HD int32_t divsteps30(int32_t delta, uint32_t f, uint32_t g, int32_t t[4]) {
 
 // (f, g) <- (u f + v g, q f + r g) / 2^30, exact
 SG_HD void s30_update_fg(S30& f, S30& g, const int32_t t[4]) {
+  SG_COUNT_MULS(2 * 4 * 9);  // 36 wide products
   const int64_t u = t[0], v = t[1], q = t[2], r = t[3];
   int64_t cf = u * f.v[0] + v * g.v[0];
   int64_t cg = q * f.v[0] + r * g.v[0];
@@ -91,6 +92,7 @@ SG_HD void s30_update_fg(S30& f, S30& g, const int32_t t[4]) {
 // (d, e) <- (u d + v e, q d + r e) / 2^30 mod M, keeping both in (-2M, M):
 // a multiple of M chosen to clear the low 30 bits is added before the shift
 SG_HD void s30_update_de(S30& d, S30& e, const int32_t t[4], const S30& M, uint32_t minv30) {
+  SG_COUNT_MULS(2 * 6 * 9 + 2);  // 54 wide products and two low ones
   const int32_t u = t[0], v = t[1], q = t[2], r = t[3];
   const int32_t sd = d.v[8] >> 31, se = e.v[8] >> 31;
   int32_t md = (u & sd) + (v & se);

@@ -1,4 +1,7 @@
 // Batched mixed-curve engine: classify kernel, variant dispatch.
+#include <algorithm>
+#include <atomic>
+
 #include "batched.cuh"
 
 namespace sg {
@@ -27,15 +30,46 @@ int batched_occupancy_0();
 int batched_occupancy_1();
 int batched_occupancy_2();
 int batched_occupancy_3();
+int batched_occupancy_k1(int minb);
+int batched_occupancy_r1(int minb);
+int batched_occupancy_ed(int minb);
 cudaError_t batched_launch_0(const MixedIO&, const uint32_t*, const BatchTables&, Scratch*, uint32_t*, int, cudaStream_t);
 cudaError_t batched_launch_1(const MixedIO&, const uint32_t*, const BatchTables&, Scratch*, uint32_t*, int, cudaStream_t);
 cudaError_t batched_launch_2(const MixedIO&, const uint32_t*, const BatchTables&, Scratch*, uint32_t*, int, cudaStream_t);
 cudaError_t batched_launch_3(const MixedIO&, const uint32_t*, const BatchTables&, Scratch*, uint32_t*, int, cudaStream_t);
+cudaError_t batched_launch_k1(int, const MixedIO&, const uint32_t*, const BatchTables&, Scratch*, uint32_t*, int, cudaStream_t);
+cudaError_t batched_launch_r1(int, const MixedIO&, const uint32_t*, const BatchTables&, Scratch*, uint32_t*, int, cudaStream_t);
+cudaError_t batched_launch_ed(int, const MixedIO&, const uint32_t*, const BatchTables&, Scratch*, uint32_t*, int, cudaStream_t);
 
-// variants: 0 = 256 threads x 1 block/SM, 1 = 256 x 2, 2 = 128 x 4, 3 = 64 threads
-static const int kBlock[BATCHED_VARIANTS] = {256, 256, 128, 64};
+static const int kFusedBlock[BATCHED_FUSED_VARIANTS] = {256, 256, 128, 64};
 
-int batched_variant_block(int v) { return (v >= 0 && v < BATCHED_VARIANTS) ? kBlock[v] : 0; }
+// single-curve kernels: occupancy level 0 = 256 threads x 1 block per SM,
+// 1 = 128 x 3, 2 = 256 x 2 (8, 12 and 16 warps per SM)
+static const int kLevelBlock[3] = {256, 128, 256};
+
+// blocks per SM of curve c's single-curve kernel at an occupancy level
+// (queried once; the kernels are the same on every device of one process)
+static int curve_occupancy(int c, int level) {
+  static std::atomic<int> cache[3][3];
+  int b = cache[c][level].load(std::memory_order_relaxed);
+  if (b == 0) {
+    b = c == 0 ? batched_occupancy_k1(level) : c == 1 ? batched_occupancy_r1(level) : batched_occupancy_ed(level);
+    cache[c][level].store(b, std::memory_order_relaxed);
+  }
+  return b;
+}
+
+// variant 4 + a + 3 b + 9 c: levels a, b, c for secp256k1, P-256, ed25519
+static int split_level(int variant, int c) {
+  int v = variant - BATCHED_FUSED_VARIANTS;
+  for (int k = 0; k < c; ++k) v /= 3;
+  return v % 3;
+}
+
+int batched_variant_block(int v) {
+  if (v >= 0 && v < BATCHED_FUSED_VARIANTS) return kFusedBlock[v];
+  return (v >= BATCHED_FUSED_VARIANTS && v < BATCHED_VARIANTS) ? 256 : 0;
+}
 
 int batched_max_blocks_per_sm(int v) {
   switch (v) {
@@ -43,14 +77,51 @@ int batched_max_blocks_per_sm(int v) {
     case 1: return batched_occupancy_1();
     case 2: return batched_occupancy_2();
     case 3: return batched_occupancy_3();
-    default: return 0;
+    default: break;
   }
+  if (v < BATCHED_FUSED_VARIANTS || v >= BATCHED_VARIANTS) return 0;
+  // in 256-thread blocks: the grid cap of a single-curve variant
+  int m = 0;
+  for (int c = 0; c < 3; ++c) {
+    const int l = split_level(v, c);
+    const int b = curve_occupancy(c, l) * kLevelBlock[l] / 256;
+    if (b <= 0) return 0;
+    m = b > m ? b : m;
+  }
+  return m;
+}
+
+cudaError_t fork_streams_create(ForkStreams* f) {
+  *f = ForkStreams{};
+  cudaError_t e;
+  for (int k = 0; k < 2; ++k)
+    if ((e = cudaStreamCreateWithFlags(&f->aux[k], cudaStreamNonBlocking)) != cudaSuccess) return e;
+  for (int k = 0; k < 3; ++k)
+    if ((e = cudaEventCreateWithFlags(&f->ev[k], cudaEventDisableTiming)) != cudaSuccess) return e;
+  return cudaSuccess;
+}
+
+void fork_streams_destroy(ForkStreams* f) {
+  for (int k = 0; k < 2; ++k)
+    if (f->aux[k]) cudaStreamDestroy(f->aux[k]);
+  for (int k = 0; k < 3; ++k)
+    if (f->ev[k]) cudaEventDestroy(f->ev[k]);
+  *f = ForkStreams{};
+}
+
+static cudaError_t launch_curve(int c, int level, const MixedIO& io, const uint32_t* idx, const BatchTables& t, Scratch* sc,
+                                uint32_t* err, int grid, cudaStream_t s) {
+  if (c == 0) return batched_launch_k1(level, io, idx, t, sc, err, grid, s);
+  if (c == 1) return batched_launch_r1(level, io, idx, t, sc, err, grid, s);
+  return batched_launch_ed(level, io, idx, t, sc, err, grid, s);
 }
 
 cudaError_t launch_batched(const uint8_t* curves, const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks, size_t n, uint8_t* out,
                            uint8_t* status, uint32_t* idx, void* scratch, const uint32_t* gk1, const uint32_t* gr1, const uint32_t* ged,
-                           uint32_t* err, int grid, int variant, int classify_grid, cudaStream_t stream) {
+                           uint32_t* err, int grid, int variant, int classify_grid, int num_sms, const ForkStreams* fork,
+                           cudaStream_t stream) {
   if (n == 0) return cudaSuccess;
+  if (variant < 0 || variant >= BATCHED_VARIANTS || grid <= 0) return cudaErrorInvalidValue;
   Scratch* sc = (Scratch*)scratch;
   cudaError_t e = cudaMemsetAsync(sc, 0, sizeof(Scratch), stream);
   if (e != cudaSuccess) return e;
@@ -62,8 +133,38 @@ cudaError_t launch_batched(const uint8_t* curves, const uint8_t* sigs, const uin
     case 1: return batched_launch_1(io, idx, t, sc, err, grid, stream);
     case 2: return batched_launch_2(io, idx, t, sc, err, grid, stream);
     case 3: return batched_launch_3(io, idx, t, sc, err, grid, stream);
-    default: return cudaErrorInvalidValue;
+    default: break;
   }
+  // single-curve kernels: secp256k1 on the caller's stream, the other two on
+  // the side streams, so that each starts filling SMs as another's blocks retire
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  cudaStream_t s[3] = {stream, stream, stream};
+  if (fork) {
+    if ((e = cudaEventRecord(fork->ev[0], stream)) != cudaSuccess) return e;
+    for (int k = 0; k < 2; ++k) {
+      if ((e = cudaStreamWaitEvent(fork->aux[k], fork->ev[0], 0)) != cudaSuccess) return e;
+      s[k + 1] = fork->aux[k];
+    }
+  }
+  cudaError_t first = cudaSuccess;
+  for (int c = 0; c < 3; ++c) {
+    // blocks: a full persistent grid, at most one item per thread, and at most
+    // the caller's grid (counted in 256-thread blocks)
+    const int l = split_level(variant, c), block = kLevelBlock[l];
+    size_t g = (size_t)num_sms * curve_occupancy(c, l);
+    g = std::min(g, (n + block - 1) / block);
+    g = std::min(g, (size_t)grid * 256 / block);
+    e = launch_curve(c, l, io, idx, t, sc, err, (int)std::max<size_t>(g, 1), s[c]);
+    if (e != cudaSuccess && first == cudaSuccess) first = e;
+  }
+  if (fork) {  // join, even after a failed launch, so no side stream stays forked
+    for (int k = 0; k < 2; ++k) {
+      e = cudaEventRecord(fork->ev[k + 1], fork->aux[k]);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(stream, fork->ev[k + 1], 0);
+      if (e != cudaSuccess && first == cudaSuccess) first = e;
+    }
+  }
+  return first;
 }
 
 size_t batched_scratch_bytes() { return sizeof(Scratch); }

@@ -5,13 +5,13 @@ namespace sg {
 
 int batched_occupancy_1() {
   int b = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, batched_kernel<256, 2>, 256, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, batched_kernel<256, 2, CM_ALL>, 256, 0);
   return b;
 }
 
 cudaError_t batched_launch_1(const MixedIO& io, const uint32_t* idx, const BatchTables& t, Scratch* sc, uint32_t* err, int grid,
                                cudaStream_t stream) {
-  batched_kernel<256, 2><<<grid, 256, 0, stream>>>(io, idx, t, sc, err);
+  batched_kernel<256, 2, CM_ALL><<<grid, 256, 0, stream>>>(io, idx, t, sc, err);
   return cudaGetLastError();
 }
 

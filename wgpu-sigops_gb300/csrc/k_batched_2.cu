@@ -5,13 +5,13 @@ namespace sg {
 
 int batched_occupancy_2() {
   int b = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, batched_kernel<128, 4>, 128, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, batched_kernel<128, 4, CM_ALL>, 128, 0);
   return b;
 }
 
 cudaError_t batched_launch_2(const MixedIO& io, const uint32_t* idx, const BatchTables& t, Scratch* sc, uint32_t* err, int grid,
                                cudaStream_t stream) {
-  batched_kernel<128, 4><<<grid, 128, 0, stream>>>(io, idx, t, sc, err);
+  batched_kernel<128, 4, CM_ALL><<<grid, 128, 0, stream>>>(io, idx, t, sc, err);
   return cudaGetLastError();
 }
 

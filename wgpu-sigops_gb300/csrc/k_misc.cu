@@ -77,6 +77,47 @@ __global__ void imad_probe_kernel(uint32_t* out, uint32_t iters, uint32_t seed) 
   if (x == 0x9e3779b9u) out[0] = x;  // keeps the chains live
 }
 
+// Throughput probe of the multiply forms the field arithmetic issues.
+// form 1: mad.hi.u32; 2: carry-chain rows alternating mad.lo.cc / madc.hi.cc
+// (two independent 8-instruction chains per iteration, the shape of one row of
+// a 256-bit product); 3: mad.wide.u32.  Counts are multiply instructions.
+template <int FORM>
+__global__ void mul_probe_kernel(uint32_t* out, uint32_t iters, uint32_t seed) {
+  uint32_t acc[16];
+#pragma unroll
+  for (int k = 0; k < 16; ++k) acc[k] = seed + threadIdx.x * 17u + k;
+  const uint32_t m = seed | 1u;
+  for (uint32_t it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+      if constexpr (FORM == 1) {
+#pragma unroll
+        for (int k = 0; k < 16; ++k) asm volatile("mad.hi.u32 %0, %0, %1, %2;" : "+r"(acc[k]) : "r"(m), "r"(k));
+      } else if constexpr (FORM == 2) {
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+          acc[8 * c] = mad_lo_cc(acc[8 * c + 1], m, acc[8 * c]);
+#pragma unroll
+          for (int j = 1; j < 8; ++j)
+            acc[8 * c + j] = (j & 1) ? madc_hi_cc(acc[8 * c + j - 1], m, acc[8 * c + j]) : madc_lo_cc(acc[8 * c + j - 1], m, acc[8 * c + j]);
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k < 16; k += 2) {
+          uint64_t w = ((uint64_t)acc[k + 1] << 32) | acc[k];
+          asm volatile("mad.wide.u32 %0, %1, %2, %0;" : "+l"(w) : "r"(acc[(k + 2) & 15]), "r"(m));
+          acc[k] = (uint32_t)w;
+          acc[k + 1] = (uint32_t)(w >> 32);
+        }
+      }
+    }
+  }
+  uint32_t x = 0;
+#pragma unroll
+  for (int k = 0; k < 16; ++k) x ^= acc[k];
+  if (x == 0x9e3779b9u) out[0] = x;  // keeps the chains live
+}
+
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
@@ -112,6 +153,18 @@ cudaError_t launch_sha512_test(const void* in, void* out, int n, cudaStream_t st
 
 cudaError_t launch_imad_probe(uint32_t* out, uint32_t iters, int grid, int block, cudaStream_t stream) {
   imad_probe_kernel<<<grid, block, 0, stream>>>(out, iters, 12345u);
+  return cudaGetLastError();
+}
+
+// multiply instructions per thread per iteration: 128 (forms 0..2), 8 wide (3)
+cudaError_t launch_mul_probe(int form, uint32_t* out, uint32_t iters, int grid, int block, cudaStream_t stream) {
+  switch (form) {
+    case 0: imad_probe_kernel<<<grid, block, 0, stream>>>(out, iters, 12345u); break;
+    case 1: mul_probe_kernel<1><<<grid, block, 0, stream>>>(out, iters, 12345u); break;
+    case 2: mul_probe_kernel<2><<<grid, block, 0, stream>>>(out, iters, 12345u); break;
+    case 3: mul_probe_kernel<3><<<grid, block, 0, stream>>>(out, iters, 12345u); break;
+    default: return cudaErrorInvalidValue;
+  }
   return cudaGetLastError();
 }
 

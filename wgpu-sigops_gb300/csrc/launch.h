@@ -32,14 +32,30 @@ cudaError_t launch_sign_ecdsa(int curve, const uint8_t* secrets, const uint8_t* 
 cudaError_t launch_sign_ed(const uint8_t* seeds, const uint8_t* msgs, size_t n, const uint32_t* btab, uint8_t* sigs, uint8_t* pks,
                            uint32_t* err, int grid, cudaStream_t stream);
 // batched mixed-curve engine: scratch = Scratch record + 3*n u32 index lists.
-// variants: 0 = 256 threads x 1 block/SM, 1 = 256 x 2, 2 = 128 x 4, 3 = 64 threads
-constexpr int BATCHED_VARIANTS = 4;
+// variants 0..3: the fused kernel (0 = 256 threads x 1 block/SM, 1 = 256 x 2,
+// 2 = 128 x 4, 3 = 64 threads); variants 4 + a + 3 b + 9 c (4..30): three
+// single-curve kernels (secp256k1 at occupancy level a, P-256 at b, ed25519
+// at c; level 0 = 256 threads x 1 block per SM, 1 = 128 x 3, 2 = 256 x 2).
+constexpr int BATCHED_FUSED_VARIANTS = 4;
+constexpr int BATCHED_VARIANTS = 31;
 int batched_variant_block(int variant);
 int batched_max_blocks_per_sm(int variant);
 size_t batched_scratch_bytes();
+// side streams and events on which the single-curve kernels run beside each
+// other (fork after the classify kernel, join before returning); without them
+// the three kernels run one after another on the caller's stream
+struct ForkStreams {
+  cudaStream_t aux[2];
+  cudaEvent_t ev[3];
+};
+cudaError_t fork_streams_create(ForkStreams* f);
+void fork_streams_destroy(ForkStreams* f);
+// grid: blocks of the fused kernel, or the cap on each single-curve kernel's
+// grid (which is also bounded by num_sms x its occupancy)
 cudaError_t launch_batched(const uint8_t* curves, const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks, size_t n, uint8_t* out,
                            uint8_t* status, uint32_t* idx, void* scratch, const uint32_t* gk1, const uint32_t* gr1, const uint32_t* ged,
-                           uint32_t* err, int grid, int variant, int classify_grid, cudaStream_t stream);
+                           uint32_t* err, int grid, int variant, int classify_grid, int num_sms, const ForkStreams* fork,
+                           cudaStream_t stream);
 // what the serving loop needs from a context (host.cu)
 struct CtxView {
   int device;
@@ -57,5 +73,6 @@ bool tune_cache_lookup(int device, int variants[4]);
 cudaError_t launch_field_test(int field, int op, const void* a, const void* b, void* out, int n, cudaStream_t stream);
 cudaError_t launch_sha512_test(const void* in, void* out, int n, cudaStream_t stream);
 cudaError_t launch_imad_probe(uint32_t* out, uint32_t iters, int grid, int block, cudaStream_t stream);
+cudaError_t launch_mul_probe(int form, uint32_t* out, uint32_t iters, int grid, int block, cudaStream_t stream);
 
 }  // namespace sg

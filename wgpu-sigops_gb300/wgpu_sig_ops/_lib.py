@@ -71,6 +71,7 @@ SIGNATURES = {
     "sigops_server_run_load": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp, _vp, _vp, ctypes.POINTER(ctypes.c_double)]),
     "sigops_sync": (ctypes.c_int, [_vp]),
     "sigops_probe_imad": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_double)]),
+    "sigops_probe_mul": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
     "sigops_device_info": (ctypes.c_int, [_vp] + [ctypes.POINTER(ctypes.c_int)] * 4),
     "sigops_test_field": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp, _sz]),
     "sigops_test_sha512": (ctypes.c_int, [_vp, _vp, _vp, _sz]),

@@ -40,6 +40,13 @@ class Context:
         check(lib.sigops_probe_imad(self.ptr, ctypes.byref(v)), "sigops_probe_imad")
         return v.value
 
+    def probe_mul(self, form: int) -> float:
+        """Multiply instructions per second of one form: 0 mad.lo, 1 mad.hi,
+        2 mad.lo.cc/madc.hi.cc carry-chain rows, 3 mad.wide."""
+        v = ctypes.c_double()
+        check(lib.sigops_probe_mul(self.ptr, form, ctypes.byref(v)), "sigops_probe_mul")
+        return v.value
+
     def autotune(self, probe_items: int = 0) -> dict:
         """Time every launch variant on a device-signed probe batch and keep the fastest."""
         import json
@@ -47,6 +54,10 @@ class Context:
         buf = ctypes.create_string_buffer(4096)
         check(lib.sigops_autotune(self.ptr, probe_items, buf, len(buf)), "sigops_autotune")
         return json.loads(buf.value.decode())
+
+    def set_variant(self, kernel: int, variant: int):
+        """kernel 0..2: plain kernel of that curve; 3: the batched engine."""
+        check(lib.sigops_set_variant(self.ptr, kernel, variant), "sigops_set_variant")
 
     def variants(self) -> dict:
         out = {}
