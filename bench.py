@@ -274,7 +274,7 @@ def main():
             check(lib.sigops_set_variant(ctx.ptr, k, args.plain_variant), "plain variant")
     tune = None
     if not args.no_autotune and args.variant < 0 and args.plain_variant < 0:
-        tune = ctx.autotune()
+        tune = ctx.autotune(probe_items=args.n)  # the ranking depends on the batch size: tune at the workload's
     info = ctx.device_info()
     info["variants"] = ctx.variants()
     mul_forms = {name: max(ctx.probe_mul(form) for _ in range(3)) for form, name in enumerate(("mad.lo", "mad.hi", "lo/hi chain", "mad.wide"))}

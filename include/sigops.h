@@ -199,18 +199,22 @@ void sigops_mixed_plan_destroy(sigops_plan* plan);
  * 256-thread block per SM, 1 = two (register budget 128); kernel 3: the
  * batched engine, variants 0..3 = the fused mixed-curve kernel at 256 threads
  * x 1 block per SM, 256 x 2, 128 x 4, 64-thread blocks (as many per SM as
- * registers allow); variants 4 + a + 3 b + 9 c (4..30) = three single-curve
+ * registers allow); variants 4 + a + 4 b + 16 c (4..67) = three single-curve
  * kernels run side by side on forked streams, secp256k1 at occupancy level a,
  * P-256 at b, ed25519 at c (level 0 = 256 threads x 1 block per SM, 1 = 128
- * threads x 3 blocks, register budget 170; 2 = 256 x 2, budget 128).
+ * threads x 3 blocks, register budget 170; 2 = 256 x 2, budget 128; 3 = 64
+ * threads, at most 200 registers: 5 or more blocks per SM).
  * sigops_get_variant also reports the grid and block used. */
 int sigops_set_variant(sigops_ctx* ctx, int kernel, int variant);
 int sigops_get_variant(sigops_ctx* ctx, int kernel, int* variant, int* grid, int* block);
 
-/* Autotuner: signs a probe batch (probe_items, 0 = 4 waves of the device) with
- * the 40/30/30 curve mix on the device, times every variant of the batched
- * kernel and of each plain kernel (best of three after a warm-up), and selects
- * the fastest.  report (may be NULL) receives a JSON summary of the timings.
+/* Autotuner: signs a probe batch (probe_items, 0 = 16 waves of the device) with
+ * the 40/30/30 curve mix on the device, times every variant of each plain
+ * kernel (best of three after a warm-up) and of the batched engine (all
+ * variants once on a 4-wave prefix, then the eight fastest on the whole probe,
+ * best of three), and selects the fastest.  The batched ranking depends on the
+ * batch size: pass the size of the batches that will run.  report (may be
+ * NULL) receives a JSON summary of the timings.
  * When SIGOPS_TUNE_CACHE names a file, the choice is stored there per device
  * model and sigops_create applies it. */
 int sigops_autotune(sigops_ctx* ctx, size_t probe_items, char* report, size_t report_cap);

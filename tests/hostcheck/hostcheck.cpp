@@ -124,6 +124,15 @@ extern "C" void hc_ed_sign(const uint8_t* seed, const uint8_t* msg, uint8_t* sig
   memcpy(sig, s, 64); memcpy(pk, p, 32);
 }
 
+// x < 2^256 into the field's canonical range (from_int); field 0 k1, 1 r1, 2 ed
+extern "C" void hc_canon(int field, const uint8_t* x, uint8_t* out) {
+  u256 v = load_le(x), r;
+  if (field == 0) r = FpK1::from_int(v);
+  else if (field == 1) r = FpR1::to_int(FpR1::from_int(v));
+  else r = FpEd::canon(v);
+  store_le(r, out);
+}
+
 // multiply instructions counted since the last reset (this thread)
 extern "C" uint64_t hc_mulcount(int reset) {
   const uint64_t c = mulcount_();

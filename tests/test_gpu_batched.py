@@ -109,9 +109,9 @@ def test_matches_plain_kernels(w):
     assert (valid == out[sel, 0]).all() and (st == status[sel]).all()
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 17, 30, 4 + 2 + 3 * 1, 4 + 1 + 9 * 2])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 4 + 1 + 4 * 2 + 16 * 3, 4 + 3 + 4 * 3 + 16 * 3, 4 + 2 + 4 * 1 + 16 * 0, 67])
 def test_every_launch_variant(w, variant):
-    """Fused (0..3) and single-curve (4..30) variants give the oracle's results,
+    """Fused (0..3) and single-curve (4..67) variants give the oracle's results,
     on a mixed batch and on ragged ones that leave some curves empty."""
     ctx = w.Context(0)
     ctx.set_variant(3, variant)
@@ -124,7 +124,7 @@ def test_every_launch_variant(w, variant):
     ctx.close()
 
 
-@pytest.mark.parametrize("variant", [0, 30])
+@pytest.mark.parametrize("variant", [0, 67])
 def test_graph_plan_replays(w, variant):
     import torch
 

@@ -64,6 +64,29 @@ def test_mul_wide_forms(hc, form):
         assert int.from_bytes(out.raw, "little") == a * b, (hex(a), hex(b))
 
 
+@pytest.mark.parametrize("field", [0, 1, 2], ids=["k1", "r1", "ed"])
+def test_canonical_boundaries(hc, field):
+    """Canonicalisation and add/sub next to the reduction boundaries:
+    [p, 2^256) for secp256k1 / P-256, and the two ranges around 2^255 for
+    ed25519 (before and after folding bit 255)."""
+    m = MODS[field]
+    xs = [0, 1, m - 1, m, m + 1, 2**256 - 1, 2**256 - 2, 2**255, 2**255 - 1, 2**255 + 18, 2**255 + 19, 2**255 - 19, 2**255 - 20]
+    xs += [m + k for k in range(0, 40)] + [2**256 - 1 - k for k in range(0, 40)] + [2**255 + k for k in range(-40, 40)]
+    out = ctypes.create_string_buffer(32)
+    for x in xs:
+        if not 0 <= x < 2**256:
+            continue
+        hc.hc_canon(field, le(x), out)
+        assert int.from_bytes(out.raw, "little") == x % m, hex(x)
+    # add / sub with operands next to 0, p and the fold boundaries
+    near = [0, 1, 2, 18, 19, 20, 977, 2**32 + 977, m - 1, m - 2, m - 19, m - 20, m // 2, m // 2 + 1, 2**255 - 20 if 2**255 - 20 < m else 5]
+    for a in near:
+        for b in near:
+            for op, f in ((1, lambda a, b: (a + b) % m), (2, lambda a, b: (a - b) % m)):
+                hc.hc_field(field, op, le(a), le(b), out)
+                assert int.from_bytes(out.raw, "little") == f(a, b), (op, hex(a), hex(b))
+
+
 def test_sqr_wide(hc):
     rng = random.Random(6)
     cases = [2**256 - 1, 0, 1, 2**255, 2**32 - 1] + [rng.getrandbits(256) for _ in range(500)]

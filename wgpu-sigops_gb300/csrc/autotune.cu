@@ -3,12 +3,16 @@
 // No counterpart in the reference (its launch shape is fixed at 256-thread
 // workgroups, src/benchmarks/mod.rs:10-53).  A probe batch with the 40/30/30
 // curve mix is signed on the device (valid signatures, so every item runs the
-// full path), then each variant of the batched kernel and of each curve's
-// plain kernel is timed with CUDA events (one warm-up, best of three) and the
-// fastest is selected.  The search space is the compiled variants: block shape
-// (64 / 128 / 256 threads) and register budget (one or two blocks per SM).
-// Window widths are fixed at compile time (5 bits for the per-signature point,
-// 7 for the generator tables), chosen by the operation-count model.
+// full path).  Each curve's plain kernel is timed per variant with CUDA events
+// (one warm-up, best of three).  The batched engine is tuned in two stages: all
+// variants once on a short prefix of the probe (the prefix keeps the curve
+// mix: items are interleaved 4:3:3), then the eight fastest again on the whole
+// probe, best of three.  The ranking of the concurrent single-curve kernels
+// depends on the batch size, so the probe should be as large as the batches
+// the caller runs.  The search space is the compiled variants: block shape and
+// register budget.  Window widths are fixed at compile time (5 bits for the
+// per-signature point, 7 for the generator tables), chosen by the
+// operation-count model.
 //
 // Results can be kept in a cache file (SIGOPS_TUNE_CACHE, one line per device
 // name and SM count) that sigops_create reads back.
@@ -37,6 +41,17 @@ void fill_random(std::vector<uint8_t>& v, uint64_t& s) {
   for (size_t i = 0; i < v.size(); i += 8) {
     uint64_t r = splitmix(s);
     for (size_t k = 0; k < 8 && i + k < v.size(); ++k) v[i + k] = (uint8_t)(r >> (8 * k));
+  }
+}
+
+// dst row i = src row perm[i]
+__global__ void gather_rows_kernel(uint8_t* __restrict__ dst, const uint8_t* __restrict__ src, const uint32_t* __restrict__ perm, size_t n,
+                                   uint32_t row) {
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const uint8_t* s = src + (size_t)perm[i] * row;
+    uint8_t* d = dst + i * row;
+    for (uint32_t k = 0; k < row; ++k) d[k] = s[k];
   }
 }
 
@@ -107,7 +122,7 @@ static void tune_cache_store(int device, const int variants[4]) {
 extern "C" int sigops_autotune(sigops_ctx* ctx, size_t probe_items, char* report, size_t report_cap) {
   sg::CtxView v;
   if (!ctx || sg::ctx_view(ctx, &v) != SIGOPS_OK) return SIGOPS_E_INVAL;
-  if (probe_items == 0) probe_items = (size_t)v.num_sms * 256 * 4;
+  if (probe_items == 0) probe_items = (size_t)v.num_sms * 256 * 16;
   const size_t n = probe_items;
   cudaSetDevice(v.device);
   // probe batch: 40/30/30 by position
@@ -119,10 +134,25 @@ extern "C" int sigops_autotune(sigops_ctx* ctx, size_t probe_items, char* report
   fill_random(msgs, s);
   fill_random(seeds, s);
   for (size_t i = 0; i < n; ++i) curves[i] = i < n1 ? 0 : (i < n1 + n2 ? 1 : 2);
+  // interleaved order for the batched engine: every prefix keeps the 4:3:3 mix
+  std::vector<uint32_t> perm;
+  perm.reserve(n);
+  {
+    static const int pat[10] = {0, 1, 2, 0, 1, 2, 0, 0, 1, 2};
+    size_t next[3] = {0, n1, n1 + n2};
+    const size_t end[3] = {n1, n1 + n2, n};
+    for (size_t i = 0; perm.size() < n; ++i) {
+      int c = pat[i % 10];
+      for (int t = 0; t < 3 && next[c] == end[c]; ++t) c = (c + 1) % 3;
+      perm.push_back((uint32_t)next[c]++);
+    }
+  }
   DevBuf d;
-  const size_t o_cur = 0, o_sec = 256 * ((n + 255) / 256), o_non = o_sec + n * 32, o_msg = o_non + n * 32, o_seed = o_msg + n * 32,
+  const size_t pad = 256 * ((n + 255) / 256);
+  const size_t o_cur = 0, o_sec = pad, o_non = o_sec + n * 32, o_msg = o_non + n * 32, o_seed = o_msg + n * 32,
                o_sig = o_seed + n * 32, o_pub = o_sig + n * 64, o_pk = o_pub + n * 64, o_out = o_pk + n * 32, o_st = o_out + n * 64,
-               o_idx = o_st + 256 * ((n + 255) / 256), o_scr = o_idx + 3 * n * 4, total = o_scr + 256;
+               o_idx = o_st + pad, o_scr = o_idx + 3 * n * 4, o_perm = o_scr + 256, o_icur = o_perm + 4 * pad, o_isig = o_icur + pad,
+               o_imsg = o_isig + n * 64, o_ipk = o_imsg + n * 32, total = o_ipk + n * 32;
   if (cudaMalloc(&d.p, total) != cudaSuccess) return SIGOPS_E_NOMEM;
   cudaStream_t st;
   if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return SIGOPS_E_CUDA;
@@ -138,6 +168,15 @@ extern "C" int sigops_autotune(sigops_ctx* ctx, size_t probe_items, char* report
                         d.p + o_pub + n1 * 64, d.p + o_st + n1, v.d_err, sign_grid, st);
   sg::launch_sign_ed(d.p + o_seed + (n1 + n2) * 32, d.p + o_msg + (n1 + n2) * 32, n3, v.gtab[2], d.p + o_sig + (n1 + n2) * 64,
                      d.p + o_pk + (n1 + n2) * 32, v.d_err, sign_grid, st);
+  cudaMemcpyAsync(d.p + o_perm, perm.data(), n * 4, cudaMemcpyHostToDevice, st);
+  {
+    const uint32_t* pm = (const uint32_t*)(d.p + o_perm);
+    const int gg = v.num_sms * 4;
+    gather_rows_kernel<<<gg, 256, 0, st>>>(d.p + o_icur, d.p + o_cur, pm, n, 1);
+    gather_rows_kernel<<<gg, 256, 0, st>>>(d.p + o_isig, d.p + o_sig, pm, n, 64);
+    gather_rows_kernel<<<gg, 256, 0, st>>>(d.p + o_imsg, d.p + o_msg, pm, n, 32);
+    gather_rows_kernel<<<gg, 256, 0, st>>>(d.p + o_ipk, d.p + o_pk, pm, n, 32);
+  }
   if (cudaStreamSynchronize(st) != cudaSuccess) {
     cudaStreamDestroy(st);
     return SIGOPS_E_CUDA;
@@ -151,10 +190,10 @@ extern "C" int sigops_autotune(sigops_ctx* ctx, size_t probe_items, char* report
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  auto time_it = [&](auto&& launch) -> float {
+  auto time_it = [&](auto&& launch, int reps = 3) -> float {
     launch();
     float best = 1e30f;
-    for (int r = 0; r < 3; ++r) {
+    for (int r = 0; r < reps; ++r) {
       cudaEventRecord(e0, st);
       launch();
       cudaEventRecord(e1, st);
@@ -167,22 +206,41 @@ extern "C" int sigops_autotune(sigops_ctx* ctx, size_t probe_items, char* report
   };
   std::string rep = "{";
   int chosen[4] = {0, 0, 0, 0};
-  // batched engine
+  // batched engine: stage 1, every variant once on a prefix of the interleaved
+  // probe; stage 2, the eight fastest on the whole probe, best of three
   {
-    float best = 1e30f;
+    const size_t n_short = std::min(n, (size_t)v.num_sms * 256 * 4);
+    auto run_batched = [&](int var, size_t items) {
+      const int grid = v.num_sms * sg::batched_max_blocks_per_sm(var);
+      const int classify_grid = (int)std::min((items + 255) / 256, (size_t)v.num_sms * 8);
+      return time_it(
+          [&] {
+            sg::launch_batched(d.p + o_icur, d.p + o_isig, d.p + o_imsg, d.p + o_ipk, items, d.p + o_out, d.p + o_st,
+                               (uint32_t*)(d.p + o_idx), d.p + o_scr, v.gtab[0], v.gtab[1], v.gtab[2], v.d_err, grid, var, classify_grid,
+                               v.num_sms, &fork, st);
+          },
+          items == n ? 3 : 1);
+    };
+    std::vector<std::pair<float, int>> stage1;
     rep += "\"batched\": {";
     for (int var = 0; var < sg::BATCHED_VARIANTS; ++var) {
-      int bps = sg::batched_max_blocks_per_sm(var);
-      if (bps <= 0) continue;
-      const int grid = v.num_sms * bps;
-      size_t cg = (n + 255) / 256;
-      int classify_grid = (int)std::min(cg, (size_t)v.num_sms * 8);
-      float ms = time_it([&] {
-        sg::launch_batched(d.p + o_cur, d.p + o_sig, d.p + o_msg, d.p + o_pk, n, d.p + o_out, d.p + o_st, (uint32_t*)(d.p + o_idx),
-                           d.p + o_scr, v.gtab[0], v.gtab[1], v.gtab[2], v.d_err, grid, var, classify_grid, v.num_sms, &fork, st);
-      });
+      if (sg::batched_max_blocks_per_sm(var) <= 0) continue;
+      const float ms = run_batched(var, n_short);
+      stage1.push_back({ms, var});
       char b[96];
       snprintf(b, sizeof b, "%s\"%d\": %.3f", var ? ", " : "", var, ms);
+      rep += b;
+    }
+    rep += "}";
+    std::sort(stage1.begin(), stage1.end());
+    float best = 1e30f;
+    rep += ", \"batched_full\": {";
+    const size_t keep = std::min<size_t>(stage1.size(), 8);
+    for (size_t k = 0; k < keep; ++k) {
+      const int var = stage1[k].second;
+      const float ms = n == n_short ? stage1[k].first : run_batched(var, n);
+      char b[96];
+      snprintf(b, sizeof b, "%s\"%d\": %.3f", k ? ", " : "", var, ms);
       rep += b;
       if (ms < best) {
         best = ms;

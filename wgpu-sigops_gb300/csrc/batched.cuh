@@ -102,9 +102,10 @@ __device__ __forceinline__ uint8_t ed_item(const MixedIO& io, size_t i, const ui
   return st;
 }
 
-template <int BLOCK, int MINB, int CM>
-__global__ void __launch_bounds__(BLOCK, MINB) batched_kernel(MixedIO io, const uint32_t* __restrict__ idx, BatchTables tabs, Scratch* sc,
-                                                        uint32_t* err) {
+// one launch's work: tables staged, then tiles until the queue is empty
+template <int CM>
+__device__ __forceinline__ void batched_body(const MixedIO& io, const uint32_t* __restrict__ idx, const BatchTables& tabs, Scratch* sc,
+                                             uint32_t* err) {
   __shared__ __align__(128) uint32_t tk1[(CM & CM_K1) ? 2 * ECDSA_GTAB * 16 : 4];  // G and 2^128 G multiples (GLV)
   __shared__ __align__(128) uint32_t tr1[(CM & CM_R1) ? ECDSA_GTAB * 16 : 4];
   __shared__ __align__(128) uint32_t ted[(CM & CM_ED) ? ED_GTAB * 24 : 4];
@@ -152,6 +153,20 @@ __global__ void __launch_bounds__(BLOCK, MINB) batched_kernel(MixedIO io, const 
       io.status[i] = st;
     }
   }
+}
+
+// occupancy by blocks per SM (__launch_bounds__) ...
+template <int BLOCK, int MINB, int CM>
+__global__ void __launch_bounds__(BLOCK, MINB) batched_kernel(MixedIO io, const uint32_t* __restrict__ idx, BatchTables tabs, Scratch* sc,
+                                                        uint32_t* err) {
+  batched_body<CM>(io, idx, tabs, sc, err);
+}
+
+// ... or by an explicit register cap
+template <int BLOCK, int MAXREG, int CM>
+__global__ void __launch_bounds__(BLOCK) __maxnreg__(MAXREG) batched_kernel_r(MixedIO io, const uint32_t* __restrict__ idx, BatchTables tabs,
+                                                                            Scratch* sc, uint32_t* err) {
+  batched_body<CM>(io, idx, tabs, sc, err);
 }
 
 }  // namespace sg

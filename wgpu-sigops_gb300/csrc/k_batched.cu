@@ -44,13 +44,15 @@ cudaError_t batched_launch_ed(int, const MixedIO&, const uint32_t*, const BatchT
 static const int kFusedBlock[BATCHED_FUSED_VARIANTS] = {256, 256, 128, 64};
 
 // single-curve kernels: occupancy level 0 = 256 threads x 1 block per SM,
-// 1 = 128 x 3, 2 = 256 x 2 (8, 12 and 16 warps per SM)
-static const int kLevelBlock[3] = {256, 128, 256};
+// 1 = 128 x 3, 2 = 256 x 2 (8, 12 and 16 warps per SM), 3 = 64 threads with
+// at most 200 registers (as many blocks as the registers allow: 10-12 warps)
+constexpr int kLevels = 4;
+static const int kLevelBlock[kLevels] = {256, 128, 256, 64};
 
 // blocks per SM of curve c's single-curve kernel at an occupancy level
 // (queried once; the kernels are the same on every device of one process)
 static int curve_occupancy(int c, int level) {
-  static std::atomic<int> cache[3][3];
+  static std::atomic<int> cache[3][kLevels];
   int b = cache[c][level].load(std::memory_order_relaxed);
   if (b == 0) {
     b = c == 0 ? batched_occupancy_k1(level) : c == 1 ? batched_occupancy_r1(level) : batched_occupancy_ed(level);
@@ -59,11 +61,11 @@ static int curve_occupancy(int c, int level) {
   return b;
 }
 
-// variant 4 + a + 3 b + 9 c: levels a, b, c for secp256k1, P-256, ed25519
+// variant 4 + a + 4 b + 16 c: levels a, b, c for secp256k1, P-256, ed25519
 static int split_level(int variant, int c) {
   int v = variant - BATCHED_FUSED_VARIANTS;
-  for (int k = 0; k < c; ++k) v /= 3;
-  return v % 3;
+  for (int k = 0; k < c; ++k) v /= kLevels;
+  return v % kLevels;
 }
 
 int batched_variant_block(int v) {
@@ -84,7 +86,7 @@ int batched_max_blocks_per_sm(int v) {
   int m = 0;
   for (int c = 0; c < 3; ++c) {
     const int l = split_level(v, c);
-    const int b = curve_occupancy(c, l) * kLevelBlock[l] / 256;
+    const int b = (curve_occupancy(c, l) * kLevelBlock[l] + 255) / 256;  // rounded up: never caps a kernel
     if (b <= 0) return 0;
     m = b > m ? b : m;
   }

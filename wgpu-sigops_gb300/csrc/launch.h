@@ -33,11 +33,12 @@ cudaError_t launch_sign_ed(const uint8_t* seeds, const uint8_t* msgs, size_t n, 
                            uint32_t* err, int grid, cudaStream_t stream);
 // batched mixed-curve engine: scratch = Scratch record + 3*n u32 index lists.
 // variants 0..3: the fused kernel (0 = 256 threads x 1 block/SM, 1 = 256 x 2,
-// 2 = 128 x 4, 3 = 64 threads); variants 4 + a + 3 b + 9 c (4..30): three
+// 2 = 128 x 4, 3 = 64 threads); variants 4 + a + 4 b + 16 c (4..67): three
 // single-curve kernels (secp256k1 at occupancy level a, P-256 at b, ed25519
-// at c; level 0 = 256 threads x 1 block per SM, 1 = 128 x 3, 2 = 256 x 2).
+// at c; level 0 = 256 threads x 1 block per SM, 1 = 128 x 3, 2 = 256 x 2,
+// 3 = 64 threads with at most 200 registers).
 constexpr int BATCHED_FUSED_VARIANTS = 4;
-constexpr int BATCHED_VARIANTS = 31;
+constexpr int BATCHED_VARIANTS = 68;
 int batched_variant_block(int variant);
 int batched_max_blocks_per_sm(int variant);
 size_t batched_scratch_bytes();
