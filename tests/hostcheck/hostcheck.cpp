@@ -133,6 +133,13 @@ extern "C" void hc_canon(int field, const uint8_t* x, uint8_t* out) {
   store_le(r, out);
 }
 
+// P-256 reduction of a 512-bit value
+extern "C" void hc_r1_reduce(const uint8_t* x64, uint8_t* out) {
+  uint32_t t[16];
+  memcpy(t, x64, 64);
+  store_le(FpR1::reduce(t), out);
+}
+
 // multiply instructions counted since the last reset (this thread)
 extern "C" uint64_t hc_mulcount(int reset) {
   const uint64_t c = mulcount_();

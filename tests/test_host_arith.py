@@ -87,6 +87,21 @@ def test_canonical_boundaries(hc, field):
                 assert int.from_bytes(out.raw, "little") == f(a, b), (op, hex(a), hex(b))
 
 
+def test_p256_reduction(hc):
+    """The P-256 reduction on products of field elements and on extreme
+    512-bit values (all ones, single high words), where the signed column
+    sums and the folded top word reach their bounds."""
+    p = o.SECP256R1.p
+    rng = random.Random(70)
+    xs = [0, 1, p, p * p, (p - 1) * (p - 1), 2**512 - 1, 2**511, (2**256 - 1) * (2**256 - 1)]
+    xs += [sum(rng.choice([0, 0xFFFFFFFF, 1, 0x80000000]) << (32 * k) for k in range(16)) for _ in range(300)]
+    xs += [rng.randrange(p) * rng.randrange(p) for _ in range(300)] + [rng.getrandbits(512) for _ in range(300)]
+    out = ctypes.create_string_buffer(32)
+    for x in xs:
+        hc.hc_r1_reduce(x.to_bytes(64, "little"), out)
+        assert int.from_bytes(out.raw, "little") == x % p, hex(x)
+
+
 def test_sqr_wide(hc):
     rng = random.Random(6)
     cases = [2**256 - 1, 0, 1, 2**255, 2**32 - 1] + [rng.getrandbits(256) for _ in range(500)]

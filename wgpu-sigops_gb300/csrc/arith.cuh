@@ -229,14 +229,9 @@ SG_HD void mul_wide_kara(uint32_t r[16], const u256& a, const u256& b) {
   r[15] = addc(p2[7], 0u);
 }
 
-// the 512-bit product the field multiplications use
-SG_HD void mul_wide(uint32_t r[16], const u256& a, const u256& b) {
-#if defined(SG_MUL_KARATSUBA)
-  mul_wide_kara(r, a, b);
-#else
-  mul_wide_school(r, a, b);
-#endif
-}
+// the 512-bit product of the secp256k1 / P-256 / scalar-field multiplications
+// (ed25519 uses mul_wide_kara)
+SG_HD void mul_wide(uint32_t r[16], const u256& a, const u256& b) { mul_wide_school(r, a, b); }
 
 // 512-bit square r[0..15] = a^2: the 28 cross products a_i a_j (i < j) are
 // accumulated with the same even/odd single-chain rows as mul_wide (row i

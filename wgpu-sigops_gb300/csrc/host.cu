@@ -465,8 +465,15 @@ int sigops_verify_mixed(sigops_ctx* ctx, const uint8_t* curves, const uint8_t* s
                         uint8_t* out, uint8_t* out_status) {
   if (n == 0) return SIGOPS_OK;
   if (!curves || !sigs || !msgs || !pks || !out) return fail(SIGOPS_E_INVAL, "null buffer");
-  for (size_t i = 0; i < n; ++i)
-    if (curves[i] > 2) return fail(SIGOPS_E_INVAL, "item %zu has unknown curve tag %u", i, (unsigned)curves[i]);
+  {
+    // the largest tag (a loop the compiler vectorises) decides; the index of
+    // the first bad tag is only searched for the error message
+    uint8_t top = 0;
+    for (size_t i = 0; i < n; ++i) top = curves[i] > top ? curves[i] : top;
+    if (top > 2)
+      for (size_t i = 0; i < n; ++i)
+        if (curves[i] > 2) return fail(SIGOPS_E_INVAL, "item %zu has unknown curve tag %u", i, (unsigned)curves[i]);
+  }
   sigops_ctx* c = resolve(ctx);
   if (!c) return SIGOPS_E_NODEV;
   std::lock_guard<std::mutex> g(c->mu);
