@@ -232,6 +232,11 @@ int sigops_autotune(sigops_ctx* ctx, size_t probe_items, char* report, size_t re
 sigops_server* sigops_server_create(sigops_ctx* ctx, int slots, size_t slot_items, double hbm_fraction);
 void sigops_server_destroy(sigops_server* server);
 size_t sigops_server_slot_items(sigops_server* server);
+/* Batched-engine launch variant of the server's launches (as sigops_set_variant
+ * kernel 3; default 0, the fused kernel at 256 threads); applies from the next
+ * launch.  Variants 4..67 run their three curve kernels one after another on
+ * the slot's stream.  No counterpart in the reference. */
+int sigops_server_set_variant(sigops_server* server, int variant);
 
 /* Queue one request of n items.  curves: n tags, or NULL with uniform_curve
  * set for a single-curve request; pks may be NULL for ECDSA-only requests.

@@ -21,14 +21,15 @@ def W(w):
     return wl.config("c4", n=40000, seed=77)
 
 
-def test_alone_equals_in_the_mix(w, W):
+@pytest.mark.parametrize("variant", [0, 40], ids=["fused", "single-curve"])
+def test_alone_equals_in_the_mix(w, W, variant):
     from wgpu_sig_ops.serving import Server, curve_sorted_pool, request_stream
 
     ctx = w.default_context()
     pool, regions = curve_sorted_pool(W)
     offs, cnts, arr = request_stream(regions, 0.0, 0.0, seed=3, n_requests=120)
     # reference: every request alone, one at a time, through its own server call
-    srv = Server(ctx, slots=3, slot_items=8192)
+    srv = Server(ctx, slots=3, slot_items=8192, variant=variant)
     alone = []
     for o, c in zip(offs, cnts):
         sl = slice(int(o), int(o) + int(c))

@@ -83,8 +83,11 @@ struct sigops_server {
   sg::CtxView cv{};
   std::vector<Slot> slots;
   size_t cap = 0;          // items per slot
-  int variant = 0;         // batched-kernel launch variant (256-thread blocks; 64-thread blocks cut saturation by a third)
-  int grid_cap = 0;        // blocks of that variant the device holds at once
+  // batched-engine launch variant and its grid cap, packed in one word so the
+  // worker reads a consistent pair (variant << 16 | blocks per launch at most).
+  // Default: the fused kernel at 256 threads (64-thread blocks cut saturation
+  // by a third); sigops_server_set_variant changes it between launches.
+  std::atomic<uint32_t> shape{0};
   size_t queue_bound = 0;  // max queued (not yet launched) items
   Layout lay{};
   std::mutex mu;
@@ -140,10 +143,12 @@ void pack_and_launch(sigops_server* s, Slot& sl) {
   int classify_grid = (int)std::min(cg, (size_t)s->cv.num_sms * 8);
   // grid sized to the batch (one item per thread up to a full persistent grid):
   // a light batch occupies few SMs and launches from other slots run beside it
-  const int block = sg::batched_variant_block(s->variant);
-  const int grid = (int)std::min<size_t>((size_t)s->grid_cap, (n + block - 1) / block);
+  const uint32_t shape = s->shape.load(std::memory_order_relaxed);
+  const int variant = (int)(shape >> 16), grid_cap = (int)(shape & 0xffffu);
+  const int block = sg::batched_variant_block(variant);
+  const int grid = (int)std::min<size_t>((size_t)grid_cap, (n + block - 1) / block);
   cudaError_t e = sg::launch_batched(sl.d + L.cur, sl.d + L.sig, sl.d + L.msg, sl.d + L.pk, n, sl.d + L.out, sl.d + L.st, sl.d_idx,
-                                     sl.d_scratch, s->cv.gtab[0], s->cv.gtab[1], s->cv.gtab[2], s->cv.d_err, grid, s->variant,
+                                     sl.d_scratch, s->cv.gtab[0], s->cv.gtab[1], s->cv.gtab[2], s->cv.d_err, grid, variant,
                                      classify_grid, s->cv.num_sms, nullptr, sl.stream);
   cudaMemcpyAsync(sl.h + L.out, sl.d + L.out, n * 64, cudaMemcpyDeviceToHost, sl.stream);
   cudaMemcpyAsync(sl.h + L.st, sl.d + L.st, n, cudaMemcpyDeviceToHost, sl.stream);
@@ -213,6 +218,19 @@ void worker_loop(sigops_server* s) {
 
 extern "C" {
 
+static int set_shape(sigops_server* s, int variant) {
+  const int bps = sg::batched_max_blocks_per_sm(variant);
+  if (bps <= 0) return SIGOPS_E_INVAL;
+  const uint32_t grid_cap = std::min<uint32_t>(0xffffu, (uint32_t)(s->cv.num_sms * bps));
+  s->shape.store(((uint32_t)variant << 16) | grid_cap, std::memory_order_relaxed);
+  return SIGOPS_OK;
+}
+
+int sigops_server_set_variant(sigops_server* s, int variant) {
+  if (!s || variant < 0 || variant >= sg::BATCHED_VARIANTS) return SIGOPS_E_INVAL;
+  return set_shape(s, variant);
+}
+
 sigops_server* sigops_server_create(sigops_ctx* ctx, int nslots, size_t slot_items, double hbm_fraction) {
   sg::CtxView v;
   if (!ctx || sg::ctx_view(ctx, &v) != SIGOPS_OK) return nullptr;
@@ -232,9 +250,10 @@ sigops_server* sigops_server_create(sigops_ctx* ctx, int nslots, size_t slot_ite
   s->cap = slot_items;
   s->queue_bound = std::max<size_t>(slot_items * 64, budget_items);
   s->lay = layout(slot_items);
-  s->variant = 0;
-  const int bps = sg::batched_max_blocks_per_sm(s->variant);
-  s->grid_cap = v.num_sms * (bps > 0 ? bps : 1);
+  if (set_shape(s, 0) != SIGOPS_OK) {
+    delete s;
+    return nullptr;
+  }
   s->slots.resize(nslots);
   for (Slot& sl : s->slots) {
     bool ok = cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking) == cudaSuccess &&
