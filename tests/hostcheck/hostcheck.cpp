@@ -133,6 +133,43 @@ extern "C" void hc_canon(int field, const uint8_t* x, uint8_t* out) {
   store_le(r, out);
 }
 
+// Weierstrass point operations on Jacobian inputs built from affine points and
+// chosen Z: P = (x z^2, y z^3, z) (z = 0: infinity).  op 0: add(P, Q),
+// 1: madd(P, Q affine), 2: dbl(P).  out = affine x || y, returns 1 for the
+// point at infinity.
+template <class T>
+static int weier_op(int op, const uint8_t* pa, const uint8_t* pz, const uint8_t* qa, const uint8_t* qz, uint8_t* out) {
+  using F = typename T::F;
+  using W = Weier<F, T::A_M3>;
+  auto jac = [](const uint8_t* a, const uint8_t* zb) {
+    JPoint r;
+    const u256 z = F::from_int(load_le(zb));
+    if (u256_is_zero(z)) return W::infinity();
+    const u256 x = F::from_int(load_le(a)), y = F::from_int(load_le(a + 32)), z2 = F::sqr(z);
+    r.X = F::mul(x, z2);
+    r.Y = F::mul(y, F::mul(z2, z));
+    r.Z = z;
+    return r;
+  };
+  JPoint P = jac(pa, pz), R;
+  if (op == 0) R = W::add(P, jac(qa, qz));
+  else if (op == 1) {
+    APoint q;
+    q.x = F::from_int(load_le(qa));
+    q.y = F::from_int(load_le(qa + 32));
+    R = W::madd(P, q);
+  } else R = W::dbl(P);
+  if (W::is_inf(R)) return 1;
+  APoint a = W::to_affine(R);
+  store_le(F::to_int(a.x), out);
+  store_le(F::to_int(a.y), out + 32);
+  return 0;
+}
+
+extern "C" int hc_weier_op(int curve, int op, const uint8_t* pa, const uint8_t* pz, const uint8_t* qa, const uint8_t* qz, uint8_t* out) {
+  return curve == 0 ? weier_op<K1Traits>(op, pa, pz, qa, qz, out) : weier_op<R1Traits>(op, pa, pz, qa, qz, out);
+}
+
 // P-256 reduction of a 512-bit value
 extern "C" void hc_r1_reduce(const uint8_t* x64, uint8_t* out) {
   uint32_t t[16];

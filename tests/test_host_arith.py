@@ -248,3 +248,41 @@ def test_divstep_inverse(hc, name):
         hc.hc_divstep_inv(x.to_bytes(32, "little"), M.to_bytes(32, "little"), minv, out, ctypes.byref(used))
         assert int.from_bytes(out.raw, "little") == pow(x, -1, M)
         assert 0 < used.value <= 25
+
+
+@pytest.mark.parametrize("curve", [0, 1], ids=["secp256k1", "secp256r1"])
+def test_weierstrass_exceptional_cases(hc, curve):
+    """Jacobian add / mixed add / double against the oracle, including the
+    exceptional inputs the Strauss loop can meet: P + P (falls back to
+    doubling), P + (-P) = infinity, infinity + Q, P + infinity, and points
+    with non-unit, different Z."""
+    c = o.SECP256K1 if curve == 0 else o.SECP256R1
+    rng = random.Random(90 + curve)
+    hc.hc_weier_op.argtypes = [ctypes.c_int, ctypes.c_int] + [ctypes.c_char_p] * 5
+    G = c.g
+
+    def pt(k):
+        return o.ws_mul(c, k, G)
+
+    def enc(A):
+        return le(A[0]) + le(A[1]) if A is not None else bytes(64)
+
+    def run(op, A, za, B, zb):
+        out = ctypes.create_string_buffer(64)
+        inf = hc.hc_weier_op(curve, op, enc(A), le(za if A is not None else 0), enc(B), le(zb if B is not None else 0), out)
+        return None if inf else (int.from_bytes(out.raw[:32], "little"), int.from_bytes(out.raw[32:], "little"))
+
+    def add_ref(A, B):
+        return o._to_affine(c, o._jac_add(c, None if A is None else (A[0], A[1], 1), None if B is None else (B[0], B[1], 1)))
+
+    cases = []
+    for _ in range(12):
+        A, B = pt(rng.randrange(1, c.n)), pt(rng.randrange(1, c.n))
+        negA = (A[0], (-A[1]) % c.p)
+        cases += [(A, B), (A, A), (A, negA), (None, B), (A, None), (None, None)]
+    for A, B in cases:
+        za, zb = rng.randrange(1, c.p), rng.randrange(1, c.p)
+        assert run(0, A, za, B, zb) == add_ref(A, B)
+        if B is not None:  # mixed add: Q affine, never infinity
+            assert run(1, A, za, B, 1) == add_ref(A, B)
+        assert run(2, A, za, None, 0) == add_ref(A, A)
