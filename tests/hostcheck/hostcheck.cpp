@@ -25,9 +25,12 @@ extern "C" {
 
 int hc_bases(int curve, uint32_t L, uint32_t* out) { return build_bases(curve, L, out); }
 
+// entries of the generator tables: ECDSA (per half for secp256k1), ed25519
+int hc_gtab_entries(int ed) { return ed ? ED_GTAB : ECDSA_GTAB; }
+
 void hc_gtab(int curve, uint32_t* out) {
   init();
-  if (curve == 0) memcpy(out, g_k1, ECDSA_GTAB * 64);
+  if (curve == 0) memcpy(out, g_k1, sizeof g_k1);
   else if (curve == 1) memcpy(out, g_r1, sizeof g_r1);
   else memcpy(out, g_ed, sizeof g_ed);
 }

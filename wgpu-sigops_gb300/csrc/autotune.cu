@@ -11,7 +11,7 @@
 // depends on the batch size, so the probe should be as large as the batches
 // the caller runs.  The search space is the compiled variants: block shape and
 // register budget.  Window widths are fixed at compile time (5 bits for the
-// per-signature point, 7 for the generator tables), chosen by the
+// per-signature point, 8 for the generator tables), chosen by the
 // operation-count model.
 //
 // Results can be kept in a cache file (SIGOPS_TUNE_CACHE, one line per device

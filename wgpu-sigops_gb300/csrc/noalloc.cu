@@ -9,7 +9,7 @@
 // (per-curve counters and index lists), the generator tables and the device
 // error word live in the file-scope static __device__ arrays below, which every
 // GPU that loads the library holds until the process exits
-// (about 0.8 MiB for the scratch, 18 KiB for the tables).
+// (about 0.8 MiB for the scratch, 36 KiB for the tables).
 //
 // The first call on each device performs a one-time set-up with that device
 // current: cudaGetSymbolAddress for each array (host code must not use the

@@ -40,11 +40,11 @@ SG_HD void u256_to_be_words(const u256& v, uint32_t* w) {
 // uses multiples 1..2^(WR-1) built per thread; the generator uses a shared
 // table of multiples 1..2^(WG-1).
 constexpr int ECDSA_WR = 5;
-constexpr int ECDSA_WG = 7;
-constexpr int ECDSA_GTAB = 1 << (ECDSA_WG - 1);  // 64 affine points
+constexpr int ECDSA_WG = 8;
+constexpr int ECDSA_GTAB = 1 << (ECDSA_WG - 1);  // 128 affine points
 constexpr int ED_WR = 5;
-constexpr int ED_WG = 7;
-constexpr int ED_GTAB = 1 << (ED_WG - 1);  // 64 affine Niels points
+constexpr int ED_WG = 8;
+constexpr int ED_GTAB = 1 << (ED_WG - 1);  // 128 affine Niels points
 
 struct K1Traits {
   using F = FpK1;
@@ -119,7 +119,7 @@ SG_NOINL JPoint ecdsa_lincomb(const u256 u1, const u256 u2, const APoint R, cons
 // doublings instead of ~260.  Decomposition constants as in the reference's
 // src/curve_algos/secp256k1_curve.rs:47-71 (Babai rounding with g1, g2 scaled
 // by 2^384); the CPU model of GLV is src/curve_algos/secp256k1_mul.rs:38-94.
-// gtab2: multiples 1..64 of G followed by multiples 1..64 of 2^128 G.
+// gtab2: multiples 1..ECDSA_GTAB of G followed by the same multiples of 2^128 G.
 // ---------------------------------------------------------------------------
 struct K1Glv {
   SG_HD static u256 LAMBDA_MONT() { return SG_U256(0xc9926c9eu, 0xf07deb3du, 0x83c6944cu, 0x2c93e7adu, 0x52697d91u, 0x73a96606u, 0x8558d639u, 0x53284017u); }

@@ -1,7 +1,7 @@
 // Generator tables, computed once on the host with the same field and curve
 // code the kernels run.
 //
-//  * kernel tables: multiples 1..64 of the generator (affine; Niels form for
+//  * kernel tables: multiples 1..128 of the generator (affine; Niels form for
 //    ed25519) in the field representation the kernels use;
 //  * the reference's table_limbs encoding: precompute::*_bases(log_limb_size)
 //    (src/precompute.rs:14-69) = [1G .. 16G], each coordinate as
@@ -66,7 +66,7 @@ inline void build_weier_gtab(const u256& gx, const u256& gy, uint32_t* out) {
     }
 }
 
-// secp256k1 GLV table: multiples 1..64 of G, then multiples 1..64 of 2^128 G
+// secp256k1 GLV table: multiples 1..128 of G, then multiples 1..128 of 2^128 G
 inline void build_k1_glv_gtab(uint32_t* out) {
   using F = FpK1;
   using W = Weier<F, false>;
