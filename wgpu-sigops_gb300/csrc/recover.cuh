@@ -85,7 +85,9 @@ SG_NOINL JPoint ecdsa_lincomb(const u256 u1, const u256 u2, const APoint R, cons
 
   constexpr int JR = (257 + ECDSA_WR - 1) / ECDSA_WR;  // windows for a 256-bit scalar
   constexpr int JG = (257 + ECDSA_WG - 1) / ECDSA_WG;
-  constexpr int TOP = (JR * ECDSA_WR > JG * ECDSA_WG ? JR * ECDSA_WR : JG * ECDSA_WG) - 1;
+  // the chain starts at the highest window position that adds anything:
+  // doublings above it would only double the point at infinity
+  constexpr int TOP = ((JR - 1) * ECDSA_WR > (JG - 1) * ECDSA_WG) ? (JR - 1) * ECDSA_WR : (JG - 1) * ECDSA_WG;
   JPoint acc = W::infinity();
 #pragma unroll 1
   for (int pos = TOP; pos >= 0; --pos) {
@@ -193,7 +195,9 @@ SG_NOINL JPoint k1_glv_lincomb(const u256 u1, const u256 u2, const APoint R, con
 
   constexpr int JR = (130 + ECDSA_WR - 1) / ECDSA_WR;  // windows for a 129-bit magnitude
   constexpr int JG = (129 + ECDSA_WG - 1) / ECDSA_WG;  // windows for a 128-bit half
-  constexpr int TOP = (JR * ECDSA_WR > JG * ECDSA_WG ? JR * ECDSA_WR : JG * ECDSA_WG) - 1;
+  // the chain starts at the highest window position that adds anything:
+  // doublings above it would only double the point at infinity
+  constexpr int TOP = ((JR - 1) * ECDSA_WR > (JG - 1) * ECDSA_WG) ? (JR - 1) * ECDSA_WR : (JG - 1) * ECDSA_WG;
   JPoint acc = W::infinity();
 #pragma unroll 1
   for (int pos = TOP; pos >= 0; --pos) {
@@ -331,7 +335,7 @@ SG_NOINL EPoint ed_lincomb(const u256 s, const u256 k, const EPoint negA, const 
   // both scalars are < l < 2^253
   constexpr int JR = (254 + ED_WR - 1) / ED_WR;
   constexpr int JG = (254 + ED_WG - 1) / ED_WG;
-  constexpr int TOP = (JR * ED_WR > JG * ED_WG ? JR * ED_WR : JG * ED_WG) - 1;
+  constexpr int TOP = ((JR - 1) * ED_WR > (JG - 1) * ED_WG) ? (JR - 1) * ED_WR : (JG - 1) * ED_WG;
   EPoint acc = Edw::identity();
 #pragma unroll 1
   for (int pos = TOP; pos >= 0; --pos) {
