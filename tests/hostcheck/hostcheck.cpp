@@ -187,6 +187,16 @@ extern "C" uint64_t hc_mulcount(int reset) {
   return c;
 }
 
+// which = 0: sqr_wide, 1: subtractive Karatsuba square
+extern "C" void hc_sqr_wide_form(int which, const uint8_t* a, uint8_t* out64) {
+  uint32_t t[16];
+  u256 x;
+  memcpy(x.w, a, 32);
+  if (which) sqr_wide_kara(t, x);
+  else sqr_wide(t, x);
+  memcpy(out64, t, 64);
+}
+
 extern "C" void hc_sqr_wide(const uint8_t* a, uint8_t* out64) {
   uint32_t t[16];
   u256 x;
