@@ -130,6 +130,16 @@ int sigops_ed25519_ecverify(sigops_ctx* ctx, const uint8_t* sigs, const uint8_t*
 int sigops_ed25519_ecverify_single(sigops_ctx* ctx, const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks, size_t n,
                                    uint32_t log_limb_size, uint8_t* out_valid, uint8_t* out_status);
 
+/* ed25519 verification of messages of any length (ed25519-dalek
+ * VerifyingKey::verify(&[u8], &Signature) semantics, per item as
+ * sigops_ed25519_ecverify).  No counterpart in the reference, whose API
+ * passes 32-byte fuel messages (src/ed25519_eddsa.rs:67-74).  Message i is
+ * msgs[msg_offsets[i] .. msg_offsets[i] + msg_lens[i]); every message must lie
+ * within the msgs_bytes bytes of msgs (else SIGOPS_E_INVAL).  The challenge
+ * SHA-512(R || A || M) runs ceil((81 + len) / 128) blocks on the GPU. */
+int sigops_ed25519_verify_raw(sigops_ctx* ctx, const uint8_t* sigs, const uint8_t* msgs, size_t msgs_bytes, const uint64_t* msg_offsets,
+                              const uint32_t* msg_lens, const uint8_t* pks, size_t n, uint8_t* out_valid, uint8_t* out_status);
+
 /* ------------------------------------------ device-resident plain kernels */
 
 /* One plain (one signature per thread) kernel over device buffers on `stream`
@@ -211,7 +221,7 @@ int sigops_get_variant(sigops_ctx* ctx, int kernel, int* variant, int* grid, int
 /* Autotuner: signs a probe batch (probe_items, 0 = 16 waves of the device) with
  * the 40/30/30 curve mix on the device, times every variant of each plain
  * kernel (best of three after a warm-up) and of the batched engine (all
- * variants once on a 4-wave prefix, then the eight fastest on the whole probe,
+ * variants once on an 8-wave prefix, then the twelve fastest on the whole probe,
  * best of three), and selects the fastest.  The batched ranking depends on the
  * batch size: pass the size of the batches that will run.  report (may be
  * NULL) receives a JSON summary of the timings.

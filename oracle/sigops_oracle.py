@@ -376,6 +376,16 @@ def ed25519_ecverify(sig64: bytes, msg32: bytes, pk32: bytes) -> tuple[int, bool
     """
     if len(sig64) != 64 or len(msg32) != 32 or len(pk32) != 32:
         raise ValueError("signature 64, message 32 and key 32 bytes expected")
+    return ed25519_verify_raw(sig64, msg32, pk32)
+
+
+def ed25519_verify_raw(sig64: bytes, msg: bytes, pk32: bytes) -> tuple[int, bool]:
+    """The same check for a message of any length (ed25519-dalek
+    ``VerifyingKey::verify(&[u8], &Signature)``); the reference's own API only
+    passes 32-byte fuel messages (src/ed25519_eddsa.rs:67-74)."""
+    if len(sig64) != 64 or len(pk32) != 32:
+        raise ValueError("signature 64 and key 32 bytes expected")
+    msg32 = bytes(msg)
     A = ed_decompress(pk32)
     if A is None:
         return ST_NO_POINT, False

@@ -99,6 +99,13 @@ int hc_ed_verify(const uint8_t* sig, const uint8_t* msg, const uint8_t* pk) {
   return ed25519_verify(s, m, p, g_ed);
 }
 
+int hc_ed_verify_raw(const uint8_t* sig, const uint8_t* msg, uint32_t len, const uint8_t* pk) {
+  init();
+  uint32_t s[16], p[8];
+  memcpy(s, sig, 64); memcpy(p, pk, 32);
+  return ed25519_verify_raw(s, msg, len, p, g_ed);
+}
+
 void hc_sha512_96(const uint8_t* in, uint8_t* out) {
   uint32_t m[24], h[16];
   memcpy(m, in, 96);
@@ -185,16 +192,6 @@ extern "C" uint64_t hc_mulcount(int reset) {
   const uint64_t c = mulcount_();
   if (reset) mulcount_() = 0;
   return c;
-}
-
-// which = 0: sqr_wide, 1: subtractive Karatsuba square
-extern "C" void hc_sqr_wide_form(int which, const uint8_t* a, uint8_t* out64) {
-  uint32_t t[16];
-  u256 x;
-  memcpy(x.w, a, 32);
-  if (which) sqr_wide_kara(t, x);
-  else sqr_wide(t, x);
-  memcpy(out64, t, 64);
 }
 
 extern "C" void hc_sqr_wide(const uint8_t* a, uint8_t* out64) {

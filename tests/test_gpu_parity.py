@@ -119,6 +119,70 @@ def test_ed25519_random_batch_vs_oracle(w):
         assert (status[i], bool(valid[i])) == (st, ok), i
 
 
+def test_ed25519_raw_golden(w):
+    """Messages of any length (0..4096 bytes, around the SHA-512 block
+    boundaries of R || A || M) against OpenSSL / libsodium verdicts."""
+    from tests.golden_io import load_raw
+
+    V = load_raw()
+    valid, status = w.ed25519_eddsa.verify_raw_arrays([bytes.fromhex(v["sig"]) for v in V], [bytes.fromhex(v["msg"]) for v in V],
+                                                      [bytes.fromhex(v["pubkey"]) for v in V])
+    for k, v in enumerate(V):
+        assert bool(valid[k]) == v["valid"], (v["case"], v["len"])
+        if v["case"] == "s_plus_l":
+            assert status[k] == o.ST_BAD_SCALAR
+
+
+def test_ed25519_raw_random_vs_oracle(w):
+    """Random lengths and tampering, every status equal to the oracle's; the
+    32-byte items also equal the fixed-length API."""
+    rng = random.Random(31)
+    sigs, msgs, pks = [], [], []
+    for i in range(400):
+        seed = rng.randbytes(32)
+        msg = rng.randbytes(rng.choice([0, 1, 32, 47, 48, 111, 112, 175, 176, rng.randrange(0, 700)]))
+        _, _, pk = o.ed25519_keypair(seed)
+        sig = o.ed25519_sign(seed, msg)
+        mode = rng.randrange(6)
+        if mode == 1 and msg:
+            j = rng.randrange(len(msg))
+            msg = msg[:j] + bytes([msg[j] ^ 0x40]) + msg[j + 1:]
+        elif mode == 2:
+            sig = bytes([sig[0] ^ 1]) + sig[1:]
+        elif mode == 3:
+            pk = rng.randbytes(32)
+        sigs.append(sig)
+        msgs.append(msg)
+        pks.append(pk)
+    valid, status = w.ed25519_eddsa.verify_raw_arrays(sigs, msgs, pks)
+    for i in range(len(sigs)):
+        st, ok = o.ed25519_verify_raw(sigs[i], msgs[i], pks[i])
+        assert (status[i], bool(valid[i])) == (st, ok), (i, len(msgs[i]))
+    sel = [i for i in range(len(sigs)) if len(msgs[i]) == 32]
+    v32, s32 = w.ed25519_eddsa.ecverify_arrays([sigs[i] for i in sel], [msgs[i] for i in sel], [pks[i] for i in sel])
+    assert (v32 == valid[sel]).all() and (s32 == status[sel]).all()
+
+
+def test_ed25519_raw_bounds(w):
+    """A message running past the message buffer is refused on the host."""
+    import ctypes
+
+    from wgpu_sig_ops._lib import lib
+
+    seed = bytes(range(32))
+    _, _, pk = o.ed25519_keypair(seed)
+    sig = o.ed25519_sign(seed, b"abc")
+    blob = (ctypes.c_uint8 * 3)(*b"abc")
+    offs = (ctypes.c_uint64 * 1)(1)
+    lens = (ctypes.c_uint32 * 1)(3)
+    valid = (ctypes.c_uint8 * 1)()
+    ctx = w.default_context()
+    rc = lib.sigops_ed25519_verify_raw(ctx.ptr, sig, blob, 3, offs, lens, pk, 1, valid, None)
+    assert rc == -22  # SIGOPS_E_INVAL
+    offs[0] = 0
+    assert lib.sigops_ed25519_verify_raw(ctx.ptr, sig, blob, 3, offs, lens, pk, 1, valid, None) == 0 and valid[0] == 1
+
+
 def test_empty_and_errors(w):
     t = w.precompute.secp256k1_bases(L)
     assert w.secp256k1_ecdsa.ecrecover([], [], t, L) == []

@@ -102,23 +102,6 @@ def test_p256_reduction(hc):
         assert int.from_bytes(out.raw, "little") == x % p, hex(x)
 
 
-@pytest.mark.parametrize("form", [0, 1], ids=["rows", "karatsuba"])
-def test_sqr_wide_forms(hc, form):
-    """Both square forms, including equal halves, a0 < a1 and all-ones limbs."""
-    rng = random.Random(60 + form)
-    h = 2**128
-    cases = [2**256 - 1, 0, 1, h, h - 1, h * 5 + 3, 3 * h + 5, (h - 1) * h, h - 1 + (h - 1) * h]
-    for _ in range(400):
-        a1, a0 = (rng.choice([rng.getrandbits(128), 0, h - 1, rng.getrandbits(8)]) for _ in range(2))
-        cases.append(a1 * h + a0)
-    cases += [rng.getrandbits(256) for _ in range(400)]
-    hc.hc_sqr_wide_form.argtypes = [ctypes.c_int, ctypes.c_char_p, ctypes.c_char_p]
-    for a in cases:
-        out = ctypes.create_string_buffer(64)
-        hc.hc_sqr_wide_form(form, le(a), out)
-        assert int.from_bytes(out.raw, "little") == a * a, hex(a)
-
-
 def test_sqr_wide(hc):
     rng = random.Random(6)
     cases = [2**256 - 1, 0, 1, 2**255, 2**32 - 1] + [rng.getrandbits(256) for _ in range(500)]
@@ -172,6 +155,18 @@ def test_ed25519_golden(hc):
     for v in G["ed25519"]:
         st = hc.hc_ed_verify(bytes.fromhex(v["sig"]), bytes.fromhex(v["msg"]), bytes.fromhex(v["pubkey"]))
         assert st == v["status"], v["case"]
+
+
+def test_ed25519_raw_golden(hc):
+    """Messages of any length: the multi-block challenge hash straddles the
+    SHA-512 block boundaries; verdicts from OpenSSL and libsodium."""
+    from tests.golden_io import load_raw
+
+    hc.hc_ed_verify_raw.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_uint32, ctypes.c_char_p]
+    for v in load_raw():
+        m = bytes.fromhex(v["msg"])
+        st = hc.hc_ed_verify_raw(bytes.fromhex(v["sig"]), m, len(m), bytes.fromhex(v["pubkey"]))
+        assert (st == 0) == v["valid"], (v["case"], v["len"])
 
 
 def test_random_vs_oracle(hc):

@@ -103,3 +103,17 @@ def test_log_limb_size_range():
     with pytest.raises(ValueError):
         o.ed25519_bases(10)
     assert o.num_limbs(13) == 20
+
+
+def test_ed25519_raw_golden():
+    """The oracle's any-length ed25519 check against OpenSSL / libsodium
+    verdicts (lengths around the SHA-512 block boundaries)."""
+    from tests.golden_io import load_raw
+
+    V = load_raw()
+    assert len({v["len"] for v in V}) >= 30
+    for v in V:
+        st, ok = o.ed25519_verify_raw(bytes.fromhex(v["sig"]), bytes.fromhex(v["msg"]), bytes.fromhex(v["pubkey"]))
+        assert ok == v["valid"], (v["case"], v["len"])
+        if v["case"] == "s_plus_l":
+            assert st == o.ST_BAD_SCALAR

@@ -71,6 +71,14 @@ inline uint32_t mul_hi(uint32_t a, uint32_t b) { ++mulcount_(); return (uint32_t
 
 #endif
 
+SG_HD uint32_t bswap32(uint32_t x) {
+#if defined(__CUDA_ARCH__)
+  return __byte_perm(x, 0, 0x0123);
+#else
+  return (x >> 24) | ((x >> 8) & 0xff00u) | ((x << 8) & 0xff0000u) | (x << 24);
+#endif
+}
+
 // 256-bit unsigned integer, little-endian 32-bit limbs.
 struct u256 {
   uint32_t w[8];
@@ -296,106 +304,6 @@ SG_HD void sqr_wide(uint32_t r[16], const u256& a) {
     r[2 * i] = madc_lo_cc(a.w[i], a.w[i], d[2 * i]);
     r[2 * i + 1] = (i < 7) ? madc_hi_cc(a.w[i], a.w[i], d[2 * i + 1]) : madc_hi(a.w[i], a.w[i], d[2 * i + 1]);
   }
-}
-
-// 2N-limb square r = a^2 of an N-limb value (N even): the same row scheme as
-// sqr_wide, for any even N.
-template <int N>
-SG_HD void sqr_rows(uint32_t* r, const uint32_t* a) {
-  uint32_t e[2 * N], o[2 * N];
-  e[0] = 0;
-  e[1] = 0;
-#pragma unroll
-  for (int j = 2; j < N; j += 2) {
-    e[j] = mul_lo(a[j], a[0]);
-    e[j + 1] = mul_hi(a[j], a[0]);
-  }
-#pragma unroll
-  for (int j = 1; j < N; j += 2) {
-    o[j] = mul_lo(a[j], a[0]);
-    o[j + 1] = mul_hi(a[j], a[0]);
-  }
-  e[N] = 0;
-  o[N + 1] = 0;
-#pragma unroll
-  for (int i = 1; i < N - 1; ++i) {
-    const uint32_t bi = a[i];
-    const int j0 = (i & 1) ? i + 1 : i + 2;
-    if (j0 <= N - 2) {
-#pragma unroll
-      for (int j = j0; j <= N - 2; j += 2) {
-        e[i + j] = (j == j0) ? mad_lo_cc(a[j], bi, e[i + j]) : madc_lo_cc(a[j], bi, e[i + j]);
-        e[i + j + 1] = madc_hi_cc(a[j], bi, e[i + j + 1]);
-      }
-      e[i + N] = addc(0u, 0u);
-    } else {
-      e[i + N] = 0;
-    }
-    const int j1 = (i & 1) ? i + 2 : i + 1;
-#pragma unroll
-    for (int j = j1; j <= N - 1; j += 2) {
-      o[i + j] = (j == j1) ? mad_lo_cc(a[j], bi, o[i + j]) : madc_lo_cc(a[j], bi, o[i + j]);
-      o[i + j + 1] = madc_hi_cc(a[j], bi, o[i + j + 1]);
-    }
-    if (i + N + 1 < 2 * N) o[i + N + 1] = addc(0u, 0u);
-  }
-  e[2 * N - 1] = 0;
-  uint32_t c[2 * N];
-  c[0] = 0;
-  c[1] = add_cc(e[1], o[1]);
-#pragma unroll
-  for (int k = 2; k < 2 * N; ++k) c[k] = addc_cc(e[k], o[k]);
-  uint32_t d[2 * N];
-  d[0] = c[0] << 1;
-#pragma unroll
-  for (int k = 1; k < 2 * N; ++k) d[k] = (c[k] << 1) | (c[k - 1] >> 31);
-  r[0] = mad_lo_cc(a[0], a[0], d[0]);
-  r[1] = madc_hi_cc(a[0], a[0], d[1]);
-#pragma unroll
-  for (int i = 1; i < N; ++i) {
-    r[2 * i] = madc_lo_cc(a[i], a[i], d[2 * i]);
-    r[2 * i + 1] = (i < N - 1) ? madc_hi_cc(a[i], a[i], d[2 * i + 1]) : madc_hi(a[i], a[i], d[2 * i + 1]);
-  }
-}
-
-// 512-bit square by one subtractive Karatsuba level over 128-bit halves:
-//   2 a0 a1 = a0^2 + a1^2 - (a0 - a1)^2,
-// three 128-bit squares (60 multiplies instead of 72) and ~45 more adds.
-SG_HD void sqr_wide_kara(uint32_t r[16], const u256& a) {
-  uint32_t p0[8], p2[8], m[8], d[4], t[4];
-  sqr_rows<4>(p0, a.w);
-  sqr_rows<4>(p2, a.w + 4);
-  d[0] = sub_cc(a.w[0], a.w[4]);
-#pragma unroll
-  for (int k = 1; k < 4; ++k) d[k] = subc_cc(a.w[k], a.w[4 + k]);
-  const uint32_t sg = subc(0u, 0u);
-  t[0] = sub_cc(a.w[4], a.w[0]);
-#pragma unroll
-  for (int k = 1; k < 4; ++k) t[k] = subc_cc(a.w[4 + k], a.w[k]);
-#pragma unroll
-  for (int k = 0; k < 4; ++k) d[k] = sg ? t[k] : d[k];
-  sqr_rows<4>(m, d);
-  // mid = p0 + p2 - m = 2 a0 a1 (9 limbs, below 2^257)
-  uint32_t mid[9];
-  mid[0] = add_cc(p0[0], p2[0]);
-#pragma unroll
-  for (int k = 1; k < 8; ++k) mid[k] = addc_cc(p0[k], p2[k]);
-  mid[8] = addc(0u, 0u);
-  mid[0] = sub_cc(mid[0], m[0]);
-#pragma unroll
-  for (int k = 1; k < 8; ++k) mid[k] = subc_cc(mid[k], m[k]);
-  mid[8] = subc(mid[8], 0u);
-  // r = p0 + mid 2^128 + p2 2^256
-#pragma unroll
-  for (int k = 0; k < 4; ++k) r[k] = p0[k];
-  r[4] = add_cc(p0[4], mid[0]);
-#pragma unroll
-  for (int k = 5; k < 8; ++k) r[k] = addc_cc(p0[k], mid[k - 4]);
-#pragma unroll
-  for (int k = 8; k < 13; ++k) r[k] = addc_cc(p2[k - 8], mid[k - 4]);
-  r[13] = addc_cc(p2[5], 0u);
-  r[14] = addc_cc(p2[6], 0u);
-  r[15] = addc(p2[7], 0u);
 }
 
 }  // namespace sg

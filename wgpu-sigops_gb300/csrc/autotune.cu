@@ -5,8 +5,8 @@
 // curve mix is signed on the device (valid signatures, so every item runs the
 // full path).  Each curve's plain kernel is timed per variant with CUDA events
 // (one warm-up, best of three).  The batched engine is tuned in two stages: all
-// variants once on a short prefix of the probe (the prefix keeps the curve
-// mix: items are interleaved 4:3:3), then the eight fastest again on the whole
+// variants once on an 8-wave prefix of the probe (the prefix keeps the curve
+// mix: items are interleaved 4:3:3), then the twelve fastest again on the whole
 // probe, best of three.  The ranking of the concurrent single-curve kernels
 // depends on the batch size, so the probe should be as large as the batches
 // the caller runs.  The search space is the compiled variants: block shape and
@@ -207,9 +207,9 @@ extern "C" int sigops_autotune(sigops_ctx* ctx, size_t probe_items, char* report
   std::string rep = "{";
   int chosen[4] = {0, 0, 0, 0};
   // batched engine: stage 1, every variant once on a prefix of the interleaved
-  // probe; stage 2, the eight fastest on the whole probe, best of three
+  // probe; stage 2, the twelve fastest on the whole probe, best of three
   {
-    const size_t n_short = std::min(n, (size_t)v.num_sms * 256 * 4);
+    const size_t n_short = std::min(n, (size_t)v.num_sms * 256 * 8);
     auto run_batched = [&](int var, size_t items) {
       const int grid = v.num_sms * sg::batched_max_blocks_per_sm(var);
       const int classify_grid = (int)std::min((items + 255) / 256, (size_t)v.num_sms * 8);
@@ -235,7 +235,7 @@ extern "C" int sigops_autotune(sigops_ctx* ctx, size_t probe_items, char* report
     std::sort(stage1.begin(), stage1.end());
     float best = 1e30f;
     rep += ", \"batched_full\": {";
-    const size_t keep = std::min<size_t>(stage1.size(), 8);
+    const size_t keep = std::min<size_t>(stage1.size(), 12);
     for (size_t k = 0; k < keep; ++k) {
       const int var = stage1[k].second;
       const float ms = n == n_short ? stage1[k].first : run_batched(var, n);

@@ -418,6 +418,40 @@ int sigops_ed25519_ecverify_single(sigops_ctx* ctx, const uint8_t* sigs, const u
   return run_host_call(ctx, SIGOPS_ED25519, sigs, msgs, pks, n, valid, status);
 }
 
+int sigops_ed25519_verify_raw(sigops_ctx* ctx, const uint8_t* sigs, const uint8_t* msgs, size_t msgs_bytes, const uint64_t* msg_offsets,
+                              const uint32_t* msg_lens, const uint8_t* pks, size_t n, uint8_t* valid, uint8_t* status) {
+  if (n == 0) return SIGOPS_OK;
+  if (!sigs || !msg_offsets || !msg_lens || !pks || !valid || (!msgs && msgs_bytes)) return fail(SIGOPS_E_INVAL, "null buffer");
+  for (size_t i = 0; i < n; ++i)
+    if (msg_offsets[i] > msgs_bytes || msg_lens[i] > msgs_bytes - msg_offsets[i])
+      return fail(SIGOPS_E_INVAL, "message %zu (offset %llu, %u bytes) runs past the %zu message bytes", i,
+                  (unsigned long long)msg_offsets[i], msg_lens[i], msgs_bytes);
+  sigops_ctx* c = resolve(ctx);
+  if (!c) return SIGOPS_E_NODEV;
+  std::lock_guard<std::mutex> g(c->mu);
+  SG_CUDA(cudaSetDevice(c->device));
+  auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+  const size_t o_sig = 0, o_pk = al(n * 64), o_off = o_pk + al(n * 32), o_len = o_off + al(n * 8), o_msg = o_len + al(n * 4),
+               o_out = o_msg + al(msgs_bytes ? msgs_bytes : 1), o_st = o_out + al(n), total = o_st + al(n);
+  int rc = ensure_buffers(c, total);
+  if (rc) return rc;
+  memcpy(c->h_buf + o_sig, sigs, n * 64);
+  memcpy(c->h_buf + o_pk, pks, n * 32);
+  memcpy(c->h_buf + o_off, msg_offsets, n * 8);
+  memcpy(c->h_buf + o_len, msg_lens, n * 4);
+  if (msgs_bytes) memcpy(c->h_buf + o_msg, msgs, msgs_bytes);
+  SG_CUDA(cudaMemcpyAsync(c->d_buf, c->h_buf, o_out, cudaMemcpyHostToDevice, c->stream));
+  SG_CUDA(launch_raw_ed(c->d_buf + o_sig, c->d_buf + o_msg, (const uint64_t*)(c->d_buf + o_off), (const uint32_t*)(c->d_buf + o_len),
+                        c->d_buf + o_pk, n, c->d_gtab[SIGOPS_ED25519], c->d_buf + o_out, c->d_buf + o_st, c->d_err,
+                        c->grid[SIGOPS_ED25519], c->variant[SIGOPS_ED25519], c->stream));
+  SG_CUDA(cudaMemcpyAsync(c->h_buf + o_out, c->d_buf + o_out, total - o_out, cudaMemcpyDeviceToHost, c->stream));
+  rc = check_device_errors(c);
+  if (rc) return rc;
+  memcpy(valid, c->h_buf + o_out, n);
+  if (status) memcpy(status, c->h_buf + o_st, n);
+  return SIGOPS_OK;
+}
+
 int sigops_plain_device(sigops_ctx* ctx, int curve, const uint8_t* d_sigs, const uint8_t* d_msgs, const uint8_t* d_pks, size_t n,
                         uint8_t* d_out, uint8_t* d_status, void* stream) {
   if (!valid_curve(curve)) return fail(SIGOPS_E_INVAL, "bad curve %d", curve);

@@ -24,6 +24,9 @@ cudaError_t launch_plain_r1(const uint8_t* sigs, const uint8_t* msgs, size_t n, 
                             uint32_t* err, int grid, int variant, cudaStream_t stream);
 cudaError_t launch_plain_ed(const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks, size_t n, const uint32_t* btab, uint8_t* valid,
                             uint8_t* status, uint32_t* err, int grid, int variant, cudaStream_t stream);
+cudaError_t launch_raw_ed(const uint8_t* sigs, const uint8_t* msgs, const uint64_t* offsets, const uint32_t* lens, const uint8_t* pks,
+                          size_t n, const uint32_t* btab, uint8_t* valid, uint8_t* status, uint32_t* err, int grid, int variant,
+                          cudaStream_t stream);
 int occupancy_plain_k1(int variant);
 int occupancy_plain_r1(int variant);
 int occupancy_plain_ed(int variant);

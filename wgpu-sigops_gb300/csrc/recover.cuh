@@ -13,14 +13,6 @@ namespace sg {
 // per-item status (include/sigops.h SIGOPS_ST_*)
 enum : uint8_t { ST_OK = 0, ST_BAD_SCALAR = 1, ST_NO_POINT = 2, ST_INFINITY = 3, ST_MISMATCH = 4 };
 
-SG_HD uint32_t bswap32(uint32_t x) {
-#if defined(__CUDA_ARCH__)
-  return __byte_perm(x, 0, 0x0123);
-#else
-  return (x >> 24) | ((x >> 8) & 0xff00u) | ((x << 8) & 0xff0000u) | (x << 24);
-#endif
-}
-
 // 32 big-endian bytes (as 8 loaded words) -> integer
 SG_HD u256 be_words_to_u256(const uint32_t* w) {
   u256 r;
@@ -368,7 +360,10 @@ SG_NOINL EPoint ed_lincomb(const u256 s, const u256 k, const EPoint negA, const 
 // src/wgsl/main/ed25519_eddsa_main.wgsl:23-113 and
 // src/curve_algos/ed25519_eddsa.rs:49-77; adds the S < l check the reference
 // GPU path lacks (src/wgsl/main/ed25519_eddsa_main_0.wgsl:45-54).
-SG_HD uint8_t ed25519_verify(const uint32_t sig[16], const uint32_t msg[8], const uint32_t pk[8], const uint32_t* btab) {
+// challenge(R, A) returns k = SHA-512(R || A || M) mod l; it runs only after
+// the key and S checks passed.
+template <class Challenge>
+SG_HD uint8_t ed25519_verify_with(const uint32_t sig[16], const uint32_t pk[8], const uint32_t* btab, Challenge challenge) {
   u256 aenc;
 #pragma unroll
   for (int k = 0; k < 8; ++k) aenc.w[k] = pk[k];
@@ -378,7 +373,7 @@ SG_HD uint8_t ed25519_verify(const uint32_t sig[16], const uint32_t msg[8], cons
 #pragma unroll
   for (int k = 0; k < 8; ++k) { renc.w[k] = sig[k]; s.w[k] = sig[8 + k]; }
   if (u256_gte(s, EdScalarC::N())) return ST_BAD_SCALAR;
-  u256 k = ed_challenge(sig, pk, msg);
+  u256 k = challenge(renc, aenc);
   EPoint negA;
   negA.X = FpEd::neg(A.X);
   negA.Y = A.Y;
@@ -387,6 +382,20 @@ SG_HD uint8_t ed25519_verify(const uint32_t sig[16], const uint32_t msg[8], cons
   EPoint Rp = ed_lincomb<>(s, k, negA, btab);
   u256 enc = Edw::compress(Rp);
   return u256_eq(enc, renc) ? ST_OK : ST_MISMATCH;
+}
+
+// the reference's API: 32-byte (fuel) messages
+SG_HD uint8_t ed25519_verify(const uint32_t sig[16], const uint32_t msg[8], const uint32_t pk[8], const uint32_t* btab) {
+  return ed25519_verify_with(sig, pk, btab, [&](const u256&, const u256&) { return ed_challenge(sig, pk, msg); });
+}
+
+// a message of any length (msg: len bytes, device memory on the GPU)
+SG_HD uint8_t ed25519_verify_raw(const uint32_t sig[16], const uint8_t* msg, uint32_t len, const uint32_t pk[8], const uint32_t* btab) {
+  return ed25519_verify_with(sig, pk, btab, [&](const u256& renc, const u256& aenc) {
+    uint32_t h[16];
+    sha512_ed_raw<>(renc, aenc, msg, len, h);
+    return reduce512_mod_l(h);
+  });
 }
 
 }  // namespace sg

@@ -16,9 +16,19 @@ SG_HD uint64_t rotr64(uint64_t x, int n) { return (x >> n) | (x << (64 - n)); }
 // One-block SHA-512 of NB bytes (NB a multiple of 8, at most 104).
 // m: the input bytes as NB/4 little-endian u32 words (as loaded from memory).
 // out: the 64-byte digest as 16 little-endian u32 words (digest byte order).
-template <int NB>
-SG_HD void sha512_fixed(const uint32_t* m, uint32_t out[16]) {
-  static_assert(NB % 8 == 0 && NB <= 104, "one-block input");
+SG_HD void sha512_init(uint64_t st[8]) {
+  st[0] = 0x6a09e667f3bcc908ull;
+  st[1] = 0xbb67ae8584caa73bull;
+  st[2] = 0x3c6ef372fe94f82bull;
+  st[3] = 0xa54ff53a5f1d36f1ull;
+  st[4] = 0x510e527fade682d1ull;
+  st[5] = 0x9b05688c2b3e6c1full;
+  st[6] = 0x1f83d9abfb41bd6bull;
+  st[7] = 0x5be0cd19137e2179ull;
+}
+
+// one 128-byte block (w: 16 big-endian 64-bit words, overwritten) into st
+SG_HD void sha512_compress(uint64_t st[8], uint64_t w[16]) {
   const uint64_t K[80] = {
     0x428a2f98d728ae22ull, 0x7137449123ef65cdull, 0xb5c0fbcfec4d3b2full, 0xe9b5dba58189dbbcull,
     0x3956c25bf348b538ull, 0x59f111f1b605d019ull, 0x923f82a4af194f9bull, 0xab1c5ed5da6d8118ull,
@@ -41,23 +51,7 @@ SG_HD void sha512_fixed(const uint32_t* m, uint32_t out[16]) {
     0x28db77f523047d84ull, 0x32caab7b40c72493ull, 0x3c9ebe0a15c9bebcull, 0x431d67c49c100d4cull,
     0x4cc5d4becb3e42b6ull, 0x597f299cfc657e2aull, 0x5fcb6fab3ad6faecull, 0x6c44198c4a475817ull,
   };
-  uint64_t w[16];
-#pragma unroll
-  for (int i = 0; i < 16; ++i) {
-    if (i < NB / 8) {
-      uint32_t hi = m[2 * i], lo = m[2 * i + 1];
-      hi = (hi >> 24) | ((hi >> 8) & 0xff00u) | ((hi << 8) & 0xff0000u) | (hi << 24);
-      lo = (lo >> 24) | ((lo >> 8) & 0xff00u) | ((lo << 8) & 0xff0000u) | (lo << 24);
-      w[i] = ((uint64_t)hi << 32) | lo;
-    } else if (i == NB / 8) {
-      w[i] = 0x8000000000000000ull;
-    } else {
-      w[i] = 0;
-    }
-  }
-  w[15] = (uint64_t)NB * 8;
-  const uint64_t H0[8] = { 0x6a09e667f3bcc908ull, 0xbb67ae8584caa73bull, 0x3c6ef372fe94f82bull, 0xa54ff53a5f1d36f1ull, 0x510e527fade682d1ull, 0x9b05688c2b3e6c1full, 0x1f83d9abfb41bd6bull, 0x5be0cd19137e2179ull };
-  uint64_t a = H0[0], b = H0[1], c = H0[2], d = H0[3], e = H0[4], f = H0[5], g = H0[6], h = H0[7];
+  uint64_t a = st[0], b = st[1], c = st[2], d = st[3], e = st[4], f = st[5], g = st[6], h = st[7];
 #pragma unroll
   for (int i = 0; i < 80; ++i) {
     uint64_t wi;
@@ -78,17 +72,98 @@ SG_HD void sha512_fixed(const uint32_t* m, uint32_t out[16]) {
     uint64_t t2 = S0 + maj;
     h = g; g = f; f = e; e = d + t1; d = c; c = b; b = a; a = t1 + t2;
   }
-  uint64_t st[8] = {a, b, c, d, e, f, g, h};
+  st[0] += a;
+  st[1] += b;
+  st[2] += c;
+  st[3] += d;
+  st[4] += e;
+  st[5] += f;
+  st[6] += g;
+  st[7] += h;
+}
+
+// the 64-byte digest as 16 little-endian u32 words (digest byte order)
+SG_HD void sha512_digest(const uint64_t st[8], uint32_t out[16]) {
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
-    uint64_t v = st[i] + H0[i];
-    uint32_t hi = (uint32_t)(v >> 32), lo = (uint32_t)v;
-    out[2 * i] = (hi >> 24) | ((hi >> 8) & 0xff00u) | ((hi << 8) & 0xff0000u) | (hi << 24);
-    out[2 * i + 1] = (lo >> 24) | ((lo >> 8) & 0xff00u) | ((lo << 8) & 0xff0000u) | (lo << 24);
+    out[2 * i] = bswap32((uint32_t)(st[i] >> 32));
+    out[2 * i + 1] = bswap32((uint32_t)st[i]);
   }
+}
+
+// One-block SHA-512 of NB bytes (NB a multiple of 8, at most 104).
+// m: the input bytes as NB/4 little-endian u32 words (as loaded from memory).
+// out: the 64-byte digest as 16 little-endian u32 words (digest byte order).
+template <int NB>
+SG_HD void sha512_fixed(const uint32_t* m, uint32_t out[16]) {
+  static_assert(NB % 8 == 0 && NB <= 104, "one-block input");
+  uint64_t w[16];
+#pragma unroll
+  for (int i = 0; i < 16; ++i) {
+    if (i < NB / 8) {
+      w[i] = ((uint64_t)bswap32(m[2 * i]) << 32) | bswap32(m[2 * i + 1]);
+    } else if (i == NB / 8) {
+      w[i] = 0x8000000000000000ull;
+    } else {
+      w[i] = 0;
+    }
+  }
+  w[15] = (uint64_t)NB * 8;
+  uint64_t st[8];
+  sha512_init(st);
+  sha512_compress(st, w);
+  sha512_digest(st, out);
 }
 
 // the ed25519 challenge preimage R || A || M
 SG_HD void sha512_96(const uint32_t m[24], uint32_t out[16]) { sha512_fixed<96>(m, out); }
+
+// SHA-512 of R || A || msg for a message of any length (ed25519 over raw
+// messages): R and A as 8 little-endian u32 words each, msg as bytes (device
+// memory on the GPU).  ceil((64 + len + 17) / 128) blocks; every lane of a
+// warp runs the block count of its own message.
+template <int = 0>
+SG_NOINL void sha512_ed_raw(const u256 R, const u256 A, const uint8_t* msg, uint32_t len, uint32_t out[16]) {
+  const uint64_t total = 64ull + len;
+  const uint64_t nblocks = (total + 17 + 127) / 128;
+  uint64_t st[8];
+  sha512_init(st);
+#pragma unroll 1
+  for (uint64_t blk = 0; blk < nblocks; ++blk) {
+    uint64_t w[16];
+#pragma unroll
+    for (int t = 0; t < 16; ++t) {
+      const uint64_t base = blk * 128 + (uint64_t)t * 8;
+      uint64_t v = 0;
+      if (base + 8 <= 64) {  // a whole word of R || A
+        const uint32_t* src = base < 32 ? R.w : A.w;
+        const int k = (int)((base & 31) >> 2);
+        v = ((uint64_t)bswap32(src[k]) << 32) | bswap32(src[k + 1]);
+      } else {
+#pragma unroll 1
+        for (int q = 0; q < 8; ++q) {
+          const uint64_t pos = base + q;
+          uint32_t byte = 0;
+          if (pos < 64) {
+            const uint32_t* src = pos < 32 ? R.w : A.w;
+            byte = (src[(pos & 31) >> 2] >> (8 * (pos & 3))) & 0xffu;
+          } else if (pos < total) {
+            byte = msg[pos - 64];
+          } else if (pos == total) {
+            byte = 0x80u;
+          }
+          v = (v << 8) | byte;
+        }
+      }
+      w[t] = v;
+    }
+    if (blk + 1 == nblocks) {  // 128-bit big-endian bit length in the last 16 bytes
+      w[14] = 0;
+      w[15] = total * 8;
+    }
+    sha512_compress(st, w);
+  }
+  sha512_digest(st, out);
+}
 
 }  // namespace sg

@@ -48,6 +48,7 @@ SIGNATURES = {
     "sigops_secp256r1_ecrecover_single_shader": (ctypes.c_int, [_vp, _vp, _vp, _sz, ctypes.c_uint32, _vp, _vp]),
     "sigops_ed25519_ecverify": (ctypes.c_int, [_vp, _vp, _vp, _vp, _sz, _u32p, _sz, ctypes.c_uint32, _vp, _vp]),
     "sigops_ed25519_ecverify_single": (ctypes.c_int, [_vp, _vp, _vp, _vp, _sz, ctypes.c_uint32, _vp, _vp]),
+    "sigops_ed25519_verify_raw": (ctypes.c_int, [_vp, _vp, _vp, _sz, _vp, _vp, _vp, _sz, _vp, _vp]),
     "sigops_plain_device": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp, _vp, _sz, _vp, _vp, _vp]),
     "sigops_verify_mixed": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _sz, _vp, _vp]),
     "sigops_verify_mixed_device": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _sz, _vp, _vp, _vp]),

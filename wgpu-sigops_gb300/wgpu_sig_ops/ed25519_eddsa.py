@@ -50,3 +50,36 @@ def ecverify_single(signatures, messages, verifying_keys, log_limb_size: int, ct
     """`ecverify_single` (src/ed25519_eddsa.rs:259-324)."""
     valid, _ = ecverify_arrays(signatures, messages, verifying_keys, None, log_limb_size, ctx)
     return [bool(v) for v in valid]
+
+
+def verify_raw_arrays(signatures, messages, verifying_keys, ctx=None):
+    """Messages of any length (list of bytes-like): returns (valid (n,) uint8
+    0/1, status (n,) uint8).  No counterpart in the reference, whose API takes
+    32-byte messages only."""
+    sigs = as_rows(signatures, 64, "signatures")
+    pks = as_rows(verifying_keys, 32, "verifying_keys")
+    msgs = [bytes(m) for m in messages]
+    if not (len(sigs) == len(msgs) == len(pks)):
+        raise ValueError(f"lengths differ: {len(sigs)} signatures, {len(msgs)} messages, {len(pks)} keys")
+    n = len(sigs)
+    lens = np.array([len(m) for m in msgs], dtype=np.uint32)
+    offsets = np.zeros(n, dtype=np.uint64)
+    if n:
+        offsets[1:] = np.cumsum(lens[:-1], dtype=np.uint64)
+    blob = np.frombuffer(b"".join(msgs), dtype=np.uint8) if n else np.zeros(0, np.uint8)
+    blob = np.ascontiguousarray(blob) if len(blob) else np.zeros(1, np.uint8)
+    valid = np.zeros(n, dtype=np.uint8)
+    status = np.zeros(n, dtype=np.uint8)
+    c = (ctx or default_context()).ptr
+    rc = lib.sigops_ed25519_verify_raw(c, ptr(sigs), ptr(blob), int(lens.sum()), ptr(offsets), ptr(lens), ptr(pks), n, ptr(valid),
+                                       ptr(status))
+    if rc < 0:
+        _raise(rc, "sigops_ed25519_verify_raw")
+    return valid, status
+
+
+def verify_raw(signatures, messages, verifying_keys, ctx=None) -> list[bool]:
+    """ed25519-dalek `VerifyingKey::verify(&[u8], &Signature)` per item, for
+    messages of any length."""
+    valid, _ = verify_raw_arrays(signatures, messages, verifying_keys, ctx)
+    return [bool(v) for v in valid]
