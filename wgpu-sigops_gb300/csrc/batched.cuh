@@ -103,6 +103,22 @@ __device__ __forceinline__ uint8_t ed_item(const MixedIO& io, size_t i, const ui
 }
 
 // one launch's work: tables staged, then tiles until the queue is empty
+// One item: load, verify or recover, store.  Called rather than inlined, so
+// that the tile loop's pointers and counters are saved once per signature
+// instead of staying live (about 20 registers) through its arithmetic.
+template <int CURVE>
+__device__ __noinline__ void batched_item(const MixedIO io, size_t i, const uint32_t* tab) {
+  uint32_t s[16], m[8], o[16];
+  load_words(io.sigs, i, 16, s);
+  load_words(io.msgs, i, 8, m);
+  uint8_t st;
+  if constexpr (CURVE == 0) st = ecdsa_recover<K1Traits, true>(s, m, tab, o);
+  else if constexpr (CURVE == 1) st = ecdsa_recover<R1Traits>(s, m, tab, o);
+  else st = ed_item(io, i, s, m, tab, o);
+  store_words(io.out, i, 16, o);
+  io.status[i] = st;
+}
+
 template <int CM>
 __device__ __forceinline__ void batched_body(const MixedIO& io, const uint32_t* __restrict__ idx, const BatchTables& tabs, Scratch* sc,
                                              uint32_t* err) {
@@ -133,24 +149,18 @@ __device__ __forceinline__ void batched_body(const MixedIO& io, const uint32_t* 
     const uint32_t slot = first + lane;
     if (slot < cnt) {
       const size_t i = idx[(size_t)curve * io.n + slot];
-      uint32_t s[16], m[8], o[16];
-      load_words(io.sigs, i, 16, s);
-      load_words(io.msgs, i, 8, m);
-      uint8_t st;
       if constexpr (CM == CM_K1) {
-        st = ecdsa_recover<K1Traits, true>(s, m, tk1, o);
+        batched_item<0>(io, i, tk1);
       } else if constexpr (CM == CM_R1) {
-        st = ecdsa_recover<R1Traits>(s, m, tr1, o);
+        batched_item<1>(io, i, tr1);
       } else if constexpr (CM == CM_ED) {
-        st = ed_item(io, i, s, m, ted, o);
+        batched_item<2>(io, i, ted);
       } else {
         static_assert(CM == CM_ALL, "one curve or all three");
-        if (curve == 0) st = ecdsa_recover<K1Traits, true>(s, m, tk1, o);
-        else if (curve == 1) st = ecdsa_recover<R1Traits>(s, m, tr1, o);
-        else st = ed_item(io, i, s, m, ted, o);
+        if (curve == 0) batched_item<0>(io, i, tk1);
+        else if (curve == 1) batched_item<1>(io, i, tr1);
+        else batched_item<2>(io, i, ted);
       }
-      store_words(io.out, i, 16, o);
-      io.status[i] = st;
     }
   }
 }
