@@ -5,15 +5,18 @@
 // (src/secp256k1_ecdsa.rs:25-44); it has no mixed-curve path.  Here:
 //   1. classify_kernel buckets item indices by curve (warp-aggregated atomics
 //      into per-curve index lists);
-//   2. batched_kernel runs a persistent grid: each warp repeatedly takes the
-//      next 32-item tile from a global counter; tiles never straddle curves, so
-//      the curve dispatch is warp-uniform and no lane idles on another curve's
-//      code.  The generator tables it needs are staged into shared memory by
-//      bulk (TMA) copies completing on one mbarrier.
-// The curve mask CM selects what one launch serves: CM_ALL is the fused
-// kernel (one queue over all three curves, registers sized for the largest
-// path); a single-curve mask gives a kernel with that curve's own register
-// budget, and the three are launched side by side on forked streams.
+//   2. either the fused batched_kernel, a persistent grid in which each warp
+//      repeatedly takes the next 32-item tile from a global counter (tiles
+//      never straddle curves, so the curve dispatch is warp-uniform and no
+//      lane idles on another curve's code), registers sized for the largest
+//      path;
+//   3. or three single-curve kernels (batched_curve_kernel), one item per
+//      thread and no loop, each with its own register budget, launched side
+//      by side on forked streams.  With no loop state live across the
+//      signature arithmetic, the 168-register budget (12 warps per SM) fits
+//      secp256k1 recovery with small spills.
+// The generator tables a block needs are staged into shared memory by bulk
+// (TMA) copies completing on one mbarrier.
 // Scratch (global memory beyond inputs and outputs): Scratch below.
 #pragma once
 #include "kernels.cuh"
@@ -27,10 +30,9 @@ constexpr uint32_t QUEUE_MAX_SPINS = 1u << 20;
 constexpr int CM_K1 = 1, CM_R1 = 2, CM_ED = 4, CM_ALL = 7;
 
 struct Scratch {
-  uint32_t count[3];            // items per curve (classify)
-  uint32_t next_tile;           // work-stealing counter of the fused kernel
-  uint32_t tiles_done;          // unused; keeps the record at 32 bytes
-  uint32_t next_curve_tile[3];  // work-stealing counters of the single-curve kernels
+  uint32_t count[3];   // items per curve (classify)
+  uint32_t next_tile;  // work-stealing counter of the fused kernel
+  uint32_t pad[4];     // keeps the record at 32 bytes
 };
 
 // Mixed output record: ECDSA key bytes, or for ed25519 byte 0 = valid.
@@ -131,10 +133,7 @@ __device__ __forceinline__ void batched_body(const MixedIO& io, const uint32_t* 
   const uint32_t n1 = (CM & CM_K1) ? sc->count[0] : 0, n2 = (CM & CM_R1) ? sc->count[1] : 0, n3 = (CM & CM_ED) ? sc->count[2] : 0;
   const uint32_t t1 = (n1 + BATCH_TILE - 1) / BATCH_TILE, t2 = (n2 + BATCH_TILE - 1) / BATCH_TILE, t3 = (n3 + BATCH_TILE - 1) / BATCH_TILE;
   const uint32_t total = t1 + t2 + t3;
-  uint32_t* counter = CM == CM_K1 ? &sc->next_curve_tile[0]
-                      : CM == CM_R1 ? &sc->next_curve_tile[1]
-                      : CM == CM_ED ? &sc->next_curve_tile[2]
-                                    : &sc->next_tile;
+  uint32_t* counter = &sc->next_tile;
   const unsigned lane = threadIdx.x & 31u;
   for (;;) {
     uint32_t tile = 0;
@@ -165,18 +164,54 @@ __device__ __forceinline__ void batched_body(const MixedIO& io, const uint32_t* 
   }
 }
 
-// occupancy by blocks per SM (__launch_bounds__) ...
+// the fused kernel (CM_ALL): occupancy by blocks per SM
 template <int BLOCK, int MINB, int CM>
 __global__ void __launch_bounds__(BLOCK, MINB) batched_kernel(MixedIO io, const uint32_t* __restrict__ idx, BatchTables tabs, Scratch* sc,
                                                         uint32_t* err) {
   batched_body<CM>(io, idx, tabs, sc, err);
 }
 
+
+// Single-curve kernel body: block b serves items [b BLOCK, (b + 1) BLOCK) of
+// curve CURVE's index list; blocks past the list's end return before staging.
+template <int BLOCK, int CURVE>
+__device__ __forceinline__ void curve_body(const MixedIO& io, const uint32_t* __restrict__ idx, const BatchTables& tabs, Scratch* sc,
+                                           uint32_t* err) {
+  constexpr int CM = CURVE == 0 ? CM_K1 : CURVE == 1 ? CM_R1 : CM_ED;
+  const uint32_t cnt = sc->count[CURVE];
+  const uint32_t first = blockIdx.x * BLOCK;
+  if (first >= cnt) return;
+  __shared__ __align__(128) uint32_t tk1[(CM & CM_K1) ? 2 * ECDSA_GTAB * 16 : 4];  // G and 2^128 G multiples (GLV)
+  __shared__ __align__(128) uint32_t tr1[(CM & CM_R1) ? ECDSA_GTAB * 16 : 4];
+  __shared__ __align__(128) uint32_t ted[(CM & CM_ED) ? ED_GTAB * 24 : 4];
+  __shared__ __align__(8) uint64_t bar;
+  if (!stage_tables<CM>(tk1, tr1, ted, tabs, &bar, err)) return;
+  const uint32_t slot = first + threadIdx.x;
+  if (slot >= cnt) return;
+  const size_t i = idx[(size_t)CURVE * io.n + slot];
+  uint32_t s[16], m[8], o[16];
+  load_words(io.sigs, i, 16, s);
+  load_words(io.msgs, i, 8, m);
+  uint8_t st;
+  if constexpr (CURVE == 0) st = ecdsa_recover<K1Traits, true>(s, m, tk1, o);
+  else if constexpr (CURVE == 1) st = ecdsa_recover<R1Traits>(s, m, tr1, o);
+  else st = ed_item(io, i, s, m, ted, o);
+  store_words(io.out, i, 16, o);
+  io.status[i] = st;
+}
+
+// occupancy by blocks per SM ...
+template <int BLOCK, int MINB, int CURVE>
+__global__ void __launch_bounds__(BLOCK, MINB) batched_curve_kernel(MixedIO io, const uint32_t* __restrict__ idx, BatchTables tabs, Scratch* sc,
+                                                                uint32_t* err) {
+  curve_body<BLOCK, CURVE>(io, idx, tabs, sc, err);
+}
+
 // ... or by an explicit register cap
-template <int BLOCK, int MAXREG, int CM>
-__global__ void __launch_bounds__(BLOCK) __maxnreg__(MAXREG) batched_kernel_r(MixedIO io, const uint32_t* __restrict__ idx, BatchTables tabs,
-                                                                            Scratch* sc, uint32_t* err) {
-  batched_body<CM>(io, idx, tabs, sc, err);
+template <int BLOCK, int MAXREG, int CURVE>
+__global__ void __launch_bounds__(BLOCK) __maxnreg__(MAXREG) batched_curve_kernel_r(MixedIO io, const uint32_t* __restrict__ idx,
+                                                                                  BatchTables tabs, Scratch* sc, uint32_t* err) {
+  curve_body<BLOCK, CURVE>(io, idx, tabs, sc, err);
 }
 
 }  // namespace sg

@@ -37,9 +37,9 @@ cudaError_t batched_launch_0(const MixedIO&, const uint32_t*, const BatchTables&
 cudaError_t batched_launch_1(const MixedIO&, const uint32_t*, const BatchTables&, Scratch*, uint32_t*, int, cudaStream_t);
 cudaError_t batched_launch_2(const MixedIO&, const uint32_t*, const BatchTables&, Scratch*, uint32_t*, int, cudaStream_t);
 cudaError_t batched_launch_3(const MixedIO&, const uint32_t*, const BatchTables&, Scratch*, uint32_t*, int, cudaStream_t);
-cudaError_t batched_launch_k1(int, const MixedIO&, const uint32_t*, const BatchTables&, Scratch*, uint32_t*, int, cudaStream_t);
-cudaError_t batched_launch_r1(int, const MixedIO&, const uint32_t*, const BatchTables&, Scratch*, uint32_t*, int, cudaStream_t);
-cudaError_t batched_launch_ed(int, const MixedIO&, const uint32_t*, const BatchTables&, Scratch*, uint32_t*, int, cudaStream_t);
+cudaError_t batched_launch_k1(int, const MixedIO&, const uint32_t*, const BatchTables&, Scratch*, uint32_t*, cudaStream_t);
+cudaError_t batched_launch_r1(int, const MixedIO&, const uint32_t*, const BatchTables&, Scratch*, uint32_t*, cudaStream_t);
+cudaError_t batched_launch_ed(int, const MixedIO&, const uint32_t*, const BatchTables&, Scratch*, uint32_t*, cudaStream_t);
 
 static const int kFusedBlock[BATCHED_FUSED_VARIANTS] = {256, 256, 128, 64};
 
@@ -112,16 +112,15 @@ void fork_streams_destroy(ForkStreams* f) {
 }
 
 static cudaError_t launch_curve(int c, int level, const MixedIO& io, const uint32_t* idx, const BatchTables& t, Scratch* sc,
-                                uint32_t* err, int grid, cudaStream_t s) {
-  if (c == 0) return batched_launch_k1(level, io, idx, t, sc, err, grid, s);
-  if (c == 1) return batched_launch_r1(level, io, idx, t, sc, err, grid, s);
-  return batched_launch_ed(level, io, idx, t, sc, err, grid, s);
+                                uint32_t* err, cudaStream_t s) {
+  if (c == 0) return batched_launch_k1(level, io, idx, t, sc, err, s);
+  if (c == 1) return batched_launch_r1(level, io, idx, t, sc, err, s);
+  return batched_launch_ed(level, io, idx, t, sc, err, s);
 }
 
 cudaError_t launch_batched(const uint8_t* curves, const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks, size_t n, uint8_t* out,
                            uint8_t* status, uint32_t* idx, void* scratch, const uint32_t* gk1, const uint32_t* gr1, const uint32_t* ged,
-                           uint32_t* err, int grid, int variant, int classify_grid, int num_sms, const ForkStreams* fork,
-                           cudaStream_t stream) {
+                           uint32_t* err, int grid, int variant, int classify_grid, const ForkStreams* fork, cudaStream_t stream) {
   if (n == 0) return cudaSuccess;
   if (variant < 0 || variant >= BATCHED_VARIANTS || grid <= 0) return cudaErrorInvalidValue;
   Scratch* sc = (Scratch*)scratch;
@@ -150,13 +149,8 @@ cudaError_t launch_batched(const uint8_t* curves, const uint8_t* sigs, const uin
   }
   cudaError_t first = cudaSuccess;
   for (int c = 0; c < 3; ++c) {
-    // blocks: a full persistent grid, at most one item per thread, and at most
-    // the caller's grid (counted in 256-thread blocks)
-    const int l = split_level(variant, c), block = kLevelBlock[l];
-    size_t g = (size_t)num_sms * curve_occupancy(c, l);
-    g = std::min(g, (n + block - 1) / block);
-    g = std::min(g, (size_t)grid * 256 / block);
-    e = launch_curve(c, l, io, idx, t, sc, err, (int)std::max<size_t>(g, 1), s[c]);
+    // one item per thread: the kernel sizes its grid to the batch
+    e = launch_curve(c, split_level(variant, c), io, idx, t, sc, err, s[c]);
     if (e != cudaSuccess && first == cudaSuccess) first = e;
   }
   if (fork) {  // join, even after a failed launch, so no side stream stays forked

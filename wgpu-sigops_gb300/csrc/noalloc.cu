@@ -109,6 +109,6 @@ extern "C" int sigops_verify_mixed_noalloc(const uint8_t* d_curves, const uint8_
   // the per-curve index lists follow the counters; launch_batched clears the counters
   uint32_t* idx = reinterpret_cast<uint32_t*>(d->scratch + kScratchHead);
   cudaError_t e = sg::launch_batched(d_curves, d_sigs, d_msgs, d_pks, n, d_out, d_status, idx, d->scratch, d->tab[0], d->tab[1], d->tab[2],
-                                     d->err, d->grid, 0, classify_grid, d->num_sms, nullptr, (cudaStream_t)stream);
+                                     d->err, d->grid, 0, classify_grid, nullptr, (cudaStream_t)stream);
   return e == cudaSuccess ? SIGOPS_OK : SIGOPS_E_CUDA;
 }

@@ -149,7 +149,7 @@ void pack_and_launch(sigops_server* s, Slot& sl) {
   const int grid = (int)std::min<size_t>((size_t)grid_cap, (n + block - 1) / block);
   cudaError_t e = sg::launch_batched(sl.d + L.cur, sl.d + L.sig, sl.d + L.msg, sl.d + L.pk, n, sl.d + L.out, sl.d + L.st, sl.d_idx,
                                      sl.d_scratch, s->cv.gtab[0], s->cv.gtab[1], s->cv.gtab[2], s->cv.d_err, grid, variant,
-                                     classify_grid, s->cv.num_sms, nullptr, sl.stream);
+                                     classify_grid, nullptr, sl.stream);
   cudaMemcpyAsync(sl.h + L.out, sl.d + L.out, n * 64, cudaMemcpyDeviceToHost, sl.stream);
   cudaMemcpyAsync(sl.h + L.st, sl.d + L.st, n, cudaMemcpyDeviceToHost, sl.stream);
   cudaEventRecord(sl.done, sl.stream);
