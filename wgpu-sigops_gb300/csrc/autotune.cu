@@ -217,7 +217,7 @@ extern "C" int sigops_autotune(sigops_ctx* ctx, size_t probe_items, char* report
           [&] {
             sg::launch_batched(d.p + o_icur, d.p + o_isig, d.p + o_imsg, d.p + o_ipk, items, d.p + o_out, d.p + o_st,
                                (uint32_t*)(d.p + o_idx), d.p + o_scr, v.gtab[0], v.gtab[1], v.gtab[2], v.d_err, grid, var, classify_grid,
-                               v.num_sms, &fork, st);
+                               &fork, st);
           },
           items == n ? 3 : 1);
     };
@@ -257,12 +257,10 @@ extern "C" int sigops_autotune(sigops_ctx* ctx, size_t probe_items, char* report
     snprintf(b, sizeof b, ", \"plain_%d\": {", c);
     rep += b;
     for (int var = 0; var < sg::PLAIN_VARIANTS; ++var) {
-      int bps = sg::plain_max_blocks_per_sm(c, var);
-      if (bps <= 0) continue;
-      const int grid = v.num_sms * bps;
+      if (sg::plain_max_blocks_per_sm(c, var) <= 0) continue;
       float ms = time_it([&] {
         sg::launch_plain(c, d.p + o_sig + off[c] * 64, d.p + o_msg + off[c] * 32, d.p + o_pk + off[c] * 32, cnt[c], v.gtab[c],
-                         d.p + o_out, d.p + o_st, v.d_err, grid, var, st);
+                         d.p + o_out, d.p + o_st, v.d_err, var, st);
       });
       snprintf(b, sizeof b, "%s\"%d\": %.3f", var ? ", " : "", var, ms);
       rep += b;

@@ -184,7 +184,7 @@ cudaError_t launch_mixed(sigops_ctx* c, const uint8_t* curves, const uint8_t* si
   size_t cg = (n + 255) / 256;
   int classify_grid = (int)(cg < (size_t)c->num_sms * 8 ? cg : (size_t)c->num_sms * 8);
   return launch_batched(curves, sigs, msgs, pks, n, out, status, c->d_idx, c->d_scratch, c->d_gtab[0], c->d_gtab[1], c->d_gtab[2], c->d_err,
-                        c->batched_grid, c->batched_variant, classify_grid, c->num_sms, &c->fork, s);
+                        c->batched_grid, c->batched_variant, classify_grid, &c->fork, s);
 }
 
 int check_device_errors(sigops_ctx* c) {
@@ -243,7 +243,7 @@ int run_host_call(sigops_ctx* ctx, int curve, const uint8_t* sigs, const uint8_t
   if (curve == SIGOPS_ED25519) memcpy(c->h_buf + l.pk, pks, n * 32);
   SG_CUDA(cudaMemcpyAsync(c->d_buf, c->h_buf, l.out, cudaMemcpyHostToDevice, c->stream));
   SG_CUDA(launch_plain(curve, c->d_buf + l.sig, c->d_buf + l.msg, c->d_buf + l.pk, n, c->d_gtab[curve], c->d_buf + l.out,
-                       c->d_buf + l.status, c->d_err, c->grid[curve], c->variant[curve], c->stream));
+                       c->d_buf + l.status, c->d_err, c->variant[curve], c->stream));
   SG_CUDA(cudaMemcpyAsync(c->h_buf + l.out, c->d_buf + l.out, l.total - l.out, cudaMemcpyDeviceToHost, c->stream));
   rc = check_device_errors(c);
   if (rc) return rc;
@@ -443,7 +443,7 @@ int sigops_ed25519_verify_raw(sigops_ctx* ctx, const uint8_t* sigs, const uint8_
   SG_CUDA(cudaMemcpyAsync(c->d_buf, c->h_buf, o_out, cudaMemcpyHostToDevice, c->stream));
   SG_CUDA(launch_raw_ed(c->d_buf + o_sig, c->d_buf + o_msg, (const uint64_t*)(c->d_buf + o_off), (const uint32_t*)(c->d_buf + o_len),
                         c->d_buf + o_pk, n, c->d_gtab[SIGOPS_ED25519], c->d_buf + o_out, c->d_buf + o_st, c->d_err,
-                        c->grid[SIGOPS_ED25519], c->variant[SIGOPS_ED25519], c->stream));
+                        c->variant[SIGOPS_ED25519], c->stream));
   SG_CUDA(cudaMemcpyAsync(c->h_buf + o_out, c->d_buf + o_out, total - o_out, cudaMemcpyDeviceToHost, c->stream));
   rc = check_device_errors(c);
   if (rc) return rc;
@@ -466,7 +466,7 @@ int sigops_plain_device(sigops_ctx* ctx, int curve, const uint8_t* d_sigs, const
   std::lock_guard<std::mutex> g(c->mu);
   SG_CUDA(cudaSetDevice(c->device));
   cudaStream_t s = stream ? (cudaStream_t)stream : c->stream;
-  SG_CUDA(launch_plain(curve, d_sigs, d_msgs, d_pks, n, c->d_gtab[curve], d_out, d_status, c->d_err, c->grid[curve], c->variant[curve], s));
+  SG_CUDA(launch_plain(curve, d_sigs, d_msgs, d_pks, n, c->d_gtab[curve], d_out, d_status, c->d_err, c->variant[curve], s));
   return SIGOPS_OK;
 }
 
@@ -608,7 +608,7 @@ int sigops_get_variant(sigops_ctx* ctx, int kernel, int* variant, int* grid, int
   if (kernel >= 0 && kernel < 3) {
     if (variant) *variant = c->variant[kernel];
     if (grid) *grid = c->grid[kernel];
-    if (block) *block = PLAIN_BLOCK;
+    if (block) *block = plain_variant_block(c->variant[kernel]);
     return SIGOPS_OK;
   }
   if (kernel == 3) {

@@ -3,72 +3,76 @@
 
 namespace sg {
 
-template <int MINB>
-__global__ void __launch_bounds__(PLAIN_BLOCK, MINB) ed_plain_kernel(const uint8_t* __restrict__ sigs, const uint8_t* __restrict__ msgs,
-                                                                const uint8_t* __restrict__ pks, size_t n, const uint32_t* __restrict__ btab,
-                                                                uint8_t* __restrict__ valid, uint8_t* __restrict__ status, uint32_t* err) {
+// one item per thread; blocks past the batch's end return before staging
+template <int BLOCK, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB) ed_plain_kernel(const uint8_t* __restrict__ sigs, const uint8_t* __restrict__ msgs,
+                                                          const uint8_t* __restrict__ pks, size_t n, const uint32_t* __restrict__ btab,
+                                                          uint8_t* __restrict__ valid, uint8_t* __restrict__ status, uint32_t* err) {
+  const size_t first = (size_t)blockIdx.x * BLOCK;
+  if (first >= n) return;
   __shared__ __align__(128) uint32_t tab[ED_GTAB * 24];
   __shared__ __align__(8) uint64_t bar;
   if (!stage_to_smem(tab, btab, sizeof(tab), &bar, err)) return;
-  const size_t stride = (size_t)gridDim.x * blockDim.x;
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-    uint32_t s[16], m[8], p[8];
-    load_words(sigs, i, 16, s);
-    load_words(msgs, i, 8, m);
-    load_words(pks, i, 8, p);
-    uint8_t st = ed25519_verify(s, m, p, tab);
-    valid[i] = st == ST_OK;
-    status[i] = st;
-  }
+  const size_t i = first + threadIdx.x;
+  if (i >= n) return;
+  uint32_t s[16], m[8], p[8];
+  load_words(sigs, i, 16, s);
+  load_words(msgs, i, 8, m);
+  load_words(pks, i, 8, p);
+  uint8_t st = ed25519_verify(s, m, p, tab);
+  valid[i] = st == ST_OK;
+  status[i] = st;
 }
 
 // ed25519 over messages of any length: message i is msgs[offsets[i] ..
 // offsets[i] + lens[i]) (no alignment needed)
-template <int MINB>
-__global__ void __launch_bounds__(PLAIN_BLOCK, MINB) ed_raw_kernel(const uint8_t* __restrict__ sigs, const uint8_t* __restrict__ msgs,
-                                                              const uint64_t* __restrict__ offsets, const uint32_t* __restrict__ lens,
-                                                              const uint8_t* __restrict__ pks, size_t n, const uint32_t* __restrict__ btab,
-                                                              uint8_t* __restrict__ valid, uint8_t* __restrict__ status, uint32_t* err) {
+template <int BLOCK, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB) ed_raw_kernel(const uint8_t* __restrict__ sigs, const uint8_t* __restrict__ msgs,
+                                                        const uint64_t* __restrict__ offsets, const uint32_t* __restrict__ lens,
+                                                        const uint8_t* __restrict__ pks, size_t n, const uint32_t* __restrict__ btab,
+                                                        uint8_t* __restrict__ valid, uint8_t* __restrict__ status, uint32_t* err) {
+  const size_t first = (size_t)blockIdx.x * BLOCK;
+  if (first >= n) return;
   __shared__ __align__(128) uint32_t tab[ED_GTAB * 24];
   __shared__ __align__(8) uint64_t bar;
   if (!stage_to_smem(tab, btab, sizeof(tab), &bar, err)) return;
-  const size_t stride = (size_t)gridDim.x * blockDim.x;
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-    uint32_t s[16], p[8];
-    load_words(sigs, i, 16, s);
-    load_words(pks, i, 8, p);
-    uint8_t st = ed25519_verify_raw(s, msgs + offsets[i], lens[i], p, tab);
-    valid[i] = st == ST_OK;
-    status[i] = st;
-  }
+  const size_t i = first + threadIdx.x;
+  if (i >= n) return;
+  uint32_t s[16], p[8];
+  load_words(sigs, i, 16, s);
+  load_words(pks, i, 8, p);
+  uint8_t st = ed25519_verify_raw(s, msgs + offsets[i], lens[i], p, tab);
+  valid[i] = st == ST_OK;
+  status[i] = st;
 }
 
 cudaError_t launch_raw_ed(const uint8_t* sigs, const uint8_t* msgs, const uint64_t* offsets, const uint32_t* lens, const uint8_t* pks,
-                          size_t n, const uint32_t* btab, uint8_t* valid, uint8_t* status, uint32_t* err, int grid, int variant,
+                          size_t n, const uint32_t* btab, uint8_t* valid, uint8_t* status, uint32_t* err, int variant,
                           cudaStream_t stream) {
   if (n == 0) return cudaSuccess;
-  if (variant == 1)
-    ed_raw_kernel<2><<<grid, PLAIN_BLOCK, 0, stream>>>(sigs, msgs, offsets, lens, pks, n, btab, valid, status, err);
-  else
-    ed_raw_kernel<1><<<grid, PLAIN_BLOCK, 0, stream>>>(sigs, msgs, offsets, lens, pks, n, btab, valid, status, err);
+  const int block = plain_variant_block(variant);
+  const unsigned grid = (unsigned)((n + block - 1) / block);
+  if (variant == 1) ed_raw_kernel<256, 2><<<grid, 256, 0, stream>>>(sigs, msgs, offsets, lens, pks, n, btab, valid, status, err);
+  else if (variant == 2) ed_raw_kernel<128, 3><<<grid, 128, 0, stream>>>(sigs, msgs, offsets, lens, pks, n, btab, valid, status, err);
+  else ed_raw_kernel<256, 1><<<grid, 256, 0, stream>>>(sigs, msgs, offsets, lens, pks, n, btab, valid, status, err);
   return cudaGetLastError();
 }
 
 cudaError_t launch_plain_ed(const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks, size_t n, const uint32_t* btab, uint8_t* valid,
-                            uint8_t* status, uint32_t* err, int grid, int variant, cudaStream_t stream) {
-  if (variant == 1)
-    ed_plain_kernel<2><<<grid, PLAIN_BLOCK, 0, stream>>>(sigs, msgs, pks, n, btab, valid, status, err);
-  else
-    ed_plain_kernel<1><<<grid, PLAIN_BLOCK, 0, stream>>>(sigs, msgs, pks, n, btab, valid, status, err);
+                            uint8_t* status, uint32_t* err, int variant, cudaStream_t stream) {
+  const int block = plain_variant_block(variant);
+  const unsigned grid = (unsigned)((n + block - 1) / block);
+  if (variant == 1) ed_plain_kernel<256, 2><<<grid, 256, 0, stream>>>(sigs, msgs, pks, n, btab, valid, status, err);
+  else if (variant == 2) ed_plain_kernel<128, 3><<<grid, 128, 0, stream>>>(sigs, msgs, pks, n, btab, valid, status, err);
+  else ed_plain_kernel<256, 1><<<grid, 256, 0, stream>>>(sigs, msgs, pks, n, btab, valid, status, err);
   return cudaGetLastError();
 }
 
 int occupancy_plain_ed(int variant) {
   int b = 0;
-  if (variant == 1)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, ed_plain_kernel<2>, PLAIN_BLOCK, 0);
-  else
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, ed_plain_kernel<1>, PLAIN_BLOCK, 0);
+  if (variant == 1) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, ed_plain_kernel<256, 2>, 256, 0);
+  else if (variant == 2) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, ed_plain_kernel<128, 3>, 128, 0);
+  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, ed_plain_kernel<256, 1>, 256, 0);
   return b;
 }
 

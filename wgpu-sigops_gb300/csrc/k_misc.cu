@@ -122,12 +122,12 @@ __global__ void mul_probe_kernel(uint32_t* out, uint32_t iters, uint32_t seed) {
 // launchers
 // ---------------------------------------------------------------------------
 cudaError_t launch_plain(int curve, const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks, size_t n, const uint32_t* gtab,
-                         uint8_t* out, uint8_t* status, uint32_t* err, int grid, int variant, cudaStream_t stream) {
+                         uint8_t* out, uint8_t* status, uint32_t* err, int variant, cudaStream_t stream) {
   if (n == 0) return cudaSuccess;
   switch (curve) {
-    case CURVE_SECP256K1: return launch_plain_k1(sigs, msgs, n, gtab, out, status, err, grid, variant, stream);
-    case CURVE_SECP256R1: return launch_plain_r1(sigs, msgs, n, gtab, out, status, err, grid, variant, stream);
-    case CURVE_ED25519: return launch_plain_ed(sigs, msgs, pks, n, gtab, out, status, err, grid, variant, stream);
+    case CURVE_SECP256K1: return launch_plain_k1(sigs, msgs, n, gtab, out, status, err, variant, stream);
+    case CURVE_SECP256R1: return launch_plain_r1(sigs, msgs, n, gtab, out, status, err, variant, stream);
+    case CURVE_ED25519: return launch_plain_ed(sigs, msgs, pks, n, gtab, out, status, err, variant, stream);
     default: return cudaErrorInvalidValue;
   }
 }

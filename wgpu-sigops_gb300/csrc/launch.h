@@ -8,24 +8,27 @@ struct sigops_ctx;
 
 namespace sg {
 
-constexpr int PLAIN_BLOCK = 256;
+constexpr int PLAIN_BLOCK = 256;  // workload-generation kernels
 
 // error bits reported through the device error word
 enum : uint32_t { DEV_ERR_STAGE_TIMEOUT = 1u, DEV_ERR_MISALIGNED = 2u, DEV_ERR_QUEUE_TIMEOUT = 4u };
 
+// plain kernels: one item per thread, the grid sized to the batch.  Variants:
+// 0 = 256-thread blocks, one per SM (no register cap); 1 = two per SM (128
+// registers); 2 = 128-thread blocks, three per SM (170 registers).
+constexpr int PLAIN_VARIANTS = 3;
+inline int plain_variant_block(int variant) { return variant == 2 ? 128 : 256; }
 cudaError_t launch_plain(int curve, const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks, size_t n, const uint32_t* gtab,
-                         uint8_t* out, uint8_t* status, uint32_t* err, int grid, int variant, cudaStream_t stream);
+                         uint8_t* out, uint8_t* status, uint32_t* err, int variant, cudaStream_t stream);
 int plain_max_blocks_per_sm(int curve, int variant);
-// plain kernel variants: 0 = one 256-thread block per SM, 1 = two (128 registers)
-constexpr int PLAIN_VARIANTS = 2;
 cudaError_t launch_plain_k1(const uint8_t* sigs, const uint8_t* msgs, size_t n, const uint32_t* gtab, uint8_t* out, uint8_t* status,
-                            uint32_t* err, int grid, int variant, cudaStream_t stream);
+                            uint32_t* err, int variant, cudaStream_t stream);
 cudaError_t launch_plain_r1(const uint8_t* sigs, const uint8_t* msgs, size_t n, const uint32_t* gtab, uint8_t* out, uint8_t* status,
-                            uint32_t* err, int grid, int variant, cudaStream_t stream);
+                            uint32_t* err, int variant, cudaStream_t stream);
 cudaError_t launch_plain_ed(const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks, size_t n, const uint32_t* btab, uint8_t* valid,
-                            uint8_t* status, uint32_t* err, int grid, int variant, cudaStream_t stream);
+                            uint8_t* status, uint32_t* err, int variant, cudaStream_t stream);
 cudaError_t launch_raw_ed(const uint8_t* sigs, const uint8_t* msgs, const uint64_t* offsets, const uint32_t* lens, const uint8_t* pks,
-                          size_t n, const uint32_t* btab, uint8_t* valid, uint8_t* status, uint32_t* err, int grid, int variant,
+                          size_t n, const uint32_t* btab, uint8_t* valid, uint8_t* status, uint32_t* err, int variant,
                           cudaStream_t stream);
 int occupancy_plain_k1(int variant);
 int occupancy_plain_r1(int variant);
@@ -54,12 +57,11 @@ struct ForkStreams {
 };
 cudaError_t fork_streams_create(ForkStreams* f);
 void fork_streams_destroy(ForkStreams* f);
-// grid: blocks of the fused kernel, or the cap on each single-curve kernel's
-// grid (which is also bounded by num_sms x its occupancy)
+// grid: blocks of the fused kernel (the single-curve kernels size their grids
+// to the batch: one item per thread)
 cudaError_t launch_batched(const uint8_t* curves, const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks, size_t n, uint8_t* out,
                            uint8_t* status, uint32_t* idx, void* scratch, const uint32_t* gk1, const uint32_t* gr1, const uint32_t* ged,
-                           uint32_t* err, int grid, int variant, int classify_grid, int num_sms, const ForkStreams* fork,
-                           cudaStream_t stream);
+                           uint32_t* err, int grid, int variant, int classify_grid, const ForkStreams* fork, cudaStream_t stream);
 // what the serving loop needs from a context (host.cu)
 struct CtxView {
   int device;
