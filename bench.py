@@ -421,7 +421,7 @@ def main():
         "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
         "data": "synthetic (seeded PCG64 keys/nonces/seeds/messages; signed on the device; 2% tampered on the host)",
         "config": {"workload": WORKLOAD_DESC, "n": n, "mix": {"secp256k1": counts[0], "secp256r1": counts[1], "ed25519": counts[2]},
-                   "requests": int(len(W.requests)), "kernel": ("batched: classify + three single-curve persistent kernels side by side, CUDA graph" if split
+                   "requests": int(len(W.requests)), "kernel": ("batched: classify + three single-curve kernels (one item per thread) side by side, CUDA graph" if split
                               else "batched: classify + fused persistent mixed-curve kernel, CUDA graph"),
                    "l2": "flushed between steps (256 MiB write outside the timed interval)", "grid": info,
                    "parallelism": f"replicas x{dist.world} (weak scaling, no collective)"},
