@@ -207,9 +207,10 @@ void sigops_mixed_plan_destroy(sigops_plan* plan);
 /* Launch-shape variants (the autotuner's search space).  kernel 0..2: the
  * plain kernel of SIGOPS_SECP256K1 / SECP256R1 / ED25519, variant 0 = one
  * 256-thread block per SM, 1 = two (register budget 128); kernel 3: the
- * batched engine, variants 0..3 = the fused mixed-curve kernel at 256 threads
- * x 1 block per SM, 256 x 2, 128 x 4, 64-thread blocks (as many per SM as
- * registers allow); variants 4 + a + 4 b + 16 c (4..67) = three single-curve
+ * batched engine, variants 0..3 = the fused mixed-curve kernel: 0 = persistent,
+ * 256 threads x 1 block per SM; 1 = one 32-item tile per warp, 256 threads;
+ * 2 = one tile per warp, 128 threads x 3 blocks (170 registers); 3 =
+ * persistent, 64-thread blocks; variants 4 + a + 4 b + 16 c (4..67) = three single-curve
  * kernels run side by side on forked streams, secp256k1 at occupancy level a,
  * P-256 at b, ed25519 at c (level 0 = 256 threads x 1 block per SM, 1 = 128
  * threads x 3 blocks, register budget 170; 2 = 256 x 2, budget 128; 3 = 64
@@ -243,9 +244,10 @@ sigops_server* sigops_server_create(sigops_ctx* ctx, int slots, size_t slot_item
 void sigops_server_destroy(sigops_server* server);
 size_t sigops_server_slot_items(sigops_server* server);
 /* Batched-engine launch variant of the server's launches (as sigops_set_variant
- * kernel 3; default 0, the fused kernel at 256 threads); applies from the next
- * launch.  Variants 4..67 run their three curve kernels one after another on
- * the slot's stream.  No counterpart in the reference. */
+ * kernel 3; default 1, the fused kernel with one tile per warp at 256
+ * threads); applies from the next launch.  Variants 4..67 run their three
+ * curve kernels one after another on the slot's stream.  No counterpart in the
+ * reference. */
 int sigops_server_set_variant(sigops_server* server, int variant);
 
 /* Queue one request of n items.  curves: n tags, or NULL with uniform_curve

@@ -214,4 +214,33 @@ __global__ void __launch_bounds__(BLOCK) __maxnreg__(MAXREG) batched_curve_kerne
   curve_body<BLOCK, CURVE>(io, idx, tabs, sc, err);
 }
 
+// Fused kernel, one tile per warp: warp w of the grid takes tile w of the
+// concatenated per-curve tile lists (no loop), so the curve dispatch stays
+// warp-uniform and almost no state is live across the per-item call.
+template <int BLOCK, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB) batched_fused_flat_kernel(MixedIO io, const uint32_t* __restrict__ idx, BatchTables tabs,
+                                                                     Scratch* sc, uint32_t* err) {
+  const uint32_t n1 = sc->count[0], n2 = sc->count[1], n3 = sc->count[2];
+  const uint32_t t1 = (n1 + BATCH_TILE - 1) / BATCH_TILE, t2 = (n2 + BATCH_TILE - 1) / BATCH_TILE, t3 = (n3 + BATCH_TILE - 1) / BATCH_TILE;
+  const uint32_t first_tile = blockIdx.x * (BLOCK / 32);
+  if (first_tile >= t1 + t2 + t3) return;
+  __shared__ __align__(128) uint32_t tk1[2 * ECDSA_GTAB * 16];
+  __shared__ __align__(128) uint32_t tr1[ECDSA_GTAB * 16];
+  __shared__ __align__(128) uint32_t ted[ED_GTAB * 24];
+  __shared__ __align__(8) uint64_t bar;
+  if (!stage_tables<CM_ALL>(tk1, tr1, ted, tabs, &bar, err)) return;
+  const uint32_t tile = first_tile + (threadIdx.x >> 5), lane = threadIdx.x & 31u;
+  uint32_t slot;
+  if (tile < t1) {
+    slot = tile * BATCH_TILE + lane;
+    if (slot < n1) batched_item<0>(io, idx[slot], tk1);
+  } else if (tile < t1 + t2) {
+    slot = (tile - t1) * BATCH_TILE + lane;
+    if (slot < n2) batched_item<1>(io, idx[io.n + slot], tr1);
+  } else if (tile < t1 + t2 + t3) {
+    slot = (tile - t1 - t2) * BATCH_TILE + lane;
+    if (slot < n3) batched_item<2>(io, idx[2 * io.n + slot], ted);
+  }
+}
+
 }  // namespace sg

@@ -1,17 +1,20 @@
-// Batched mixed-curve kernel, variant 2: 128 threads x 4 blocks per SM.
+// Batched mixed-curve kernel, variant 2: the fused kernel at 128 threads x 3 blocks per SM (170 registers), one tile per warp, no loop.
 #include "batched.cuh"
 
 namespace sg {
 
 int batched_occupancy_2() {
   int b = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, batched_kernel<128, 4, CM_ALL>, 128, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, batched_fused_flat_kernel<128, 3>, 128, 0);
   return b;
 }
 
-cudaError_t batched_launch_2(const MixedIO& io, const uint32_t* idx, const BatchTables& t, Scratch* sc, uint32_t* err, int grid,
+// the grid covers every tile of the batch (one per warp): at most n / 32 + 3 tiles
+cudaError_t batched_launch_2(const MixedIO& io, const uint32_t* idx, const BatchTables& t, Scratch* sc, uint32_t* err, int,
                                cudaStream_t stream) {
-  batched_kernel<128, 4, CM_ALL><<<grid, 128, 0, stream>>>(io, idx, t, sc, err);
+  const size_t tiles = (io.n + BATCH_TILE - 1) / BATCH_TILE + 3;
+  const unsigned grid = (unsigned)((tiles + 128 / 32 - 1) / (128 / 32));
+  batched_fused_flat_kernel<128, 3><<<grid, 128, 0, stream>>>(io, idx, t, sc, err);
   return cudaGetLastError();
 }
 

@@ -29,6 +29,8 @@
 namespace {
 
 constexpr size_t kMaxItems = SIGOPS_NOALLOC_MAX_ITEMS;
+// the fused kernel with one 32-item tile per warp (one launch, no side streams)
+constexpr int kVariant = 1;
 constexpr size_t kScratchHead = 256;  // Scratch record, padded to the array's alignment
 constexpr size_t kScratchBytes = kScratchHead + 3 * kMaxItems * sizeof(uint32_t);
 
@@ -82,7 +84,7 @@ int setup(int device, DeviceSetup** out) {
       cudaMemcpyToSymbol(g_noalloc_err, &zero, sizeof zero) != cudaSuccess)
     return SIGOPS_E_CUDA;
   if (cudaDeviceGetAttribute(&d.num_sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return SIGOPS_E_CUDA;
-  int bps = sg::batched_max_blocks_per_sm(0);
+  int bps = sg::batched_max_blocks_per_sm(kVariant);
   if (bps <= 0) return SIGOPS_E_CUDA;
   d.grid = d.num_sms * bps;
   d.ready = true;
@@ -109,6 +111,6 @@ extern "C" int sigops_verify_mixed_noalloc(const uint8_t* d_curves, const uint8_
   // the per-curve index lists follow the counters; launch_batched clears the counters
   uint32_t* idx = reinterpret_cast<uint32_t*>(d->scratch + kScratchHead);
   cudaError_t e = sg::launch_batched(d_curves, d_sigs, d_msgs, d_pks, n, d_out, d_status, idx, d->scratch, d->tab[0], d->tab[1], d->tab[2],
-                                     d->err, d->grid, 0, classify_grid, nullptr, (cudaStream_t)stream);
+                                     d->err, d->grid, kVariant, classify_grid, nullptr, (cudaStream_t)stream);
   return e == cudaSuccess ? SIGOPS_OK : SIGOPS_E_CUDA;
 }

@@ -85,8 +85,10 @@ struct sigops_server {
   size_t cap = 0;          // items per slot
   // batched-engine launch variant and its grid cap, packed in one word so the
   // worker reads a consistent pair (variant << 16 | blocks per launch at most).
-  // Default: the fused kernel at 256 threads (64-thread blocks cut saturation
-  // by a third); sigops_server_set_variant changes it between launches.
+  // Default: variant 1, the fused kernel with one tile per warp at 256 threads
+  // (measured: higher saturation and lower p99 than the persistent fused
+  // kernel; the single-curve variants run three kernels in a row per slot and
+  // double the latency); sigops_server_set_variant changes it between launches.
   std::atomic<uint32_t> shape{0};
   size_t queue_bound = 0;  // max queued (not yet launched) items
   Layout lay{};
@@ -250,7 +252,7 @@ sigops_server* sigops_server_create(sigops_ctx* ctx, int nslots, size_t slot_ite
   s->cap = slot_items;
   s->queue_bound = std::max<size_t>(slot_items * 64, budget_items);
   s->lay = layout(slot_items);
-  if (set_shape(s, 0) != SIGOPS_OK) {
+  if (set_shape(s, 1) != SIGOPS_OK) {
     delete s;
     return nullptr;
   }

@@ -21,14 +21,14 @@ _dblp = ctypes.POINTER(ctypes.c_double)
 
 
 class Server:
-    def __init__(self, ctx, slots: int = 8, slot_items: int = 0, hbm_fraction: float = 0.25, variant: int = 0):
+    def __init__(self, ctx, slots: int = 8, slot_items: int = 0, hbm_fraction: float = 0.25, variant: int | None = None):
         self.ctx = ctx
         self.ptr = lib.sigops_server_create(ctx.ptr, slots, slot_items, hbm_fraction)
         if not self.ptr:
             raise RuntimeError("sigops_server_create failed")
         self.slot_items = lib.sigops_server_slot_items(self.ptr)
         self._live = {}
-        if variant:
+        if variant is not None:
             self.set_variant(variant)
 
     def set_variant(self, variant: int):
@@ -136,7 +136,7 @@ def request_stream(regions: dict, rate_rps: float, seconds: float, seed: int, ma
 
 
 def measure(ctx, W, loads=(0.25, 0.5, 0.75, 0.9), seconds: float = 10.0, seed: int = 5001, slots: int = 8,
-            slot_items: int = 0, sat_items: int = 2_000_000, variant: int = 0) -> dict:
+            slot_items: int = 0, sat_items: int = 2_000_000, variant: int | None = None) -> dict:
     """Saturation, then open-loop Poisson load levels; latency percentiles in ms."""
     pool, regions = curve_sorted_pool(W)
     srv = Server(ctx, slots=slots, slot_items=slot_items, variant=variant)
@@ -147,7 +147,7 @@ def measure(ctx, W, loads=(0.25, 0.5, 0.75, 0.9), seconds: float = 10.0, seed: i
         rc, lat, wall, out, st = srv.run_load(pool, offs, cnts, arr)
         check(rc, "saturation run")
         sat = float(cnts.sum()) / wall
-        res = {"saturation_sigs_per_s": sat, "mean_request_items": mean_size, "slot_items": srv.slot_items, "slots": slots, "variant": variant,
+        res = {"saturation_sigs_per_s": sat, "mean_request_items": mean_size, "slot_items": srv.slot_items, "slots": slots, "variant": 1 if variant is None else variant,
                "seconds_per_level": seconds, "levels": []}
         for k, load in enumerate(loads):
             rate = load * sat / mean_size
