@@ -30,9 +30,9 @@ int batched_occupancy_0();
 int batched_occupancy_1();
 int batched_occupancy_2();
 int batched_occupancy_3();
-int batched_occupancy_k1(int minb);
-int batched_occupancy_r1(int minb);
-int batched_occupancy_ed(int minb);
+int batched_occupancy_k1(int level);
+int batched_occupancy_r1(int level);
+int batched_occupancy_ed(int level);
 cudaError_t batched_launch_0(const MixedIO&, const uint32_t*, const BatchTables&, Scratch*, uint32_t*, int, cudaStream_t);
 cudaError_t batched_launch_1(const MixedIO&, const uint32_t*, const BatchTables&, Scratch*, uint32_t*, int, cudaStream_t);
 cudaError_t batched_launch_2(const MixedIO&, const uint32_t*, const BatchTables&, Scratch*, uint32_t*, int, cudaStream_t);
@@ -45,7 +45,7 @@ static const int kFusedBlock[BATCHED_FUSED_VARIANTS] = {256, 256, 128, 64};  // 
 
 // single-curve kernels: occupancy level 0 = 256 threads x 1 block per SM,
 // 1 = 128 x 3, 2 = 256 x 2 (8, 12 and 16 warps per SM), 3 = 64 threads with
-// at most 200 registers (as many blocks as the registers allow: 10-12 warps)
+// at most 200 registers (as many blocks as the registers allow)
 constexpr int kLevels = 4;
 static const int kLevelBlock[kLevels] = {256, 128, 256, 64};
 
