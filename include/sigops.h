@@ -196,9 +196,11 @@ int sigops_verify_mixed_noalloc(const uint8_t* d_curves, const uint8_t* d_sigs, 
 int sigops_reserve(sigops_ctx* ctx, size_t n);
 
 /* A CUDA graph of one batched step over fixed device buffers: the scratch
- * reset, the classify kernel and the persistent kernel, replayed by
- * sigops_mixed_plan_launch.  The plan uses the context's scratch: do not run
- * two plans or mixed calls of one context concurrently. */
+ * reset, the classify kernel and the batched engine's kernels for the
+ * context's launch variant (for the single-curve variants three kernels on
+ * parallel graph branches), replayed by sigops_mixed_plan_launch.  The plan
+ * uses the context's scratch: do not run two plans or mixed calls of one
+ * context concurrently. */
 int sigops_mixed_plan_create(sigops_ctx* ctx, const uint8_t* d_curves, const uint8_t* d_sigs, const uint8_t* d_msgs, const uint8_t* d_pks,
                              size_t n, uint8_t* d_out, uint8_t* d_status, sigops_plan** plan);
 int sigops_mixed_plan_launch(sigops_plan* plan, void* stream);
