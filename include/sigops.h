@@ -318,6 +318,13 @@ int sigops_test_field(sigops_ctx* ctx, int field, int op, const uint8_t* a, cons
 /* SHA-512 of n 96-byte inputs (R || A || M preimages); out n*64 bytes. */
 int sigops_test_sha512(sigops_ctx* ctx, const uint8_t* in, uint8_t* out, size_t n);
 
+/* Exercises the expiry of the kernels' bounded waits without any fault: a
+ * one-block kernel waits, at most max_polls polls (1..65536), on an mbarrier
+ * that nothing arrives on.  Returns SIGOPS_E_TIMEDOUT (the device error word
+ * is read and cleared, and the context stays usable).  No counterpart in the
+ * reference. */
+int sigops_test_wait_expiry(sigops_ctx* ctx, uint32_t max_polls);
+
 #ifdef __cplusplus
 }
 #endif

@@ -78,14 +78,7 @@ __device__ __forceinline__ bool stage_tables(uint32_t* sk1, uint32_t* sr1, uint3
                    "l"(t.ed), "r"(be), "r"(b)
                    : "memory");
   }
-  uint32_t done = 0;
-  for (uint32_t i = 0; i < STAGE_MAX_POLLS && !done; ++i) {
-    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n selp.u32 %0, 1, 0, p;\n}\n"
-                 : "=r"(done)
-                 : "r"(b)
-                 : "memory");
-  }
-  if (!done) {
+  if (!mbar_wait_bounded(b, STAGE_MAX_POLLS)) {
     atomicOr(err, DEV_ERR_STAGE_TIMEOUT);
     return false;
   }

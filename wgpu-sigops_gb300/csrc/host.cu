@@ -717,6 +717,16 @@ int sigops_test_field(sigops_ctx* ctx, int field, int op, const uint8_t* a, cons
   return SIGOPS_OK;
 }
 
+int sigops_test_wait_expiry(sigops_ctx* ctx, uint32_t max_polls) {
+  if (max_polls == 0 || max_polls > (1u << 16)) return fail(SIGOPS_E_INVAL, "max_polls must be in [1, 65536]");
+  sigops_ctx* c = resolve(ctx);
+  if (!c) return SIGOPS_E_NODEV;
+  std::lock_guard<std::mutex> g(c->mu);
+  SG_CUDA(cudaSetDevice(c->device));
+  SG_CUDA(launch_wait_expiry(max_polls, c->d_err, c->stream));
+  return check_device_errors(c);
+}
+
 int sigops_test_sha512(sigops_ctx* ctx, const uint8_t* in, uint8_t* out, size_t n) {
   if (!in || !out) return fail(SIGOPS_E_INVAL, "null buffer");
   if (n == 0) return SIGOPS_OK;

@@ -118,6 +118,19 @@ __global__ void mul_probe_kernel(uint32_t* out, uint32_t iters, uint32_t seed) {
   if (x == 0x9e3779b9u) out[0] = x;  // keeps the chains live
 }
 
+// The bounded wait's expiry path, exercised on purpose without any fault: one
+// mbarrier expects one arrival that nobody makes (a flag nothing sets), every
+// thread waits at most max_polls polls through the same helper as the table
+// staging, and the block reports DEV_ERR_STAGE_TIMEOUT and returns.  No bulk
+// copy is issued, so nothing is in flight when the kernel ends.
+__global__ void wait_expiry_kernel(uint32_t max_polls, uint32_t* err) {
+  __shared__ __align__(8) uint64_t bar;
+  const uint32_t b = smem_addr(&bar);
+  if (threadIdx.x == 0) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b) : "memory");
+  __syncthreads();
+  if (!mbar_wait_bounded(b, max_polls) && threadIdx.x == 0) atomicOr(err, DEV_ERR_STAGE_TIMEOUT);
+}
+
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
@@ -148,6 +161,11 @@ cudaError_t launch_field_test(int field, int op, const void* a, const void* b, v
 
 cudaError_t launch_sha512_test(const void* in, void* out, int n, cudaStream_t stream) {
   sha512_test_kernel<<<(n + 127) / 128, 128, 0, stream>>>((const uint32_t*)in, (uint32_t*)out, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_wait_expiry(uint32_t max_polls, uint32_t* err, cudaStream_t stream) {
+  wait_expiry_kernel<<<1, 32, 0, stream>>>(max_polls, err);
   return cudaGetLastError();
 }
 

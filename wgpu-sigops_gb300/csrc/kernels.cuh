@@ -13,6 +13,21 @@ constexpr uint32_t STAGE_MAX_POLLS = 1u << 22;
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
+// Wait for phase 0 of the mbarrier at shared address `bar`, at most max_polls
+// polls; false when it did not complete.  Every wait in these kernels goes
+// through here, so none can spin forever.
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t max_polls) {
+  uint32_t done = 0;
+  for (uint32_t i = 0; i < max_polls && !done; ++i) {
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(bar)
+        : "memory");
+  }
+  return done != 0;
+}
+
 // Copy `bytes` (multiple of 16, both addresses 16-byte aligned) from global to
 // shared memory with one bulk-copy (TMA) instruction completing on an
 // mbarrier; every thread of the block waits with a bounded poll.  Returns
@@ -31,15 +46,7 @@ __device__ __forceinline__ bool stage_to_smem(void* dst, const void* src, uint32
         "l"(src), "r"(bytes), "r"(b)
         : "memory");
   }
-  uint32_t done = 0;
-  for (uint32_t i = 0; i < STAGE_MAX_POLLS && !done; ++i) {
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(done)
-        : "r"(b)
-        : "memory");
-  }
-  if (!done) {
+  if (!mbar_wait_bounded(b, STAGE_MAX_POLLS)) {
     atomicOr(err, DEV_ERR_STAGE_TIMEOUT);
     return false;
   }

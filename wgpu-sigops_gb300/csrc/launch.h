@@ -80,6 +80,7 @@ bool tune_cache_lookup(int device, int variants[4]);
 cudaError_t launch_field_test(int field, int op, const void* a, const void* b, void* out, int n, cudaStream_t stream);
 cudaError_t launch_sha512_test(const void* in, void* out, int n, cudaStream_t stream);
 cudaError_t launch_imad_probe(uint32_t* out, uint32_t iters, int grid, int block, cudaStream_t stream);
+cudaError_t launch_wait_expiry(uint32_t max_polls, uint32_t* err, cudaStream_t stream);
 cudaError_t launch_mul_probe(int form, uint32_t* out, uint32_t iters, int grid, int block, cudaStream_t stream);
 
 }  // namespace sg

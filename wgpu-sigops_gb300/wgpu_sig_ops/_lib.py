@@ -74,6 +74,7 @@ SIGNATURES = {
     "sigops_sync": (ctypes.c_int, [_vp]),
     "sigops_probe_imad": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_double)]),
     "sigops_probe_mul": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
+    "sigops_test_wait_expiry": (ctypes.c_int, [_vp, ctypes.c_uint32]),
     "sigops_device_info": (ctypes.c_int, [_vp] + [ctypes.POINTER(ctypes.c_int)] * 4),
     "sigops_test_field": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp, _sz]),
     "sigops_test_sha512": (ctypes.c_int, [_vp, _vp, _vp, _sz]),
