@@ -154,8 +154,9 @@ int sigops_plain_device(sigops_ctx* ctx, int curve, const uint8_t* d_sigs, const
 
 /* ----------------------------------------- batched mixed-curve engine */
 
-/* Verify a batch that mixes the three curves in one persistent launch.  No
- * counterpart in the reference, which runs one curve per call with
+/* Verify a batch that mixes the three curves in one call of the batched engine
+ * (classify, then the context's launch variant).  No counterpart in the
+ * reference, which runs one curve per call with
  * power-of-two padding (src/secp256k1_ecdsa.rs:25-44); per-item semantics are
  * those of the per-curve calls above.
  * curves: n tags (SIGOPS_SECP256K1 / SECP256R1 / ED25519); sigs n*64; msgs

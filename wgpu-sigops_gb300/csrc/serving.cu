@@ -6,7 +6,7 @@
 // dispatcher thread keeps K slots in flight, each with its own stream, pinned
 // staging, device buffers and batched-engine scratch.  Whenever a slot is free
 // and requests are waiting, it packs as many queued requests as fit into the
-// slot and launches one batched step (H2D copy, classify, persistent kernel,
+// slot and launches one batched step (H2D copy, classify, the fused kernel,
 // D2H copy) on the slot's stream, so new arrivals join the next launch while
 // earlier launches are still running and their kernels overlap on the device.
 // Completed slots scatter results back to each request's output buffers.
@@ -143,8 +143,9 @@ void pack_and_launch(sigops_server* s, Slot& sl) {
   cudaMemcpyAsync(sl.d + L.pk, sl.h + L.pk, n * 32, cudaMemcpyHostToDevice, sl.stream);
   size_t cg = (n + 255) / 256;
   int classify_grid = (int)std::min(cg, (size_t)s->cv.num_sms * 8);
-  // grid sized to the batch (one item per thread up to a full persistent grid):
-  // a light batch occupies few SMs and launches from other slots run beside it
+  // grid sized to the batch (the persistent variants: one item per thread up
+  // to a full grid; the others size themselves): a light batch occupies few
+  // SMs and launches from other slots run beside it
   const uint32_t shape = s->shape.load(std::memory_order_relaxed);
   const int variant = (int)(shape >> 16), grid_cap = (int)(shape & 0xffffu);
   const int block = sg::batched_variant_block(variant);

@@ -1,4 +1,5 @@
-"""Batched mixed-curve verification (one persistent launch per batch)."""
+"""Batched mixed-curve verification: one call of the batched engine per batch
+(a classify kernel, then the context's launch variant)."""
 
 from __future__ import annotations
 
