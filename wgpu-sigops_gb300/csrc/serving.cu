@@ -137,10 +137,15 @@ void pack_and_launch(sigops_server* s, Slot& sl) {
     off += r->n;
   }
   cudaSetDevice(s->cv.device);
-  cudaMemcpyAsync(sl.d + L.cur, sl.h + L.cur, n, cudaMemcpyHostToDevice, sl.stream);
-  cudaMemcpyAsync(sl.d + L.sig, sl.h + L.sig, n * 64, cudaMemcpyHostToDevice, sl.stream);
-  cudaMemcpyAsync(sl.d + L.msg, sl.h + L.msg, n * 32, cudaMemcpyHostToDevice, sl.stream);
-  cudaMemcpyAsync(sl.d + L.pk, sl.h + L.pk, n * 32, cudaMemcpyHostToDevice, sl.stream);
+  // every call's status is kept: the first failure fails the slot's requests
+  cudaError_t e = cudaSuccess;
+  auto keep = [&e](cudaError_t r) {
+    if (e == cudaSuccess) e = r;
+  };
+  keep(cudaMemcpyAsync(sl.d + L.cur, sl.h + L.cur, n, cudaMemcpyHostToDevice, sl.stream));
+  keep(cudaMemcpyAsync(sl.d + L.sig, sl.h + L.sig, n * 64, cudaMemcpyHostToDevice, sl.stream));
+  keep(cudaMemcpyAsync(sl.d + L.msg, sl.h + L.msg, n * 32, cudaMemcpyHostToDevice, sl.stream));
+  keep(cudaMemcpyAsync(sl.d + L.pk, sl.h + L.pk, n * 32, cudaMemcpyHostToDevice, sl.stream));
   size_t cg = (n + 255) / 256;
   int classify_grid = (int)std::min(cg, (size_t)s->cv.num_sms * 8);
   // grid sized to the batch (the persistent variants: one item per thread up
@@ -150,12 +155,11 @@ void pack_and_launch(sigops_server* s, Slot& sl) {
   const int variant = (int)(shape >> 16), grid_cap = (int)(shape & 0xffffu);
   const int block = sg::batched_variant_block(variant);
   const int grid = (int)std::min<size_t>((size_t)grid_cap, (n + block - 1) / block);
-  cudaError_t e = sg::launch_batched(sl.d + L.cur, sl.d + L.sig, sl.d + L.msg, sl.d + L.pk, n, sl.d + L.out, sl.d + L.st, sl.d_idx,
-                                     sl.d_scratch, s->cv.gtab[0], s->cv.gtab[1], s->cv.gtab[2], s->cv.d_err, grid, variant,
-                                     classify_grid, nullptr, sl.stream);
-  cudaMemcpyAsync(sl.h + L.out, sl.d + L.out, n * 64, cudaMemcpyDeviceToHost, sl.stream);
-  cudaMemcpyAsync(sl.h + L.st, sl.d + L.st, n, cudaMemcpyDeviceToHost, sl.stream);
-  cudaEventRecord(sl.done, sl.stream);
+  keep(sg::launch_batched(sl.d + L.cur, sl.d + L.sig, sl.d + L.msg, sl.d + L.pk, n, sl.d + L.out, sl.d + L.st, sl.d_idx, sl.d_scratch,
+                          s->cv.gtab[0], s->cv.gtab[1], s->cv.gtab[2], s->cv.d_err, grid, variant, classify_grid, nullptr, sl.stream));
+  keep(cudaMemcpyAsync(sl.h + L.out, sl.d + L.out, n * 64, cudaMemcpyDeviceToHost, sl.stream));
+  keep(cudaMemcpyAsync(sl.h + L.st, sl.d + L.st, n, cudaMemcpyDeviceToHost, sl.stream));
+  keep(cudaEventRecord(sl.done, sl.stream));
   if (e != cudaSuccess) {
     for (Request* r : sl.reqs) r->rc = SIGOPS_E_CUDA;
   }
