@@ -63,6 +63,39 @@ SG_HD APoint load_apoint(const uint32_t* t, uint32_t idx) {
   return a;
 }
 
+// The per-signature table of multiples 1..NR of R, built in Jacobian form,
+// made affine in place with one inversion (Montgomery's simultaneous
+// inversion; tab[0] = R is affine already), so that every R-side addition of
+// the doubling chain is a mixed addition (7M + 4S instead of 11M + 5S).  No
+// entry is the point at infinity: R has prime order above NR.
+template <class F, int NR>
+SG_HD void normalize_table(JPoint* tab) {
+  u256 pre[NR];  // pre[k] = Z_1 ... Z_k
+  pre[1] = tab[1].Z;
+#pragma unroll 1
+  for (int k = 2; k < NR; ++k) pre[k] = F::mul(pre[k - 1], tab[k].Z);
+  u256 inv = F::inv(pre[NR - 1]);
+#pragma unroll 1
+  for (int k = NR - 1; k >= 1; --k) {
+    u256 zi = inv;
+    if (k > 1) {
+      zi = F::mul(inv, pre[k - 1]);
+      inv = F::mul(inv, tab[k].Z);
+    }
+    const u256 z2 = F::sqr(zi);
+    tab[k].X = F::mul(tab[k].X, z2);
+    tab[k].Y = F::mul(tab[k].Y, F::mul(z2, zi));
+    tab[k].Z = F::one();
+  }
+}
+
+SG_HD APoint affine_of(const JPoint& p) {
+  APoint a;
+  a.x = p.X;
+  a.y = p.Y;
+  return a;
+}
+
 // u1 * G + u2 * R, signed fixed windows, one shared doubling chain.
 // gtab: multiples 1..ECDSA_GTAB of G, affine, field representation.
 template <class T>
@@ -74,6 +107,7 @@ SG_NOINL JPoint ecdsa_lincomb(const u256 u1, const u256 u2, const APoint R, cons
   tab[1] = W::dbl(tab[0]);
 #pragma unroll 1
   for (int k = 2; k < NR; ++k) tab[k] = W::madd(tab[k - 1], R);
+  normalize_table<typename T::F, NR>(tab);
 
   constexpr int JR = (257 + ECDSA_WR - 1) / ECDSA_WR;  // windows for a 256-bit scalar
   constexpr int JG = (257 + ECDSA_WG - 1) / ECDSA_WG;
@@ -88,9 +122,9 @@ SG_NOINL JPoint ecdsa_lincomb(const u256 u1, const u256 u2, const APoint R, cons
       bool neg;
       uint32_t d = booth_digit(u2, pos / ECDSA_WR, ECDSA_WR, neg);
       if (d) {
-        JPoint e = tab[d - 1];
+        APoint e = affine_of(tab[d - 1]);
         if (neg) e = W::neg(e);
-        acc = W::add(acc, e);
+        acc = W::madd(acc, e);
       }
     }
     if (pos % ECDSA_WG == 0) {
@@ -178,7 +212,8 @@ SG_NOINL JPoint k1_glv_lincomb(const u256 u1, const u256 u2, const APoint R, con
   tab[1] = W::dbl(tab[0]);
 #pragma unroll 1
   for (int k = 2; k < NR; ++k) tab[k] = W::madd(tab[k - 1], R1);
-  // phi(+-R) multiples: (beta X, +-Y, Z); k2's sign relative to k1's
+  normalize_table<F, NR>(tab);
+  // phi(+-R) multiples: (beta x, +-y); k2's sign relative to k1's
   const bool flip2 = neg1 != neg2;
   const u256 beta = K1Glv::BETA();
   u256 a = u1, b = u256_zero();
@@ -198,16 +233,16 @@ SG_NOINL JPoint k1_glv_lincomb(const u256 u1, const u256 u2, const APoint R, con
       bool ng;
       uint32_t d = booth_digit(k1, pos / ECDSA_WR, ECDSA_WR, ng);
       if (d) {
-        JPoint e = tab[d - 1];
+        APoint e = affine_of(tab[d - 1]);
         if (ng) e = W::neg(e);
-        acc = W::add(acc, e);
+        acc = W::madd(acc, e);
       }
       d = booth_digit(k2, pos / ECDSA_WR, ECDSA_WR, ng);
       if (d) {
-        JPoint e = tab[d - 1];
-        e.X = F::mul(e.X, beta);
+        APoint e = affine_of(tab[d - 1]);
+        e.x = F::mul(e.x, beta);
         if (ng != flip2) e = W::neg(e);
-        acc = W::add(acc, e);
+        acc = W::madd(acc, e);
       }
     }
     if (pos % ECDSA_WG == 0) {
