@@ -8,6 +8,8 @@
 // generator table is staged into shared memory with one bulk (TMA) copy per
 // block; each thread then handles one signature.
 #pragma once
+#include <type_traits>
+
 #include "kernels.cuh"
 #include "launch.h"
 
@@ -22,7 +24,10 @@ __global__ void __launch_bounds__(BLOCK, MINB) ecdsa_plain_kernel(const uint8_t*
                                                              uint8_t* __restrict__ status, uint32_t* err) {
   const size_t first = (size_t)blockIdx.x * BLOCK;
   if (first >= n) return;
-  __shared__ __align__(128) uint32_t tab[ECDSA_GTAB * 16];
+  // secp256k1 recovers with the GLV split: its table holds the multiples of G
+  // and of 2^128 G
+  constexpr bool GLV = std::is_same<T, K1Traits>::value;
+  __shared__ __align__(128) uint32_t tab[(GLV ? 2 : 1) * ECDSA_GTAB * 16];
   __shared__ __align__(8) uint64_t bar;
   if (!stage_to_smem(tab, gtab, sizeof(tab), &bar, err)) return;
   const size_t i = first + threadIdx.x;
@@ -30,7 +35,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) ecdsa_plain_kernel(const uint8_t*
   uint32_t s[16], m[8], o[16];
   load_words(sigs, i, 16, s);
   load_words(msgs, i, 8, m);
-  uint8_t st = ecdsa_recover<T>(s, m, tab, o);
+  uint8_t st = ecdsa_recover<T, GLV>(s, m, tab, o);
   store_words(out, i, 16, o);
   status[i] = st;
 }
