@@ -115,7 +115,18 @@ struct FpK1 {
   SG_NOINL static u256 mul(const u256 a, const u256 b) { uint32_t t[16]; mul_wide(t, a, b); return reduce(t); }
   SG_NOINL static u256 sqr(const u256 a) { uint32_t t[16]; sqr_wide(t, a); return reduce(t); }
   SG_HD static u256 add(const u256& a, const u256& b) { return mod_add(a, b, P()); }
-  SG_HD static u256 sub(const u256& a, const u256& b) { return mod_sub(a, b, P()); }
+  // a - b for a, b < p: a borrow adds p = 2^256 - (2^32 + 977), i.e. takes
+  // 2^32 + 977 off the wrapped difference (at least 2^32 + 978): no select
+  SG_HD static u256 sub(const u256& a, const u256& b) {
+    u256 t;
+    const uint32_t bw = u256_sub(t, a, b);
+    t.w[0] = sub_cc(t.w[0], bw ? 977u : 0u);
+    t.w[1] = subc_cc(t.w[1], bw);
+#pragma unroll
+    for (int j = 2; j < 8; ++j) t.w[j] = subc_cc(t.w[j], 0u);
+    (void)subc(0u, 0u);
+    return t;
+  }
   SG_HD static u256 neg(const u256& a) { return mod_neg(a, P()); }
   SG_HD static u256 one() { return u256_small(1); }
   SG_HD static u256 zero() { return u256_zero(); }
@@ -222,7 +233,17 @@ struct FpEd {
   SG_NOINL static u256 mul(const u256 a, const u256 b) { uint32_t t[16]; mul_wide_kara(t, a, b); return reduce(t); }
   SG_NOINL static u256 sqr(const u256 a) { uint32_t t[16]; sqr_wide(t, a); return reduce(t); }
   SG_HD static u256 add(const u256& a, const u256& b) { return mod_add(a, b, P()); }
-  SG_HD static u256 sub(const u256& a, const u256& b) { return mod_sub(a, b, P()); }
+  // a - b for a, b < p: a borrow adds p, i.e. takes 2^255 + 19 off the
+  // wrapped difference (at least 2^255 + 20): no select
+  SG_HD static u256 sub(const u256& a, const u256& b) {
+    u256 t;
+    const uint32_t bw = u256_sub(t, a, b);
+    t.w[0] = sub_cc(t.w[0], bw ? 19u : 0u);
+#pragma unroll
+    for (int j = 1; j < 7; ++j) t.w[j] = subc_cc(t.w[j], 0u);
+    t.w[7] = subc(t.w[7], bw ? 0x80000000u : 0u);
+    return t;
+  }
   SG_HD static u256 neg(const u256& a) { return mod_neg(a, P()); }
   SG_HD static u256 one() { return u256_small(1); }
   SG_HD static u256 zero() { return u256_zero(); }
@@ -471,7 +492,21 @@ struct FpR1 {
   SG_NOINL static u256 mul(const u256 a, const u256 b) { uint32_t t[16]; mul_wide(t, a, b); return reduce(t); }
   SG_NOINL static u256 sqr(const u256 a) { uint32_t t[16]; sqr_wide(t, a); return reduce(t); }
   SG_HD static u256 add(const u256& a, const u256& b) { return mod_add(a, b, P()); }
-  SG_HD static u256 sub(const u256& a, const u256& b) { return mod_sub(a, b, P()); }
+  // a - b for a, b < p: a borrow adds p (masked by the borrow), no select
+  SG_HD static u256 sub(const u256& a, const u256& b) {
+    u256 t;
+    const uint32_t bw = u256_sub(t, a, b);
+    const uint32_t m = 0u - bw;  // all ones on a borrow
+    t.w[0] = add_cc(t.w[0], m);
+    t.w[1] = addc_cc(t.w[1], m);
+    t.w[2] = addc_cc(t.w[2], m);
+    t.w[3] = addc_cc(t.w[3], 0u);
+    t.w[4] = addc_cc(t.w[4], 0u);
+    t.w[5] = addc_cc(t.w[5], 0u);
+    t.w[6] = addc_cc(t.w[6], bw);
+    t.w[7] = addc(t.w[7], m);
+    return t;
+  }
   SG_HD static u256 neg(const u256& a) { return mod_neg(a, P()); }
   SG_HD static u256 one() { return u256_small(1); }
   SG_HD static u256 zero() { return u256_zero(); }
