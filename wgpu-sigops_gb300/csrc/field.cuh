@@ -127,7 +127,7 @@ struct FpK1 {
     (void)subc(0u, 0u);
     return t;
   }
-  SG_HD static u256 neg(const u256& a) { return mod_neg(a, P()); }
+  SG_HD static u256 neg(const u256& a) { return sub(u256_zero(), a); }  // 0 - 0 = 0 without a borrow
   SG_HD static u256 one() { return u256_small(1); }
   SG_HD static u256 zero() { return u256_zero(); }
   SG_HD static u256 from_int(const u256& x) { return reduce_once(x, P()); }  // x < 2^256
@@ -244,7 +244,7 @@ struct FpEd {
     t.w[7] = subc(t.w[7], bw ? 0x80000000u : 0u);
     return t;
   }
-  SG_HD static u256 neg(const u256& a) { return mod_neg(a, P()); }
+  SG_HD static u256 neg(const u256& a) { return sub(u256_zero(), a); }  // 0 - 0 = 0 without a borrow
   SG_HD static u256 one() { return u256_small(1); }
   SG_HD static u256 zero() { return u256_zero(); }
   SG_HD static u256 from_int(const u256& x) { return canon(x); }
@@ -507,7 +507,7 @@ struct FpR1 {
     t.w[7] = addc(t.w[7], m);
     return t;
   }
-  SG_HD static u256 neg(const u256& a) { return mod_neg(a, P()); }
+  SG_HD static u256 neg(const u256& a) { return sub(u256_zero(), a); }  // 0 - 0 = 0 without a borrow
   SG_HD static u256 one() { return u256_small(1); }
   SG_HD static u256 zero() { return u256_zero(); }
   SG_HD static u256 from_int(const u256& x) { return reduce_once(x, P()); }  // x < 2^256
