@@ -63,37 +63,60 @@ SG_HD APoint load_apoint(const uint32_t* t, uint32_t idx) {
   return a;
 }
 
-// The per-signature table of multiples 1..NR of R, built in Jacobian form,
-// made affine in place with one inversion (Montgomery's simultaneous
-// inversion; tab[0] = R is affine already), so that every R-side addition of
-// the doubling chain is a mixed addition (7M + 4S instead of 11M + 5S).  No
-// entry is the point at infinity: R has prime order above NR.
-template <class F, int NR>
-SG_HD void normalize_table(JPoint* tab) {
-  u256 pre[NR];  // pre[k] = Z_1 ... Z_k
-  pre[1] = tab[1].Z;
+// The per-signature table of multiples 1..NR of R, affine, so that every
+// R-side addition of the doubling chain is a mixed addition (7M + 4S instead
+// of 11M + 5S).  Built with co-Z additions (Meloni, "New point addition
+// formulae for ECC applications", WAIFI 2007): 2R comes from the doubling of
+// an affine point that also returns R at 2R's Z (1M + 5S), then
+// (k+1)R = R' + kR with R' kept at kR's Z (4M + 2S, against 7M + 4S for a
+// mixed addition).  Each such step multiplies the common Z by
+// d_k = X(R') - X(kR), so the table is made affine with one inversion of the
+// last Z followed by Z_k^-1 = Z_(k+1)^-1 d_(k+1) down the chain (no prefix
+// products).  No step meets an exceptional case: R has prime order above NR,
+// so kR != +-R for 2 <= k <= NR - 1 and R.y != 0.
+template <class F, bool A_M3, int NR>
+SG_HD void coz_table(const APoint R, APoint* tab) {
+  u256 dz[NR];  // dz[1] = Z(2R); dz[k] = Z(tab[k]) / Z(tab[k-1]) for k >= 2
+  const u256 B = F::sqr(R.x);
+  const u256 E = F::sqr(R.y);
+  const u256 L = F::sqr(E);
+  u256 S = F::sub(F::sub(F::sqr(F::add(R.x, E)), B), L);
+  S = F::add(S, S);                               // 4 x y^2 = X(R') at Z = 2y
+  u256 M = A_M3 ? F::sub(B, F::one()) : B;        // 3 x^2 + a
+  M = F::add(F::add(M, M), M);
+  u256 L8 = F::add(L, L);
+  L8 = F::add(L8, L8);
+  L8 = F::add(L8, L8);                            // 8 y^4 = Y(R') at Z = 2y
+  tab[0] = R;
+  tab[1].x = F::sub(F::sqr(M), F::add(S, S));
+  tab[1].y = F::sub(F::mul(M, F::sub(S, tab[1].x)), L8);
+  dz[1] = F::add(R.y, R.y);
+  u256 px = S, py = L8;
 #pragma unroll 1
-  for (int k = 2; k < NR; ++k) pre[k] = F::mul(pre[k - 1], tab[k].Z);
-  u256 inv = F::inv(pre[NR - 1]);
+  for (int k = 2; k < NR; ++k) {
+    const u256 d = F::sub(px, tab[k - 1].x);
+    const u256 e = F::sub(py, tab[k - 1].y);
+    const u256 C = F::sqr(d);
+    const u256 W1 = F::mul(px, C);
+    const u256 W2 = F::mul(tab[k - 1].x, C);
+    const u256 A1 = F::mul(py, F::sub(W1, W2));
+    tab[k].x = F::sub(F::sub(F::sqr(e), W1), W2);
+    tab[k].y = F::sub(F::mul(e, F::sub(W1, tab[k].x)), A1);
+    dz[k] = d;
+    px = W1;
+    py = A1;
+  }
+  u256 z = dz[1];
+#pragma unroll 1
+  for (int k = 2; k < NR; ++k) z = F::mul(z, dz[k]);
+  u256 inv = F::inv(z);
 #pragma unroll 1
   for (int k = NR - 1; k >= 1; --k) {
-    u256 zi = inv;
-    if (k > 1) {
-      zi = F::mul(inv, pre[k - 1]);
-      inv = F::mul(inv, tab[k].Z);
-    }
-    const u256 z2 = F::sqr(zi);
-    tab[k].X = F::mul(tab[k].X, z2);
-    tab[k].Y = F::mul(tab[k].Y, F::mul(z2, zi));
-    tab[k].Z = F::one();
+    const u256 z2 = F::sqr(inv);
+    tab[k].x = F::mul(tab[k].x, z2);
+    tab[k].y = F::mul(tab[k].y, F::mul(z2, inv));
+    if (k > 1) inv = F::mul(inv, dz[k]);
   }
-}
-
-SG_HD APoint affine_of(const JPoint& p) {
-  APoint a;
-  a.x = p.X;
-  a.y = p.Y;
-  return a;
 }
 
 // u1 * G + u2 * R, signed fixed windows, one shared doubling chain.
@@ -102,12 +125,8 @@ template <class T>
 SG_NOINL JPoint ecdsa_lincomb(const u256 u1, const u256 u2, const APoint R, const uint32_t* gtab) {
   using W = Weier<typename T::F, T::A_M3>;
   constexpr int NR = 1 << (ECDSA_WR - 1);
-  JPoint tab[NR];
-  tab[0] = W::from_affine(R);
-  tab[1] = W::dbl(tab[0]);
-#pragma unroll 1
-  for (int k = 2; k < NR; ++k) tab[k] = W::madd(tab[k - 1], R);
-  normalize_table<typename T::F, NR>(tab);
+  APoint tab[NR];
+  coz_table<typename T::F, T::A_M3, NR>(R, tab);
 
   constexpr int JR = (257 + ECDSA_WR - 1) / ECDSA_WR;  // windows for a 256-bit scalar
   constexpr int JG = (257 + ECDSA_WG - 1) / ECDSA_WG;
@@ -122,7 +141,7 @@ SG_NOINL JPoint ecdsa_lincomb(const u256 u1, const u256 u2, const APoint R, cons
       bool neg;
       uint32_t d = booth_digit(u2, pos / ECDSA_WR, ECDSA_WR, neg);
       if (d) {
-        APoint e = affine_of(tab[d - 1]);
+        APoint e = tab[d - 1];
         if (neg) e = W::neg(e);
         acc = W::madd(acc, e);
       }
@@ -207,12 +226,8 @@ SG_NOINL JPoint k1_glv_lincomb(const u256 u1, const u256 u2, const APoint R, con
   bool neg1, neg2;
   K1Glv::split(u2, k1, neg1, k2, neg2);
   APoint R1 = neg1 ? W::neg(R) : R;
-  JPoint tab[NR];
-  tab[0] = W::from_affine(R1);
-  tab[1] = W::dbl(tab[0]);
-#pragma unroll 1
-  for (int k = 2; k < NR; ++k) tab[k] = W::madd(tab[k - 1], R1);
-  normalize_table<F, NR>(tab);
+  APoint tab[NR];
+  coz_table<F, false, NR>(R1, tab);
   // phi(+-R) multiples: (beta x, +-y); k2's sign relative to k1's
   const bool flip2 = neg1 != neg2;
   const u256 beta = K1Glv::BETA();
@@ -233,13 +248,13 @@ SG_NOINL JPoint k1_glv_lincomb(const u256 u1, const u256 u2, const APoint R, con
       bool ng;
       uint32_t d = booth_digit(k1, pos / ECDSA_WR, ECDSA_WR, ng);
       if (d) {
-        APoint e = affine_of(tab[d - 1]);
+        APoint e = tab[d - 1];
         if (ng) e = W::neg(e);
         acc = W::madd(acc, e);
       }
       d = booth_digit(k2, pos / ECDSA_WR, ECDSA_WR, ng);
       if (d) {
-        APoint e = affine_of(tab[d - 1]);
+        APoint e = tab[d - 1];
         e.x = F::mul(e.x, beta);
         if (ng != flip2) e = W::neg(e);
         acc = W::madd(acc, e);
