@@ -179,16 +179,15 @@ int sigops_verify_mixed_device(sigops_ctx* ctx, const uint8_t* d_curves, const u
  * device synchronisation.  It needs no context and calls no cudaMalloc or
  * cudaFree: its scratch (counters and per-curve index lists), the generator
  * tables and its error word are file-scope static device arrays, which every
- * GPU that loads the library holds until the process exits (about 0.8 MiB).
+ * GPU that loads the library holds until the process exits (about 10 MiB,
+ * mostly the generator tables).
  * Limit: n <= SIGOPS_NOALLOC_MAX_ITEMS, else SIGOPS_E_RANGE.  Buffers and
  * results as sigops_verify_mixed_device: device pointers (16-byte aligned)
  * on the current device, work queued on `stream`, no host synchronisation.
  * The first call on each device does a one-time set-up (symbol addresses,
  * table upload): make that first call before any stream capture.  Every call
  * shares the static scratch and clears the counters it uses, so calls whose
- * work overlaps on the GPU race: serialise them.  If the kernel cannot stage
- * its tables it returns without writing; pre-fill d_status with 0xFF to
- * detect that. */
+ * work overlaps on the GPU race: serialise them. */
 #define SIGOPS_NOALLOC_MAX_ITEMS 65536
 int sigops_verify_mixed_noalloc(const uint8_t* d_curves, const uint8_t* d_sigs, const uint8_t* d_msgs, const uint8_t* d_pks, size_t n,
                                 uint8_t* d_out, uint8_t* d_status, void* stream);

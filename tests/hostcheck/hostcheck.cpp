@@ -7,15 +7,13 @@
 
 using namespace sg;
 
-static uint32_t g_k1[2 * ECDSA_GTAB * 16], g_r1[ECDSA_GTAB * 16], g_ed[ED_GTAB * 24];
-static bool g_init = false;
+static const uint32_t *g_k1, *g_r1, *g_ed;
 
 static void init() {
-  if (g_init) return;
-  build_k1_glv_gtab(g_k1);
-  build_weier_gtab<R1Traits>(r1_gx(), r1_gy(), g_r1);
-  build_ed_btab(g_ed);
-  g_init = true;
+  const KernelTables& t = kernel_tables();
+  g_k1 = t.tab[CURVE_SECP256K1].data();
+  g_r1 = t.tab[CURVE_SECP256R1].data();
+  g_ed = t.tab[CURVE_ED25519].data();
 }
 
 static u256 load_le(const uint8_t* b) { u256 r; memcpy(r.w, b, 32); return r; }
@@ -30,9 +28,9 @@ int hc_gtab_entries(int ed) { return ed ? ED_GTAB : ECDSA_GTAB; }
 
 void hc_gtab(int curve, uint32_t* out) {
   init();
-  if (curve == 0) memcpy(out, g_k1, sizeof g_k1);
-  else if (curve == 1) memcpy(out, g_r1, sizeof g_r1);
-  else memcpy(out, g_ed, sizeof g_ed);
+  if (curve == 0) memcpy(out, g_k1, 2 * ECDSA_GTAB * 16 * 4);
+  else if (curve == 1) memcpy(out, g_r1, ECDSA_GTAB * 16 * 4);
+  else memcpy(out, g_ed, ED_GTAB * 24 * 4);
 }
 
 // field op test: field 0 k1-p, 1 r1-p, 2 ed-p, 3 k1-n, 4 r1-n, 5 ed-l ; op 0 mul, 1 add, 2 sub, 3 inv, 4 sqrt_candidate/pow_p58

@@ -189,21 +189,21 @@ def test_kernel_tables(hc):
     """The device tables hold (i+1)*G for every entry (affine integers); the
     secp256k1 table continues with (i+1)*2^128*G (GLV)."""
     ne, ned = hc.hc_gtab_entries(0), hc.hc_gtab_entries(1)
-    assert ne == ned == 128  # generator windows of 8 bits
+    assert ne == ned == 1 << 15  # generator windows of 16 bits
     for curve, c, halves in ((0, o.SECP256K1, 2), (1, o.SECP256R1, 1)):
         buf = (ctypes.c_uint32 * (halves * ne * 16))()
         hc.hc_gtab(curve, buf)
-        words = list(buf)
+        words = buf
         for h in range(halves):
-            for i in (0, 1, 15, 63, ne - 1):
+            for i in (0, 1, 15, 255, 256, 4097, ne - 2, ne - 1):
                 e = h * ne + i
                 x = sum(words[e * 16 + k] << (32 * k) for k in range(8))
                 y = sum(words[e * 16 + 8 + k] << (32 * k) for k in range(8))
                 assert (x, y) == o.ws_mul(c, (i + 1) << (128 * h), c.g), (curve, h, i)
     buf = (ctypes.c_uint32 * (ned * 24))()
     hc.hc_gtab(2, buf)
-    words = list(buf)
-    for i in (0, 7, 63, ned - 1):
+    words = buf
+    for i in (0, 7, 255, 256, 9999, ned - 1):
         x, y = o.ed_mul(i + 1, o.ED_B)
         ypx = sum(words[i * 24 + k] << (32 * k) for k in range(8))
         ymx = sum(words[i * 24 + 8 + k] << (32 * k) for k in range(8))

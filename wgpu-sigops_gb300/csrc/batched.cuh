@@ -15,8 +15,8 @@
 //      by side on forked streams.  With no loop state live across the
 //      signature arithmetic, the 168-register budget (12 warps per SM) fits
 //      secp256k1 recovery with small spills.
-// The generator tables a block needs are staged into shared memory by bulk
-// (TMA) copies completing on one mbarrier.
+// Generator-table entries are read from global memory (L2-resident) as the
+// windows need them.
 // Scratch (global memory beyond inputs and outputs): Scratch below.
 #pragma once
 #include "kernels.cuh"
@@ -24,7 +24,6 @@
 namespace sg {
 
 constexpr int BATCH_TILE = 32;  // items per warp work unit
-constexpr uint32_t QUEUE_MAX_SPINS = 1u << 20;
 
 // curve masks of batched_kernel
 constexpr int CM_K1 = 1, CM_R1 = 2, CM_ED = 4, CM_ALL = 7;
@@ -52,39 +51,6 @@ struct BatchTables {
   const uint32_t* ed;
 };
 
-// the tables a launch needs into shared memory, bulk copies on one mbarrier
-template <int CM>
-__device__ __forceinline__ bool stage_tables(uint32_t* sk1, uint32_t* sr1, uint32_t* sed, const BatchTables& t, uint64_t* bar, uint32_t* err) {
-  const uint32_t b = smem_addr(bar);
-  constexpr uint32_t bk2 = (CM & CM_K1) ? 2 * ECDSA_GTAB * 64 : 0, bk = (CM & CM_R1) ? ECDSA_GTAB * 64 : 0,
-                     be = (CM & CM_ED) ? ED_GTAB * 96 : 0;
-  if (threadIdx.x == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b) : "memory");
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(bk2 + bk + be) : "memory");
-    if (bk2)
-      asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_addr(sk1)),
-                   "l"(t.k1), "r"(bk2), "r"(b)
-                   : "memory");
-    if (bk)
-      asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_addr(sr1)),
-                   "l"(t.r1), "r"(bk), "r"(b)
-                   : "memory");
-    if (be)
-      asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_addr(sed)),
-                   "l"(t.ed), "r"(be), "r"(b)
-                   : "memory");
-  }
-  if (!mbar_wait_bounded(b, STAGE_MAX_POLLS)) {
-    atomicOr(err, DEV_ERR_STAGE_TIMEOUT);
-    return false;
-  }
-  return true;
-}
-
 // ed25519 item of a batch: out byte 0 = valid, the rest zero
 __device__ __forceinline__ uint8_t ed_item(const MixedIO& io, size_t i, const uint32_t s[16], const uint32_t m[8], const uint32_t* ted,
                                            uint32_t o[16]) {
@@ -97,7 +63,6 @@ __device__ __forceinline__ uint8_t ed_item(const MixedIO& io, size_t i, const ui
   return st;
 }
 
-// one launch's work: tables staged, then tiles until the queue is empty
 // One item: load, verify or recover, store.  Called rather than inlined, so
 // that the tile loop's pointers and counters are saved once per signature
 // instead of staying live (about 20 registers) through its arithmetic.
@@ -117,11 +82,9 @@ __device__ __noinline__ void batched_item(const MixedIO io, size_t i, const uint
 template <int CM>
 __device__ __forceinline__ void batched_body(const MixedIO& io, const uint32_t* __restrict__ idx, const BatchTables& tabs, Scratch* sc,
                                              uint32_t* err) {
-  __shared__ __align__(128) uint32_t tk1[(CM & CM_K1) ? 2 * ECDSA_GTAB * 16 : 4];  // G and 2^128 G multiples (GLV)
-  __shared__ __align__(128) uint32_t tr1[(CM & CM_R1) ? ECDSA_GTAB * 16 : 4];
-  __shared__ __align__(128) uint32_t ted[(CM & CM_ED) ? ED_GTAB * 24 : 4];
-  __shared__ __align__(8) uint64_t bar;
-  if (!stage_tables<CM>(tk1, tr1, ted, tabs, &bar, err)) return;
+  const uint32_t* tk1 = tabs.k1;  // G and 2^128 G multiples (GLV)
+  const uint32_t* tr1 = tabs.r1;
+  const uint32_t* ted = tabs.ed;
 
   const uint32_t n1 = (CM & CM_K1) ? sc->count[0] : 0, n2 = (CM & CM_R1) ? sc->count[1] : 0, n3 = (CM & CM_ED) ? sc->count[2] : 0;
   const uint32_t t1 = (n1 + BATCH_TILE - 1) / BATCH_TILE, t2 = (n2 + BATCH_TILE - 1) / BATCH_TILE, t3 = (n3 + BATCH_TILE - 1) / BATCH_TILE;
@@ -166,7 +129,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) batched_kernel(MixedIO io, const 
 
 
 // Single-curve kernel body: block b serves items [b BLOCK, (b + 1) BLOCK) of
-// curve CURVE's index list; blocks past the list's end return before staging.
+// curve CURVE's index list; blocks past the list's end return at once.
 template <int BLOCK, int CURVE>
 __device__ __forceinline__ void curve_body(const MixedIO& io, const uint32_t* __restrict__ idx, const BatchTables& tabs, Scratch* sc,
                                            uint32_t* err) {
@@ -174,11 +137,9 @@ __device__ __forceinline__ void curve_body(const MixedIO& io, const uint32_t* __
   const uint32_t cnt = sc->count[CURVE];
   const uint32_t first = blockIdx.x * BLOCK;
   if (first >= cnt) return;
-  __shared__ __align__(128) uint32_t tk1[(CM & CM_K1) ? 2 * ECDSA_GTAB * 16 : 4];  // G and 2^128 G multiples (GLV)
-  __shared__ __align__(128) uint32_t tr1[(CM & CM_R1) ? ECDSA_GTAB * 16 : 4];
-  __shared__ __align__(128) uint32_t ted[(CM & CM_ED) ? ED_GTAB * 24 : 4];
-  __shared__ __align__(8) uint64_t bar;
-  if (!stage_tables<CM>(tk1, tr1, ted, tabs, &bar, err)) return;
+  const uint32_t* tk1 = tabs.k1;  // G and 2^128 G multiples (GLV)
+  const uint32_t* tr1 = tabs.r1;
+  const uint32_t* ted = tabs.ed;
   const uint32_t slot = first + threadIdx.x;
   if (slot >= cnt) return;
   const size_t i = idx[(size_t)CURVE * io.n + slot];
@@ -217,11 +178,9 @@ __global__ void __launch_bounds__(BLOCK, MINB) batched_fused_flat_kernel(MixedIO
   const uint32_t t1 = (n1 + BATCH_TILE - 1) / BATCH_TILE, t2 = (n2 + BATCH_TILE - 1) / BATCH_TILE, t3 = (n3 + BATCH_TILE - 1) / BATCH_TILE;
   const uint32_t first_tile = blockIdx.x * (BLOCK / 32);
   if (first_tile >= t1 + t2 + t3) return;
-  __shared__ __align__(128) uint32_t tk1[2 * ECDSA_GTAB * 16];
-  __shared__ __align__(128) uint32_t tr1[ECDSA_GTAB * 16];
-  __shared__ __align__(128) uint32_t ted[ED_GTAB * 24];
-  __shared__ __align__(8) uint64_t bar;
-  if (!stage_tables<CM_ALL>(tk1, tr1, ted, tabs, &bar, err)) return;
+  const uint32_t* tk1 = tabs.k1;  // G and 2^128 G multiples (GLV)
+  const uint32_t* tr1 = tabs.r1;
+  const uint32_t* ted = tabs.ed;
   const uint32_t tile = first_tile + (threadIdx.x >> 5), lane = threadIdx.x & 31u;
   uint32_t slot;
   if (tile < t1) {

@@ -44,21 +44,8 @@ int fail(int code, const char* fmt, ...) {
 
 // host tables (built once per process)
 struct HostTables {
-  std::vector<uint32_t> gtab[3];
   std::map<std::pair<int, uint32_t>, std::vector<uint32_t>> bases;
   std::mutex mu;
-  bool built = false;
-  void build() {
-    std::lock_guard<std::mutex> g(mu);
-    if (built) return;
-    gtab[CURVE_SECP256K1].resize(2 * ECDSA_GTAB * 16);  // G multiples, then 2^128 G multiples (GLV)
-    gtab[CURVE_SECP256R1].resize(ECDSA_GTAB * 16);
-    gtab[CURVE_ED25519].resize(ED_GTAB * 24);
-    build_k1_glv_gtab(gtab[CURVE_SECP256K1].data());
-    build_weier_gtab<R1Traits>(r1_gx(), r1_gy(), gtab[CURVE_SECP256R1].data());
-    build_ed_btab(gtab[CURVE_ED25519].data());
-    built = true;
-  }
   const std::vector<uint32_t>* get_bases(int curve, uint32_t L) {
     std::lock_guard<std::mutex> g(mu);
     auto key = std::make_pair(curve, L);
@@ -194,7 +181,7 @@ int check_device_errors(sigops_ctx* c) {
   if (e) {
     SG_CUDA(cudaMemsetAsync(c->d_err, 0, sizeof(uint32_t), c->stream));
     SG_CUDA(cudaStreamSynchronize(c->stream));
-    if (e & DEV_ERR_STAGE_TIMEOUT) return fail(SIGOPS_E_TIMEDOUT, "device: table staging wait expired (error bits 0x%x)", e);
+    if (e & DEV_ERR_WAIT_TIMEOUT) return fail(SIGOPS_E_TIMEDOUT, "device: bounded wait expired (error bits 0x%x)", e);
     return fail(SIGOPS_E_TIMEDOUT, "device error bits 0x%x", e);
   }
   return SIGOPS_OK;
@@ -299,7 +286,7 @@ sigops_ctx* sigops_create(int device) {
     fail(SIGOPS_E_NODEV, "no CUDA device %d (count %d)", device, ndev);
     return nullptr;
   }
-  host_tables().build();
+  const KernelTables& tabs = kernel_tables();
   sigops_ctx* c = new sigops_ctx();
   c->device = device;
   auto bail = [&](const char* what, cudaError_t e) -> sigops_ctx* {
@@ -313,7 +300,7 @@ sigops_ctx* sigops_create(int device) {
   if ((e = fork_streams_create(&c->fork)) != cudaSuccess) return bail("side streams", e);
   if ((e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device)) != cudaSuccess) return bail("attr", e);
   for (int k = 0; k < 3; ++k) {
-    const auto& t = host_tables().gtab[k];
+    const auto& t = tabs.tab[k];
     if ((e = cudaMalloc(&c->d_gtab[k], t.size() * 4)) != cudaSuccess) return bail("cudaMalloc(table)", e);
     if ((e = cudaMemcpy(c->d_gtab[k], t.data(), t.size() * 4, cudaMemcpyHostToDevice)) != cudaSuccess) return bail("table upload", e);
     if (set_variant(c, k, 0) != SIGOPS_OK) {

@@ -3,23 +3,18 @@
 
 namespace sg {
 
-// one item per thread; blocks past the batch's end return before staging
+// one item per thread
 template <int BLOCK, int MINB>
 __global__ void __launch_bounds__(BLOCK, MINB) ed_plain_kernel(const uint8_t* __restrict__ sigs, const uint8_t* __restrict__ msgs,
                                                           const uint8_t* __restrict__ pks, size_t n, const uint32_t* __restrict__ btab,
                                                           uint8_t* __restrict__ valid, uint8_t* __restrict__ status, uint32_t* err) {
-  const size_t first = (size_t)blockIdx.x * BLOCK;
-  if (first >= n) return;
-  __shared__ __align__(128) uint32_t tab[ED_GTAB * 24];
-  __shared__ __align__(8) uint64_t bar;
-  if (!stage_to_smem(tab, btab, sizeof(tab), &bar, err)) return;
-  const size_t i = first + threadIdx.x;
+  const size_t i = (size_t)blockIdx.x * BLOCK + threadIdx.x;
   if (i >= n) return;
   uint32_t s[16], m[8], p[8];
   load_words(sigs, i, 16, s);
   load_words(msgs, i, 8, m);
   load_words(pks, i, 8, p);
-  uint8_t st = ed25519_verify(s, m, p, tab);
+  uint8_t st = ed25519_verify(s, m, p, btab);
   valid[i] = st == ST_OK;
   status[i] = st;
 }
@@ -31,17 +26,12 @@ __global__ void __launch_bounds__(BLOCK, MINB) ed_raw_kernel(const uint8_t* __re
                                                         const uint64_t* __restrict__ offsets, const uint32_t* __restrict__ lens,
                                                         const uint8_t* __restrict__ pks, size_t n, const uint32_t* __restrict__ btab,
                                                         uint8_t* __restrict__ valid, uint8_t* __restrict__ status, uint32_t* err) {
-  const size_t first = (size_t)blockIdx.x * BLOCK;
-  if (first >= n) return;
-  __shared__ __align__(128) uint32_t tab[ED_GTAB * 24];
-  __shared__ __align__(8) uint64_t bar;
-  if (!stage_to_smem(tab, btab, sizeof(tab), &bar, err)) return;
-  const size_t i = first + threadIdx.x;
+  const size_t i = (size_t)blockIdx.x * BLOCK + threadIdx.x;
   if (i >= n) return;
   uint32_t s[16], p[8];
   load_words(sigs, i, 16, s);
   load_words(pks, i, 8, p);
-  uint8_t st = ed25519_verify_raw(s, msgs + offsets[i], lens[i], p, tab);
+  uint8_t st = ed25519_verify_raw(s, msgs + offsets[i], lens[i], p, btab);
   valid[i] = st == ST_OK;
   status[i] = st;
 }

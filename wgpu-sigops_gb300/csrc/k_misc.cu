@@ -120,15 +120,15 @@ __global__ void mul_probe_kernel(uint32_t* out, uint32_t iters, uint32_t seed) {
 
 // The bounded wait's expiry path, exercised on purpose without any fault: one
 // mbarrier expects one arrival that nobody makes (a flag nothing sets), every
-// thread waits at most max_polls polls through the same helper as the table
-// staging, and the block reports DEV_ERR_STAGE_TIMEOUT and returns.  No bulk
-// copy is issued, so nothing is in flight when the kernel ends.
+// thread waits at most max_polls polls through mbar_wait_bounded, and the
+// block reports DEV_ERR_WAIT_TIMEOUT and returns.  No copy is issued, so
+// nothing is in flight when the kernel ends.
 __global__ void wait_expiry_kernel(uint32_t max_polls, uint32_t* err) {
   __shared__ __align__(8) uint64_t bar;
   const uint32_t b = smem_addr(&bar);
   if (threadIdx.x == 0) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b) : "memory");
   __syncthreads();
-  if (!mbar_wait_bounded(b, max_polls) && threadIdx.x == 0) atomicOr(err, DEV_ERR_STAGE_TIMEOUT);
+  if (!mbar_wait_bounded(b, max_polls) && threadIdx.x == 0) atomicOr(err, DEV_ERR_WAIT_TIMEOUT);
 }
 
 // ---------------------------------------------------------------------------

@@ -9,16 +9,13 @@ __global__ void __launch_bounds__(PLAIN_BLOCK) ecdsa_sign_kernel(const uint8_t* 
                                                                   const uint8_t* __restrict__ msgs, size_t n, const uint32_t* __restrict__ gtab,
                                                                   uint8_t* __restrict__ sigs, uint8_t* __restrict__ pubs, uint8_t* __restrict__ status,
                                                                   uint32_t* err) {
-  __shared__ __align__(128) uint32_t tab[ECDSA_GTAB * 16];
-  __shared__ __align__(8) uint64_t bar;
-  if (!stage_to_smem(tab, gtab, sizeof(tab), &bar, err)) return;
   const size_t stride = (size_t)gridDim.x * blockDim.x;
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
     uint32_t d[8], k[8], m[8], s[16], p[16];
     load_words(secrets, i, 8, d);
     load_words(nonces, i, 8, k);
     load_words(msgs, i, 8, m);
-    uint8_t st = ecdsa_sign<T>(d, k, m, tab, s, p);
+    uint8_t st = ecdsa_sign<T>(d, k, m, gtab, s, p);
     store_words(sigs, i, 16, s);
     store_words(pubs, i, 16, p);
     status[i] = st;
@@ -28,15 +25,12 @@ __global__ void __launch_bounds__(PLAIN_BLOCK) ecdsa_sign_kernel(const uint8_t* 
 __global__ void __launch_bounds__(PLAIN_BLOCK) ed_sign_kernel(const uint8_t* __restrict__ seeds, const uint8_t* __restrict__ msgs, size_t n,
                                                                const uint32_t* __restrict__ btab, uint8_t* __restrict__ sigs,
                                                                uint8_t* __restrict__ pks, uint32_t* err) {
-  __shared__ __align__(128) uint32_t tab[ED_GTAB * 24];
-  __shared__ __align__(8) uint64_t bar;
-  if (!stage_to_smem(tab, btab, sizeof(tab), &bar, err)) return;
   const size_t stride = (size_t)gridDim.x * blockDim.x;
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
     uint32_t sd[8], m[8], s[16], p[8];
     load_words(seeds, i, 8, sd);
     load_words(msgs, i, 8, m);
-    ed25519_sign(sd, m, tab, s, p);
+    ed25519_sign(sd, m, btab, s, p);
     store_words(sigs, i, 16, s);
     store_words(pks, i, 8, p);
   }

@@ -6,16 +6,12 @@
 
 namespace sg {
 
-// Upper bound on mbarrier polls before a kernel gives up on a bulk copy and
-// reports DEV_ERR_STAGE_TIMEOUT (each try_wait also suspends in hardware for a
-// bounded time, so this is seconds at most).
-constexpr uint32_t STAGE_MAX_POLLS = 1u << 22;
-
 __device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
 // Wait for phase 0 of the mbarrier at shared address `bar`, at most max_polls
-// polls; false when it did not complete.  Every wait in these kernels goes
-// through here, so none can spin forever.
+// polls (each try_wait also suspends in hardware for a bounded time); false
+// when it did not complete.  Any device-side wait goes through here, so none
+// can spin forever; the caller sets DEV_ERR_WAIT_TIMEOUT and returns.
 __device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t max_polls) {
   uint32_t done = 0;
   for (uint32_t i = 0; i < max_polls && !done; ++i) {
@@ -26,31 +22,6 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t max_pol
         : "memory");
   }
   return done != 0;
-}
-
-// Copy `bytes` (multiple of 16, both addresses 16-byte aligned) from global to
-// shared memory with one bulk-copy (TMA) instruction completing on an
-// mbarrier; every thread of the block waits with a bounded poll.  Returns
-// false (and sets DEV_ERR_STAGE_TIMEOUT) if the copy did not complete.
-__device__ __forceinline__ bool stage_to_smem(void* dst, const void* src, uint32_t bytes, uint64_t* bar, uint32_t* err) {
-  const uint32_t b = smem_addr(bar);
-  if (threadIdx.x == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b) : "memory");
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(bytes) : "memory");
-    asm volatile(
-        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_addr(dst)),
-        "l"(src), "r"(bytes), "r"(b)
-        : "memory");
-  }
-  if (!mbar_wait_bounded(b, STAGE_MAX_POLLS)) {
-    atomicOr(err, DEV_ERR_STAGE_TIMEOUT);
-    return false;
-  }
-  return true;
 }
 
 __device__ __forceinline__ void load_words(const uint8_t* base, size_t idx, int nwords, uint32_t* w) {

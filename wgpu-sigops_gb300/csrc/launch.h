@@ -11,7 +11,7 @@ namespace sg {
 constexpr int PLAIN_BLOCK = 256;  // workload-generation kernels
 
 // error bits reported through the device error word
-enum : uint32_t { DEV_ERR_STAGE_TIMEOUT = 1u, DEV_ERR_MISALIGNED = 2u, DEV_ERR_QUEUE_TIMEOUT = 4u };
+enum : uint32_t { DEV_ERR_WAIT_TIMEOUT = 1u, DEV_ERR_MISALIGNED = 2u, DEV_ERR_QUEUE_TIMEOUT = 4u };
 
 // plain kernels: one item per thread, the grid sized to the batch.  Variants:
 // 0 = 256-thread blocks, one per SM (no register cap); 1 = two per SM (128

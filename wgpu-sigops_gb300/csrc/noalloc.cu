@@ -69,18 +69,12 @@ int setup(int device, DeviceSetup** out) {
   if (cudaGetSymbolAddress((void**)&d.tab[2], g_noalloc_tab_ed) != cudaSuccess) return SIGOPS_E_CUDA;
   if (cudaGetSymbolAddress((void**)&d.err, g_noalloc_err) != cudaSuccess) return SIGOPS_E_CUDA;
   // generator tables, built on the host with the kernels' own arithmetic
-  static uint32_t h_k1[2 * sg::ECDSA_GTAB * 16], h_r1[sg::ECDSA_GTAB * 16], h_ed[sg::ED_GTAB * 24];
-  static bool built = false;
-  if (!built) {
-    sg::build_k1_glv_gtab(h_k1);
-    sg::build_weier_gtab<sg::R1Traits>(sg::r1_gx(), sg::r1_gy(), h_r1);
-    sg::build_ed_btab(h_ed);
-    built = true;
-  }
+  const sg::KernelTables& h = sg::kernel_tables();
+  static_assert(sizeof g_noalloc_tab_k1 == 2 * sg::ECDSA_GTAB * 16 * 4 && sizeof g_noalloc_tab_ed == sg::ED_GTAB * 24 * 4, "table sizes");
   uint32_t zero = 0;
-  if (cudaMemcpyToSymbol(g_noalloc_tab_k1, h_k1, sizeof h_k1) != cudaSuccess ||
-      cudaMemcpyToSymbol(g_noalloc_tab_r1, h_r1, sizeof h_r1) != cudaSuccess ||
-      cudaMemcpyToSymbol(g_noalloc_tab_ed, h_ed, sizeof h_ed) != cudaSuccess ||
+  if (cudaMemcpyToSymbol(g_noalloc_tab_k1, h.tab[0].data(), sizeof g_noalloc_tab_k1) != cudaSuccess ||
+      cudaMemcpyToSymbol(g_noalloc_tab_r1, h.tab[1].data(), sizeof g_noalloc_tab_r1) != cudaSuccess ||
+      cudaMemcpyToSymbol(g_noalloc_tab_ed, h.tab[2].data(), sizeof g_noalloc_tab_ed) != cudaSuccess ||
       cudaMemcpyToSymbol(g_noalloc_err, &zero, sizeof zero) != cudaSuccess)
     return SIGOPS_E_CUDA;
   if (cudaDeviceGetAttribute(&d.num_sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return SIGOPS_E_CUDA;

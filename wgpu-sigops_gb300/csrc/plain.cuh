@@ -4,9 +4,9 @@
 // secp256r1_recover_main / ed25519_verify_main
 // (src/wgsl/main/secp256k1_ecdsa_main.wgsl:22-82 and siblings) and their
 // multi-stage variants (src/wgsl/main/*_main_{0..5}.wgsl), which split the same
-// work into 5-6 dispatches with intermediates in global memory.  The
-// generator table is staged into shared memory with one bulk (TMA) copy per
-// block; each thread then handles one signature.
+// work into 5-6 dispatches with intermediates in global memory.  Each thread
+// handles one signature; generator-table entries are read from global memory
+// (L2-resident) as the windows need them.
 #pragma once
 #include <type_traits>
 
@@ -15,27 +15,21 @@
 
 namespace sg {
 
-// One item per thread; the grid covers the batch (blocks past its end return
-// before staging).  With no loop state live across the arithmetic the
+// One item per thread; the grid covers the batch.  With no loop state live across the arithmetic the
 // 128 x 3 shape (at most 170 registers, 12 warps per SM) runs without spills.
 template <class T, int BLOCK, int MINB>
 __global__ void __launch_bounds__(BLOCK, MINB) ecdsa_plain_kernel(const uint8_t* __restrict__ sigs, const uint8_t* __restrict__ msgs,
                                                              size_t n, const uint32_t* __restrict__ gtab, uint8_t* __restrict__ out,
                                                              uint8_t* __restrict__ status, uint32_t* err) {
-  const size_t first = (size_t)blockIdx.x * BLOCK;
-  if (first >= n) return;
   // secp256k1 recovers with the GLV split: its table holds the multiples of G
   // and of 2^128 G
   constexpr bool GLV = std::is_same<T, K1Traits>::value;
-  __shared__ __align__(128) uint32_t tab[(GLV ? 2 : 1) * ECDSA_GTAB * 16];
-  __shared__ __align__(8) uint64_t bar;
-  if (!stage_to_smem(tab, gtab, sizeof(tab), &bar, err)) return;
-  const size_t i = first + threadIdx.x;
+  const size_t i = (size_t)blockIdx.x * BLOCK + threadIdx.x;
   if (i >= n) return;
   uint32_t s[16], m[8], o[16];
   load_words(sigs, i, 16, s);
   load_words(msgs, i, 8, m);
-  uint8_t st = ecdsa_recover<T, GLV>(s, m, tab, o);
+  uint8_t st = ecdsa_recover<T, GLV>(s, m, gtab, o);
   store_words(out, i, 16, o);
   status[i] = st;
 }

@@ -1,13 +1,16 @@
 // Generator tables, computed once on the host with the same field and curve
 // code the kernels run.
 //
-//  * kernel tables: multiples 1..128 of the generator (affine; Niels form for
+//  * kernel tables: multiples 1..32768 of the generator (affine; Niels form for
 //    ed25519) in the field representation the kernels use;
 //  * the reference's table_limbs encoding: precompute::*_bases(log_limb_size)
 //    (src/precompute.rs:14-69) = [1G .. 16G], each coordinate as
 //    v * 2^(L * nl) mod p in nl little-endian L-bit limbs (x, y for the
 //    Weierstrass curves, x, y, t = x*y for ed25519).
 #pragma once
+#include <algorithm>
+#include <vector>
+
 #include "recover.cuh"
 
 namespace sg {
@@ -21,44 +24,82 @@ inline u256 r1_gy() { return SG_U256(0x37bf51f5u, 0xcbb64068u, 0x6b315eceu, 0x2b
 inline u256 ed_bx() { return SG_U256(0x8f25d51au, 0xc9562d60u, 0x9525a7b2u, 0x692cc760u, 0xfdd6dc5cu, 0xc0a4e231u, 0xcd6e53feu, 0x216936d3u); }
 inline u256 ed_by() { return SG_U256(0x66666658u, 0x66666666u, 0x66666666u, 0x66666666u, 0x66666666u, 0x66666666u, 0x66666666u, 0x66666666u); }
 
-// (i+1) * G for i < count, affine, in T::F's representation
+// (i+1) * G for i < count, affine, in T::F's representation.  Jacobian
+// multiples by mixed additions, made affine in chunks with one inversion each
+// (Montgomery's simultaneous inversion).
 template <class T>
 inline void weier_multiples(const u256& gx, const u256& gy, int count, APoint* out) {
   using F = typename T::F;
   using W = Weier<F, T::A_M3>;
+  constexpr int CHUNK = 256;
   APoint g;
   g.x = F::from_int(gx);
   g.y = F::from_int(gy);
+  std::vector<JPoint> jp(CHUNK);
+  std::vector<u256> pre(CHUNK);
   JPoint acc = W::from_affine(g);
-  for (int i = 0; i < count; ++i) {
-    out[i] = W::to_affine(acc);
-    acc = W::madd(acc, g);
+  for (int base = 0; base < count; base += CHUNK) {
+    const int m = std::min(CHUNK, count - base);
+    for (int i = 0; i < m; ++i) {
+      jp[i] = acc;
+      acc = W::madd(acc, g);  // (i+1) G is never the point at infinity
+    }
+    pre[0] = jp[0].Z;
+    for (int i = 1; i < m; ++i) pre[i] = F::mul(pre[i - 1], jp[i].Z);
+    u256 inv = F::inv(pre[m - 1]);
+    for (int i = m - 1; i >= 0; --i) {
+      u256 zi = inv;
+      if (i > 0) {
+        zi = F::mul(inv, pre[i - 1]);
+        inv = F::mul(inv, jp[i].Z);
+      }
+      const u256 z2 = F::sqr(zi);
+      out[base + i].x = F::mul(jp[i].X, z2);
+      out[base + i].y = F::mul(jp[i].Y, F::mul(z2, zi));
+    }
   }
 }
 
-// (i+1) * B for i < count, affine (x, y) as integers
+// (i+1) * B for i < count, affine (x, y) as integers; chunked simultaneous
+// inversion as above
 inline void ed_multiples(int count, u256* xs, u256* ys) {
   using F = FpEd;
+  constexpr int CHUNK = 256;
   EPoint b;
   b.X = ed_bx();
   b.Y = ed_by();
   b.Z = F::one();
   b.T = F::mul(b.X, b.Y);
-  ENiels bn = Edw::to_niels(b);
+  const ENiels bn = Edw::to_niels(b);
+  std::vector<EPoint> ep(CHUNK);
+  std::vector<u256> pre(CHUNK);
   EPoint acc = b;
-  for (int i = 0; i < count; ++i) {
-    u256 zi = F::inv(acc.Z);
-    xs[i] = F::mul(acc.X, zi);
-    ys[i] = F::mul(acc.Y, zi);
-    acc = Edw::add(acc, bn);
+  for (int base = 0; base < count; base += CHUNK) {
+    const int m = std::min(CHUNK, count - base);
+    for (int i = 0; i < m; ++i) {
+      ep[i] = acc;
+      acc = Edw::add(acc, bn);
+    }
+    pre[0] = ep[0].Z;
+    for (int i = 1; i < m; ++i) pre[i] = F::mul(pre[i - 1], ep[i].Z);
+    u256 inv = F::inv(pre[m - 1]);
+    for (int i = m - 1; i >= 0; --i) {
+      u256 zi = inv;
+      if (i > 0) {
+        zi = F::mul(inv, pre[i - 1]);
+        inv = F::mul(inv, ep[i].Z);
+      }
+      xs[base + i] = F::mul(ep[i].X, zi);
+      ys[base + i] = F::mul(ep[i].Y, zi);
+    }
   }
 }
 
 // kernel table for the Weierstrass curves: ECDSA_GTAB entries of 16 words (x, y)
 template <class T>
 inline void build_weier_gtab(const u256& gx, const u256& gy, uint32_t* out) {
-  APoint pts[ECDSA_GTAB];
-  weier_multiples<T>(gx, gy, ECDSA_GTAB, pts);
+  std::vector<APoint> pts(ECDSA_GTAB);
+  weier_multiples<T>(gx, gy, ECDSA_GTAB, pts.data());
   for (int i = 0; i < ECDSA_GTAB; ++i)
     for (int k = 0; k < 8; ++k) {
       out[i * 16 + k] = pts[i].x.w[k];
@@ -66,7 +107,7 @@ inline void build_weier_gtab(const u256& gx, const u256& gy, uint32_t* out) {
     }
 }
 
-// secp256k1 GLV table: multiples 1..128 of G, then multiples 1..128 of 2^128 G
+// secp256k1 GLV table: multiples 1..32768 of G, then the same multiples of 2^128 G
 inline void build_k1_glv_gtab(uint32_t* out) {
   using F = FpK1;
   using W = Weier<F, false>;
@@ -82,8 +123,8 @@ inline void build_k1_glv_gtab(uint32_t* out) {
 
 // kernel table for ed25519: ED_GTAB entries of 24 words (y+x, y-x, 2d*x*y)
 inline void build_ed_btab(uint32_t* out) {
-  u256 xs[ED_GTAB], ys[ED_GTAB];
-  ed_multiples(ED_GTAB, xs, ys);
+  std::vector<u256> xs(ED_GTAB), ys(ED_GTAB);
+  ed_multiples(ED_GTAB, xs.data(), ys.data());
   for (int i = 0; i < ED_GTAB; ++i) {
     u256 ypx = FpEd::add(ys[i], xs[i]);
     u256 ymx = FpEd::sub(ys[i], xs[i]);
@@ -94,6 +135,25 @@ inline void build_ed_btab(uint32_t* out) {
       out[i * 24 + 16 + k] = t2d.w[k];
     }
   }
+}
+
+// The kernels' generator tables, built once per process (thread-safe static
+// initialisation): secp256k1 (G and 2^128 G multiples), P-256, ed25519.
+struct KernelTables {
+  std::vector<uint32_t> tab[3];
+};
+inline const KernelTables& kernel_tables() {
+  static const KernelTables t = [] {
+    KernelTables k;
+    k.tab[CURVE_SECP256K1].resize(2 * ECDSA_GTAB * 16);
+    k.tab[CURVE_SECP256R1].resize(ECDSA_GTAB * 16);
+    k.tab[CURVE_ED25519].resize(ED_GTAB * 24);
+    build_k1_glv_gtab(k.tab[CURVE_SECP256K1].data());
+    build_weier_gtab<R1Traits>(r1_gx(), r1_gy(), k.tab[CURVE_SECP256R1].data());
+    build_ed_btab(k.tab[CURVE_ED25519].data());
+    return k;
+  }();
+  return t;
 }
 
 // ---------------------------------------------------------------------------
