@@ -218,8 +218,9 @@ struct Edw {
     return r;
   }
 
-  // p + q, q in projective Niels form: 8M (complete)
-  SG_HD static EPoint add(const EPoint& p, const ENiels& q) {
+  // p + q, q in projective Niels form: 8M (complete); with need_t false T is
+  // left stale (7M), for a result that only a doubling reads
+  SG_HD static EPoint add(const EPoint& p, const ENiels& q, bool need_t = true) {
     u256 A = F::mul(F::sub(p.Y, p.X), q.ymx);
     u256 B = F::mul(F::add(p.Y, p.X), q.ypx);
     u256 C = F::mul(p.T, q.t2d);
@@ -229,13 +230,13 @@ struct Edw {
     EPoint r;
     r.X = F::mul(E, Fv);
     r.Y = F::mul(G, H);
-    r.T = F::mul(E, H);
+    r.T = need_t ? F::mul(E, H) : p.T;
     r.Z = F::mul(Fv, G);
     return r;
   }
 
-  // p + q, q affine Niels: 7M
-  SG_HD static EPoint madd(const EPoint& p, const EAffNiels& q) {
+  // p + q, q affine Niels: 7M (6M with need_t false, as above)
+  SG_HD static EPoint madd(const EPoint& p, const EAffNiels& q, bool need_t = true) {
     u256 A = F::mul(F::sub(p.Y, p.X), q.ymx);
     u256 B = F::mul(F::add(p.Y, p.X), q.ypx);
     u256 C = F::mul(p.T, q.t2d);
@@ -244,7 +245,7 @@ struct Edw {
     EPoint r;
     r.X = F::mul(E, Fv);
     r.Y = F::mul(G, H);
-    r.T = F::mul(E, H);
+    r.T = need_t ? F::mul(E, H) : p.T;
     r.Z = F::mul(Fv, G);
     return r;
   }

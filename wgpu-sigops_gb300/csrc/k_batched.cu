@@ -45,7 +45,7 @@ static const int kFusedBlock[BATCHED_FUSED_VARIANTS] = {256, 256, 128, 64};  // 
 
 // single-curve kernels: occupancy level 0 = 256 threads x 1 block per SM,
 // 1 = 128 x 3, 2 = 256 x 2 (8, 12 and 16 warps per SM), 3 = 64 threads with
-// at most 200 registers (as many blocks as the registers allow)
+// at most 144 registers (14 warps per SM)
 constexpr int kLevels = 4;
 static const int kLevelBlock[kLevels] = {256, 128, 256, 64};
 

@@ -1,6 +1,6 @@
 // Single-curve batched kernels for secp256k1 recovery (GLV), one item per thread, at four
 // occupancy levels: 0 = 256 threads x 1 block per SM (up to 255 registers),
-// 1 = 128 x 3 (170), 2 = 256 x 2 (128), 3 = 64 threads with at most 200
+// 1 = 128 x 3 (170), 2 = 256 x 2 (128), 3 = 64 threads with at most 144
 // registers.  The grid covers the whole batch; blocks past the curve's item
 // count return at once.
 #include "batched.cuh"
@@ -12,7 +12,7 @@ int batched_occupancy_k1(int level) {
   if (level == 0) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, batched_curve_kernel<256, 1, 0>, 256, 0);
   else if (level == 1) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, batched_curve_kernel<128, 3, 0>, 128, 0);
   else if (level == 2) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, batched_curve_kernel<256, 2, 0>, 256, 0);
-  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, batched_curve_kernel_r<64, 200, 0>, 64, 0);
+  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, batched_curve_kernel_r<64, 144, 0>, 64, 0);
   return b;
 }
 
@@ -23,7 +23,7 @@ cudaError_t batched_launch_k1(int level, const MixedIO& io, const uint32_t* idx,
   if (level == 0) batched_curve_kernel<256, 1, 0><<<grid, 256, 0, stream>>>(io, idx, t, sc, err);
   else if (level == 1) batched_curve_kernel<128, 3, 0><<<grid, 128, 0, stream>>>(io, idx, t, sc, err);
   else if (level == 2) batched_curve_kernel<256, 2, 0><<<grid, 256, 0, stream>>>(io, idx, t, sc, err);
-  else batched_curve_kernel_r<64, 200, 0><<<grid, 64, 0, stream>>>(io, idx, t, sc, err);
+  else batched_curve_kernel_r<64, 144, 0><<<grid, 64, 0, stream>>>(io, idx, t, sc, err);
   return cudaGetLastError();
 }
 

@@ -43,7 +43,7 @@ cudaError_t launch_sign_ed(const uint8_t* seeds, const uint8_t* msgs, size_t n, 
 // 3 = persistent, 64 threads); variants 4 + a + 4 b + 16 c (4..67): three
 // single-curve kernels (secp256k1 at occupancy level a, P-256 at b, ed25519
 // at c; level 0 = 256 threads x 1 block per SM, 1 = 128 x 3, 2 = 256 x 2,
-// 3 = 64 threads with at most 200 registers).
+// 3 = 64 threads with at most 144 registers).
 constexpr int BATCHED_FUSED_VARIANTS = 4;
 constexpr int BATCHED_VARIANTS = 68;
 int batched_variant_block(int variant);

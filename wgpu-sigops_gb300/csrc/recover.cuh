@@ -410,7 +410,7 @@ SG_NOINL EPoint ed_lincomb(const u256 s, const u256 k, const EPoint negA, const 
       if (d) {
         ENiels e = tab[d - 1];
         if (neg) e = Edw::neg(e);
-        acc = Edw::add(acc, e);
+        acc = Edw::add(acc, e, pos % ED_WG == 0);  // T only for a generator addition at this position
       }
     }
     if (pos % ED_WG == 0) {
@@ -419,7 +419,7 @@ SG_NOINL EPoint ed_lincomb(const u256 s, const u256 k, const EPoint negA, const 
       if (d) {
         EAffNiels e = load_eniels(btab, d - 1);
         if (neg) e = Edw::neg(e);
-        acc = Edw::madd(acc, e);
+        acc = Edw::madd(acc, e, false);  // a doubling or the compression comes next
       }
     }
   }
