@@ -219,11 +219,11 @@ extern "C" void hc_divstep_inv(const uint8_t* x, const uint8_t* m, uint32_t minv
   S30 M = s30_from_u256(mv), f = M, g = s30_from_u256(xv), d, e;
   for (int i = 0; i < 9; ++i) { d.v[i] = 0; e.v[i] = 0; }
   e.v[0] = 1;
-  int32_t delta = 1;
+  int32_t delta2 = 1;
   int used = -1;
-  for (int it = 0; it < 25; ++it) {
+  for (int it = 0; it < DIVSTEP_BATCHES; ++it) {
     int32_t t[4];
-    delta = divsteps30(delta, (uint32_t)f.v[0] | ((uint32_t)f.v[1] << 30), (uint32_t)g.v[0] | ((uint32_t)g.v[1] << 30), t);
+    delta2 = divsteps30(delta2, (uint32_t)f.v[0] | ((uint32_t)f.v[1] << 30), (uint32_t)g.v[0] | ((uint32_t)g.v[1] << 30), t);
     s30_update_de(d, e, t, M, minv30);
     s30_update_fg(f, g, t);
     bool zero = true;

@@ -7,15 +7,21 @@
 // binary extended Euclid with a data-dependent loop, src/wgsl/ff.wgsl:60-120,
 // which never terminates for 0.)
 //
-// The iteration count is fixed: 25 batches of 30 = 750 divsteps, above the
-// paper's bound floor((49 d + 57) / 17) = 741 for d = 256 (Theorem 11.2, with
-// f odd, f^2 + 4 g^2 <= 5 * 2^(2d)), so every lane of a warp runs the same
-// instruction stream.  Callers check x * inv == 1 and fall back to Fermat,
-// which only a broken bound could trigger.
+// The steps are the "half-delta" divsteps (delta starts at 1/2 instead of 1;
+// the update rules are unchanged), for which 590 steps suffice for inputs
+// below 2^256 (P. Wuille's safegcd bound analysis, as used by libsecp256k1's
+// constant-time modular inverse); the original divsteps need 741 (the paper's
+// floor((49 d + 57) / 17) for d = 256).  The iteration count is fixed at 20
+// batches of 30 = 600 steps, so every lane of a warp runs the same
+// instruction stream.  delta is kept doubled (2 delta, odd) in an int32.
+// Callers check x * inv == 1 and fall back to Fermat, which only a broken
+// bound could trigger.
 #pragma once
 #include "arith.cuh"
 
 namespace sg {
+
+constexpr int DIVSTEP_BATCHES = 20;  // of 30 half-delta divsteps
 
 struct S30 {  // value = sum v[i] 2^(30 i); v[0..7] in [0, 2^30), v[8] signed
   int32_t v[9];
@@ -36,20 +42,21 @@ SG_HD S30 s30_from_u256(const u256& x) {
   return s;
 }
 
-// 30 divsteps on the low 32 bits of f and g (two's complement).  Returns the
-// new delta; t = (u, v, q, r) with u f + v g = f' 2^30, q f + r g = g' 2^30.
-SG_HD int32_t divsteps30(int32_t delta, uint32_t f, uint32_t g, int32_t t[4]) {
+// 30 divsteps on the low 32 bits of f and g (two's complement).  delta2 is
+// 2 delta; returns the new value; t = (u, v, q, r) with u f + v g = f' 2^30,
+// q f + r g = g' 2^30.
+SG_HD int32_t divsteps30(int32_t delta2, uint32_t f, uint32_t g, int32_t t[4]) {
   int32_t u = 1, v = 0, q = 0, r = 1;
 #pragma unroll
   for (int i = 0; i < 30; ++i) {
     const bool odd = (g & 1u) != 0;
-    const bool sw = odd && delta > 0;
+    const bool sw = odd && delta2 > 0;
     // swap case: (f, g) <- (g, -f), (u, v, q, r) <- (q, r, -u, -v), delta <- -delta
     const uint32_t f1 = sw ? g : f;
     const uint32_t g1 = sw ? (0u - f) : g;
     const int32_t u1 = sw ? q : u, v1 = sw ? r : v;
     const int32_t q1 = sw ? -u : q, r1 = sw ? -v : r;
-    delta = sw ? -delta : delta;
+    delta2 = sw ? -delta2 : delta2;
     // odd g: g += f, (q, r) += (u, v)
     const uint32_t g2 = odd ? g1 + f1 : g1;
     const int32_t q2 = odd ? q1 + u1 : q1, r2 = odd ? r1 + v1 : r1;
@@ -59,13 +66,13 @@ SG_HD int32_t divsteps30(int32_t delta, uint32_t f, uint32_t g, int32_t t[4]) {
     v = v1 * 2;
     q = q2;
     r = r2;
-    delta += 1;
+    delta2 += 2;  // delta += 1
   }
   t[0] = u;
   t[1] = v;
   t[2] = q;
   t[3] = r;
-  return delta;
+  return delta2;
 }
 
 // (f, g) <- (u f + v g, q f + r g) / 2^30, exact
@@ -145,11 +152,11 @@ SG_HD u256 divstep_inverse(const u256& x, const u256& Mu, uint32_t minv30) {
     e.v[i] = 0;
   }
   e.v[0] = 1;
-  int32_t delta = 1;
+  int32_t delta2 = 1;  // delta = 1/2
 #pragma unroll 1
-  for (int it = 0; it < 25; ++it) {
+  for (int it = 0; it < DIVSTEP_BATCHES; ++it) {
     int32_t t[4];
-    delta = divsteps30(delta, (uint32_t)f.v[0] | ((uint32_t)f.v[1] << 30), (uint32_t)g.v[0] | ((uint32_t)g.v[1] << 30), t);
+    delta2 = divsteps30(delta2, (uint32_t)f.v[0] | ((uint32_t)f.v[1] << 30), (uint32_t)g.v[0] | ((uint32_t)g.v[1] << 30), t);
     s30_update_de(d, e, t, M, minv30);
     s30_update_fg(f, g, t);
   }
