@@ -90,6 +90,27 @@ def test_ecdsa_random_batch_vs_oracle(w, curve_name):
     assert (status == o.ST_NO_POINT).sum() > 10
 
 
+@pytest.mark.parametrize("curve_name", ["secp256k1", "secp256r1"])
+def test_ecdsa_generator_table_ends(w, curve_name):
+    """u1 windows steered to the generator tables' last entries (digits
+    +-32768, +-32767 in every window and both GLV halves): the plain kernel
+    (drop-in API) and the batched engine against the oracle."""
+    from tests.crafted import crafted_signatures
+
+    c = o.SECP256K1 if curve_name == "secp256k1" else o.SECP256R1
+    cases = crafted_signatures(c)
+    sigs = [s for _, s, _ in cases]
+    msgs = [m for _, _, m in cases]
+    keys, status = getattr(w, curve_name + "_ecdsa").ecrecover_arrays(sigs, msgs, None, L)
+    tag = 0 if curve_name == "secp256k1" else 1
+    out, mstatus = w.batch.verify_mixed([tag] * len(cases), sigs, msgs, [bytes(32)] * len(cases))
+    for i, (name, sig, msg) in enumerate(cases):
+        st, pk = o.ecdsa_recover(c, sig, msg)
+        assert st == o.ST_OK, name
+        assert (status[i], keys[i].tobytes()) == (st, pk), name
+        assert (mstatus[i], bytes(out[i])) == (st, pk), name
+
+
 def test_ed25519_random_batch_vs_oracle(w):
     rng = random.Random(12)
     sigs, msgs, pks = [], [], []

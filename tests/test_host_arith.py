@@ -251,6 +251,21 @@ def test_k1_glv_vs_oracle(hc):
         assert (st, out.raw) == o.ecdsa_recover(c, sig, msg)[0:1] + (o.ecdsa_recover(c, sig, msg)[1] or bytes(64),)
 
 
+def test_generator_table_ends(hc):
+    """Recovery with u1 windows steered to the generator tables' last entries
+    (digits +-32768, +-32767, every window, both GLV halves), host build of
+    the plain and GLV kernels against the oracle."""
+    from tests.crafted import crafted_signatures
+
+    for c, fns in ((o.SECP256K1, (hc.hc_k1_recover, hc.hc_k1_recover_glv)), (o.SECP256R1, (hc.hc_r1_recover,))):
+        for name, sig, msg in crafted_signatures(c):
+            st, pk = o.ecdsa_recover(c, sig, msg)
+            assert st == o.ST_OK, name
+            for fn in fns:
+                out = ctypes.create_string_buffer(64)
+                assert (fn(sig, msg, out), out.raw) == (st, pk), name
+
+
 @pytest.mark.parametrize("name", ["k1p", "k1n", "r1p", "r1n", "edp", "edl"])
 def test_divstep_inverse(hc, name):
     """Bernstein-Yang divstep inverse (20 batches of 30 half-delta divsteps):
