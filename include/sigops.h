@@ -208,15 +208,16 @@ void sigops_mixed_plan_destroy(sigops_plan* plan);
 
 /* Launch-shape variants (the autotuner's search space).  kernel 0..2: the
  * plain kernel of SIGOPS_SECP256K1 / SECP256R1 / ED25519, variant 0 = one
- * 256-thread block per SM, 1 = two (register budget 128); kernel 3: the
- * batched engine, variants 0..3 = the fused mixed-curve kernel: 0 = persistent,
- * 256 threads x 1 block per SM; 1 = one 32-item tile per warp, 256 threads;
- * 2 = one tile per warp, 128 threads x 3 blocks (170 registers); 3 =
- * persistent, 64-thread blocks; variants 4 + a + 4 b + 16 c (4..67) = three single-curve
+ * 256-thread block per SM, 1 = two (register budget 128), 2 = 128 threads x 3
+ * blocks (budget 170); kernel 3: the batched engine, variants 0..3 = the fused
+ * mixed-curve kernel: 0 = persistent, 256 threads x 1 block per SM; 1 = one
+ * 32-item tile per warp, 256 threads; 2 = one tile per warp, 128 threads x 3
+ * blocks (170 registers); 3 = one tile per warp, 256 threads x 2 blocks (128
+ * registers); variants 4 + a + 4 b + 16 c (4..67) = three single-curve
  * kernels run side by side on forked streams, secp256k1 at occupancy level a,
  * P-256 at b, ed25519 at c (level 0 = 256 threads x 1 block per SM, 1 = 128
  * threads x 3 blocks, register budget 170; 2 = 256 x 2, budget 128; 3 = 64
- * threads, at most 200 registers: 5 or more blocks per SM).
+ * threads, at most 144 registers: 7 blocks per SM).
  * sigops_get_variant also reports the grid and block used. */
 int sigops_set_variant(sigops_ctx* ctx, int kernel, int variant);
 int sigops_get_variant(sigops_ctx* ctx, int kernel, int* variant, int* grid, int* block);

@@ -41,7 +41,7 @@ cudaError_t batched_launch_k1(int, const MixedIO&, const uint32_t*, const BatchT
 cudaError_t batched_launch_r1(int, const MixedIO&, const uint32_t*, const BatchTables&, Scratch*, uint32_t*, cudaStream_t);
 cudaError_t batched_launch_ed(int, const MixedIO&, const uint32_t*, const BatchTables&, Scratch*, uint32_t*, cudaStream_t);
 
-static const int kFusedBlock[BATCHED_FUSED_VARIANTS] = {256, 256, 128, 64};  // 1, 2: one tile per warp, no loop
+static const int kFusedBlock[BATCHED_FUSED_VARIANTS] = {256, 256, 128, 256};  // 1, 2, 3: one tile per warp, no loop
 
 // single-curve kernels: occupancy level 0 = 256 threads x 1 block per SM,
 // 1 = 128 x 3, 2 = 256 x 2 (8, 12 and 16 warps per SM), 3 = 64 threads with

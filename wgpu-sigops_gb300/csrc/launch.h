@@ -40,7 +40,7 @@ cudaError_t launch_sign_ed(const uint8_t* seeds, const uint8_t* msgs, size_t n, 
 // batched mixed-curve engine: scratch = Scratch record + 3*n u32 index lists.
 // variants 0..3: the fused kernel (0 = persistent, 256 threads x 1 block/SM;
 // 1 = one tile per warp, 256 threads; 2 = one tile per warp, 128 x 3;
-// 3 = persistent, 64 threads); variants 4 + a + 4 b + 16 c (4..67): three
+// 3 = one tile per warp, 256 x 2); variants 4 + a + 4 b + 16 c (4..67): three
 // single-curve kernels (secp256k1 at occupancy level a, P-256 at b, ed25519
 // at c; level 0 = 256 threads x 1 block per SM, 1 = 128 x 3, 2 = 256 x 2,
 // 3 = 64 threads with at most 144 registers).

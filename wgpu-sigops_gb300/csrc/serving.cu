@@ -50,6 +50,7 @@ struct Request {
 
 struct Slot {
   cudaStream_t stream = nullptr;
+  sg::ForkStreams fork{};  // side streams: the single-curve variants run their three kernels side by side
   cudaEvent_t done = nullptr;
   uint8_t* h = nullptr;  // pinned staging: inputs then outputs
   uint8_t* d = nullptr;  // device buffer, same layout
@@ -86,9 +87,10 @@ struct sigops_server {
   // batched-engine launch variant and its grid cap, packed in one word so the
   // worker reads a consistent pair (variant << 16 | blocks per launch at most).
   // Default: variant 1, the fused kernel with one tile per warp at 256 threads
-  // (measured: higher saturation and lower p99 than the persistent fused
-  // kernel; the single-curve variants run three kernels in a row per slot and
-  // double the latency); sigops_server_set_variant changes it between launches.
+  // (measured: the highest saturation).  The single-curve variants run their
+  // three kernels side by side on the slot's side streams: lower latency at
+  // light load, about 18% less saturation.  sigops_server_set_variant changes
+  // it between launches.
   std::atomic<uint32_t> shape{0};
   size_t queue_bound = 0;  // max queued (not yet launched) items
   Layout lay{};
@@ -156,7 +158,7 @@ void pack_and_launch(sigops_server* s, Slot& sl) {
   const int block = sg::batched_variant_block(variant);
   const int grid = (int)std::min<size_t>((size_t)grid_cap, (n + block - 1) / block);
   keep(sg::launch_batched(sl.d + L.cur, sl.d + L.sig, sl.d + L.msg, sl.d + L.pk, n, sl.d + L.out, sl.d + L.st, sl.d_idx, sl.d_scratch,
-                          s->cv.gtab[0], s->cv.gtab[1], s->cv.gtab[2], s->cv.d_err, grid, variant, classify_grid, nullptr, sl.stream));
+                          s->cv.gtab[0], s->cv.gtab[1], s->cv.gtab[2], s->cv.d_err, grid, variant, classify_grid, &sl.fork, sl.stream));
   keep(cudaMemcpyAsync(sl.h + L.out, sl.d + L.out, n * 64, cudaMemcpyDeviceToHost, sl.stream));
   keep(cudaMemcpyAsync(sl.h + L.st, sl.d + L.st, n, cudaMemcpyDeviceToHost, sl.stream));
   keep(cudaEventRecord(sl.done, sl.stream));
@@ -264,6 +266,7 @@ sigops_server* sigops_server_create(sigops_ctx* ctx, int nslots, size_t slot_ite
   s->slots.resize(nslots);
   for (Slot& sl : s->slots) {
     bool ok = cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking) == cudaSuccess &&
+              sg::fork_streams_create(&sl.fork) == cudaSuccess &&
               cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming) == cudaSuccess &&
               cudaMallocHost(&sl.h, s->lay.total) == cudaSuccess && cudaMalloc(&sl.d, s->lay.total) == cudaSuccess &&
               cudaMalloc(&sl.d_scratch, sg::batched_scratch_bytes()) == cudaSuccess &&
@@ -289,6 +292,7 @@ void sigops_server_destroy(sigops_server* s) {
   for (Slot& sl : s->slots) {
     if (sl.stream) cudaStreamSynchronize(sl.stream);
     if (sl.done) cudaEventDestroy(sl.done);
+    sg::fork_streams_destroy(&sl.fork);
     if (sl.stream) cudaStreamDestroy(sl.stream);
     if (sl.h) cudaFreeHost(sl.h);
     if (sl.d) cudaFree(sl.d);
