@@ -49,7 +49,7 @@ void hc_field(int field, int op, const uint8_t* a, const uint8_t* b, uint8_t* ou
   switch (field) {
     case 0: if (op == 4) r = FpK1::sqrt_candidate(FpK1::from_int(x)); else OPS(FpK1); break;
     case 1: if (op == 4) r = FpR1::to_int(FpR1::sqrt_candidate(FpR1::from_int(x))); else OPS(FpR1); break;
-    case 2: if (op == 4) r = FpEd::pow_p58(FpEd::from_int(x)); else OPS(FpEd); break;
+    case 2: if (op == 4) r = FpEd::canon(FpEd::pow_p58(FpEd::from_int(x))); else OPS(FpEd); break;
     case 3: OPS(ScK1); break;
     case 4: OPS(ScR1); break;
     case 5: OPS(ScEd); break;
@@ -130,6 +130,18 @@ extern "C" void hc_ed_sign(const uint8_t* seed, const uint8_t* msg, uint8_t* sig
   memcpy(sd, seed, 32); memcpy(m, msg, 32);
   ed25519_sign(sd, m, g_ed, s, p);
   memcpy(sig, s, 64); memcpy(pk, p, 32);
+}
+
+// ed25519 field operations on raw (weakly reduced) inputs below 2^256, raw
+// result: op 0 add, 1 sub, 2 mul, 3 sqr, 4 neg
+extern "C" void hc_ed_weak(int op, const uint8_t* a, const uint8_t* b, uint8_t* out) {
+  u256 x = load_le(a), y = load_le(b), r;
+  if (op == 0) r = FpEd::add(x, y);
+  else if (op == 1) r = FpEd::sub(x, y);
+  else if (op == 2) r = FpEd::mul(x, y);
+  else if (op == 3) r = FpEd::sqr(x);
+  else r = FpEd::neg(x);
+  store_le(r, out);
 }
 
 // x < 2^256 into the field's canonical range (from_int); field 0 k1, 1 r1, 2 ed

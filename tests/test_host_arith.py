@@ -251,6 +251,26 @@ def test_k1_glv_vs_oracle(hc):
         assert (st, out.raw) == o.ecdsa_recover(c, sig, msg)[0:1] + (o.ecdsa_recover(c, sig, msg)[1] or bytes(64),)
 
 
+def test_ed25519_weak_reduction(hc):
+    """The ed25519 field keeps values below 2^256 only: add / sub / mul / sqr /
+    neg on inputs anywhere in [0, 2^256), including the double-carry and
+    double-borrow corrections, stay below 2^256 and agree mod p."""
+    p = o.ED_P
+    top = 2**256
+    edge = [0, 1, 18, 19, 37, 38, 39, p - 1, p, p + 1, p + 37, 2**255, top - 1, top - 2, top - 37, top - 38, top - 39, top - 76]
+    rng = random.Random(41)
+    vals = edge + [rng.getrandbits(256) for _ in range(30)]
+    for a in vals:
+        for b in vals:
+            for op, f in ((0, lambda a, b: a + b), (1, lambda a, b: a - b), (2, lambda a, b: a * b), (3, lambda a, b: a * a), (4, lambda a, b: -a)):
+                if op >= 3 and b != vals[0]:
+                    continue
+                out = ctypes.create_string_buffer(32)
+                hc.hc_ed_weak(op, le(a), le(b), out)
+                r = int.from_bytes(out.raw, "little")
+                assert r < top and r % p == f(a, b) % p, (op, hex(a), hex(b))
+
+
 def test_generator_table_ends(hc):
     """Recovery with u1 windows steered to the generator tables' last entries
     (digits +-32768, +-32767, every window, both GLV halves), host build of

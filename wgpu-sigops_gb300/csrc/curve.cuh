@@ -108,7 +108,8 @@ struct Weier {
     return r;
   }
 
-  // p + q with q affine (madd-2007-bl, 7M + 4S), exceptional cases exact
+  // p + q with q affine (madd-2004-hmv, 8M + 3S: one more multiply than
+  // madd-2007-bl but six fewer additions), exceptional cases exact
   SG_HD static JPoint madd(const JPoint& p, const APoint& q) {
     if (is_inf(p)) return from_affine(q);
     u256 Z1Z1 = F::sqr(p.Z);
@@ -120,18 +121,13 @@ struct Weier {
       if (u256_is_zero(rr)) return dbl(from_affine(q));
       return infinity();
     }
-    rr = F::add(rr, rr);
     u256 HH = F::sqr(H);
-    u256 I = F::add(HH, HH);
-    I = F::add(I, I);
-    u256 J = F::mul(H, I);
-    u256 V = F::mul(p.X, I);
+    u256 HHH = F::mul(H, HH);
+    u256 V = F::mul(p.X, HH);
     JPoint r;
-    r.X = F::sub(F::sub(F::sqr(rr), J), F::add(V, V));
-    u256 yj = F::mul(p.Y, J);
-    r.Y = F::sub(F::mul(rr, F::sub(V, r.X)), F::add(yj, yj));
-    u256 zh = F::add(p.Z, H);
-    r.Z = F::sub(F::sub(F::sqr(zh), Z1Z1), HH);
+    r.X = F::sub(F::sub(F::sqr(rr), HHH), F::add(V, V));
+    r.Y = F::sub(F::mul(rr, F::sub(V, r.X)), F::mul(p.Y, HHH));
+    r.Z = F::mul(p.Z, H);
     return r;
   }
 
@@ -265,25 +261,27 @@ struct Edw {
   // (src/wgsl/ed25519_curve.wgsl compress; curve25519-dalek EdwardsPoint::compress)
   SG_HD static u256 compress(const EPoint& p) {
     u256 zi = F::inv(p.Z);
-    u256 x = F::mul(p.X, zi);
-    u256 y = F::mul(p.Y, zi);
+    u256 x = F::canon(F::mul(p.X, zi));
+    u256 y = F::canon(F::mul(p.Y, zi));
     y.w[7] |= (x.w[0] & 1u) << 31;
     return y;
   }
 
-  // curve25519-dalek sqrt_ratio_i (src/curve_algos/ed25519_eddsa.rs:160-184)
+  // curve25519-dalek sqrt_ratio_i (src/curve_algos/ed25519_eddsa.rs:160-184);
+  // the comparisons and the sign test use canonical values
   SG_HD static bool sqrt_ratio_i(const u256& u, const u256& v, u256& r_out) {
     u256 v3 = F::mul(F::sqr(v), v);
     u256 v7 = F::mul(F::sqr(v3), v);
     u256 r = F::mul(F::mul(u, v3), F::pow_p58(F::mul(u, v7)));
-    u256 check = F::mul(v, F::sqr(r));
-    u256 nu = F::neg(u);
-    bool correct = u256_eq(check, u);
+    const u256 check = F::canon(F::mul(v, F::sqr(r)));
+    const u256 uc = F::canon(u);
+    const u256 nu = F::canon(F::neg(uc));
+    bool correct = u256_eq(check, uc);
     bool flipped = u256_eq(check, nu);
-    bool flipped_i = u256_eq(check, F::mul(nu, F::SQRT_M1()));
+    bool flipped_i = u256_eq(check, F::canon(F::mul(nu, F::SQRT_M1())));
     u256 ri = F::mul(r, F::SQRT_M1());
-    r = u256_select(flipped || flipped_i, ri, r);
-    r = u256_select((r.w[0] & 1u) != 0, F::neg(r), r);
+    r = F::canon(u256_select(flipped || flipped_i, ri, r));
+    r = u256_select((r.w[0] & 1u) != 0, F::canon(F::neg(r)), r);
     r_out = r;
     return correct || flipped;
   }

@@ -1,5 +1,7 @@
-// Prime fields for the three curves, 8 x 32-bit limbs, values kept canonical
-// (in [0, p)) after every operation.  The base-field multiply and square are
+// Prime fields for the three curves, 8 x 32-bit limbs.  FpK1, FpR1 and the
+// scalar fields keep values canonical (in [0, p)) after every operation; FpEd
+// keeps them below 2^256 only (weakly reduced) and makes them canonical where
+// a comparison or an encoding needs it.  The base-field multiply and square are
 // called functions, not inlined: the hot loops then fit the instruction cache
 // (inlining them everywhere measured 4% slower overall, 19% on ed25519, and
 // took six times longer to compile).
@@ -204,7 +206,7 @@ struct FpEd {
     return u256_select(ge, y, x);
   }
 
-  // t = H * 2^256 + L  ==  L + 38 H  (mod p)
+  // t = H * 2^256 + L  ==  L + 38 H  (mod p), weakly reduced (below 2^256)
   SG_HD static u256 reduce(const uint32_t t[16]) {
     uint32_t v[9];
     v[0] = mad_lo_cc(t[8], 38u, t[0]);
@@ -224,7 +226,7 @@ struct FpEd {
 #pragma unroll
     for (int j = 1; j < 8; ++j) r.w[j] = addc_cc(r.w[j], 0u);
     (void)addc(0u, 0u);
-    return canon(r);
+    return r;
   }
 
   // the ed25519 kernel is bound by the wide/high multiply pipe: its products
@@ -232,23 +234,36 @@ struct FpEd {
   // while the latency-bound secp256k1 / P-256 kernels gain nothing from it)
   SG_NOINL static u256 mul(const u256 a, const u256 b) { uint32_t t[16]; mul_wide_kara(t, a, b); return reduce(t); }
   SG_NOINL static u256 sqr(const u256 a) { uint32_t t[16]; sqr_wide(t, a); return reduce(t); }
-  SG_HD static u256 add(const u256& a, const u256& b) { return mod_add(a, b, P()); }
-  // a - b for a, b < p: a borrow adds p, i.e. takes 2^255 + 19 off the
-  // wrapped difference (at least 2^255 + 20): no select
+  // a + b for a, b < 2^256, weakly reduced: a carry out of 2^256 is worth 38.
+  // Adding it back can carry once more only when the sum left t.w[0] < 38
+  // and the other words zero, so the second correction touches word 0 alone.
+  SG_HD static u256 add(const u256& a, const u256& b) {
+    u256 t;
+    const uint32_t c = u256_add(t, a, b);
+    t.w[0] = add_cc(t.w[0], c * 38u);
+#pragma unroll
+    for (int j = 1; j < 8; ++j) t.w[j] = addc_cc(t.w[j], 0u);
+    const uint32_t c2 = addc(0u, 0u);
+    t.w[0] += c2 * 38u;
+    return t;
+  }
+  // a - b for a, b < 2^256, weakly reduced: a borrow is worth -38; a second
+  // borrow leaves t.w[0] >= 2^32 - 38, so its correction touches word 0 alone
   SG_HD static u256 sub(const u256& a, const u256& b) {
     u256 t;
     const uint32_t bw = u256_sub(t, a, b);
-    t.w[0] = sub_cc(t.w[0], bw ? 19u : 0u);
+    t.w[0] = sub_cc(t.w[0], bw * 38u);
 #pragma unroll
-    for (int j = 1; j < 7; ++j) t.w[j] = subc_cc(t.w[j], 0u);
-    t.w[7] = subc(t.w[7], bw ? 0x80000000u : 0u);
+    for (int j = 1; j < 8; ++j) t.w[j] = subc_cc(t.w[j], 0u);
+    const uint32_t bw2 = subc(0u, 0u) & 1u;
+    t.w[0] -= bw2 * 38u;
     return t;
   }
   SG_HD static u256 neg(const u256& a) { return sub(u256_zero(), a); }  // 0 - 0 = 0 without a borrow
   SG_HD static u256 one() { return u256_small(1); }
   SG_HD static u256 zero() { return u256_zero(); }
   SG_HD static u256 from_int(const u256& x) { return canon(x); }
-  SG_HD static u256 to_int(const u256& a) { return a; }
+  SG_HD static u256 to_int(const u256& a) { return canon(a); }
   SG_HD static u256 D() { return SG_U256(0x135978a3u, 0x75eb4dcau, 0x4141d8abu, 0x00700a4du, 0x7779e898u, 0x8cc74079u, 0x2b6ffe73u, 0x52036ceeu); }
   SG_HD static u256 D2() { return SG_U256(0x26b2f159u, 0xebd69b94u, 0x8283b156u, 0x00e0149au, 0xeef3d130u, 0x198e80f2u, 0x56dffce7u, 0x2406d9dcu); }
   SG_HD static u256 SQRT_M1() { return SG_U256(0x4a0ea0b0u, 0xc4ee1b27u, 0xad2fe478u, 0x2f431806u, 0x3dfbd7a7u, 0x2b4d0099u, 0x4fc1df0bu, 0x2b832480u); }
@@ -274,10 +289,11 @@ struct FpEd {
     z2_250_0 = mul(sqr_n(z2_200_0, 50), z2_50_0);
   }
 
-  // z^-1 by divsteps, verified; Fermat fallback
+  // z^-1 by divsteps (canonical result), verified; Fermat fallback
   SG_NOINL static u256 inv(const u256 z) {
-    u256 r = divstep_inverse(z, P(), 0x179435e5u);
-    return u256_eq(mul(z, r), one()) ? r : inv_fermat(z);
+    const u256 zc = canon(z);
+    u256 r = divstep_inverse(zc, P(), 0x179435e5u);
+    return u256_eq(canon(mul(zc, r)), one()) ? r : canon(inv_fermat(zc));
   }
 
   // z^(p-2) = z^(2^255 - 21)

@@ -85,11 +85,11 @@ SG_HD APoint load_apoint(const uint32_t* t, uint32_t idx) {
 }
 
 // The per-signature table of multiples 1..NR of R, affine, so that every
-// R-side addition of the doubling chain is a mixed addition (7M + 4S instead
+// R-side addition of the doubling chain is a mixed addition (8M + 3S instead
 // of 11M + 5S).  Built with co-Z additions (Meloni, "New point addition
 // formulae for ECC applications", WAIFI 2007): 2R comes from the doubling of
 // an affine point that also returns R at 2R's Z (1M + 5S), then
-// (k+1)R = R' + kR with R' kept at kR's Z (4M + 2S, against 7M + 4S for a
+// (k+1)R = R' + kR with R' kept at kR's Z (4M + 2S, against 8M + 3S for a
 // mixed addition).  Each such step multiplies the common Z by
 // d_k = X(R') - X(kR), so the table is made affine with one inversion of the
 // last Z followed by Z_k^-1 = Z_(k+1)^-1 d_(k+1) down the chain (no prefix

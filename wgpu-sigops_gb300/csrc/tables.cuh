@@ -89,8 +89,8 @@ inline void ed_multiples(int count, u256* xs, u256* ys) {
         zi = F::mul(inv, pre[i - 1]);
         inv = F::mul(inv, ep[i].Z);
       }
-      xs[base + i] = F::mul(ep[i].X, zi);
-      ys[base + i] = F::mul(ep[i].Y, zi);
+      xs[base + i] = F::canon(F::mul(ep[i].X, zi));
+      ys[base + i] = F::canon(F::mul(ep[i].Y, zi));
     }
   }
 }
@@ -126,9 +126,9 @@ inline void build_ed_btab(uint32_t* out) {
   std::vector<u256> xs(ED_GTAB), ys(ED_GTAB);
   ed_multiples(ED_GTAB, xs.data(), ys.data());
   for (int i = 0; i < ED_GTAB; ++i) {
-    u256 ypx = FpEd::add(ys[i], xs[i]);
-    u256 ymx = FpEd::sub(ys[i], xs[i]);
-    u256 t2d = FpEd::mul(FpEd::mul(xs[i], ys[i]), FpEd::D2());
+    u256 ypx = FpEd::canon(FpEd::add(ys[i], xs[i]));
+    u256 ymx = FpEd::canon(FpEd::sub(ys[i], xs[i]));
+    u256 t2d = FpEd::canon(FpEd::mul(FpEd::mul(xs[i], ys[i]), FpEd::D2()));
     for (int k = 0; k < 8; ++k) {
       out[i * 24 + k] = ypx.w[k];
       out[i * 24 + 8 + k] = ymx.w[k];
@@ -230,9 +230,9 @@ inline int build_bases(int curve, uint32_t L, uint32_t* out) {
     u256 rl = pow2_mod(e, FpEd::P());
     for (int i = 0; i < BASES_COUNT; ++i) {
       u256 t = FpEd::mul(xs[i], ys[i]);
-      split_limbs(FpEd::mul(xs[i], rl), L, out + (3 * i) * nl);
-      split_limbs(FpEd::mul(ys[i], rl), L, out + (3 * i + 1) * nl);
-      split_limbs(FpEd::mul(t, rl), L, out + (3 * i + 2) * nl);
+      split_limbs(FpEd::canon(FpEd::mul(xs[i], rl)), L, out + (3 * i) * nl);
+      split_limbs(FpEd::canon(FpEd::mul(ys[i], rl)), L, out + (3 * i + 1) * nl);
+      split_limbs(FpEd::canon(FpEd::mul(t, rl)), L, out + (3 * i + 2) * nl);
     }
     return bases_len(curve, L);
   }
