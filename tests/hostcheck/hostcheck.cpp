@@ -47,7 +47,7 @@ void hc_field(int field, int op, const uint8_t* a, const uint8_t* b, uint8_t* ou
     r = F::to_int(ra);                                                \
   }
   switch (field) {
-    case 0: if (op == 4) r = FpK1::sqrt_candidate(FpK1::from_int(x)); else OPS(FpK1); break;
+    case 0: if (op == 4) r = FpK1::to_int(FpK1::sqrt_candidate(FpK1::from_int(x))); else OPS(FpK1); break;
     case 1: if (op == 4) r = FpR1::to_int(FpR1::sqrt_candidate(FpR1::from_int(x))); else OPS(FpR1); break;
     case 2: if (op == 4) r = FpEd::canon(FpEd::pow_p58(FpEd::from_int(x))); else OPS(FpEd); break;
     case 3: OPS(ScK1); break;
@@ -132,15 +132,21 @@ extern "C" void hc_ed_sign(const uint8_t* seed, const uint8_t* msg, uint8_t* sig
   memcpy(sig, s, 64); memcpy(pk, p, 32);
 }
 
-// ed25519 field operations on raw (weakly reduced) inputs below 2^256, raw
-// result: op 0 add, 1 sub, 2 mul, 3 sqr, 4 neg
-extern "C" void hc_ed_weak(int op, const uint8_t* a, const uint8_t* b, uint8_t* out) {
-  u256 x = load_le(a), y = load_le(b), r;
-  if (op == 0) r = FpEd::add(x, y);
-  else if (op == 1) r = FpEd::sub(x, y);
-  else if (op == 2) r = FpEd::mul(x, y);
-  else if (op == 3) r = FpEd::sqr(x);
-  else r = FpEd::neg(x);
+// weakly reduced field operations (field 0 secp256k1, 2 ed25519) on raw
+// inputs below 2^256, raw result: op 0 add, 1 sub, 2 mul, 3 sqr, 4 neg,
+// 5 is_zero (secp256k1)
+template <class F>
+static u256 weak_op(int op, const u256& x, const u256& y) {
+  if (op == 0) return F::add(x, y);
+  if (op == 1) return F::sub(x, y);
+  if (op == 2) return F::mul(x, y);
+  if (op == 3) return F::sqr(x);
+  return F::neg(x);
+}
+extern "C" void hc_weak(int field, int op, const uint8_t* a, const uint8_t* b, uint8_t* out) {
+  u256 x = load_le(a), y = load_le(b), r = u256_zero();
+  if (field == 0 && op == 5) r.w[0] = FpK1::is_zero(x);
+  else r = field == 0 ? weak_op<FpK1>(op, x, y) : weak_op<FpEd>(op, x, y);
   store_le(r, out);
 }
 

@@ -251,14 +251,26 @@ def test_k1_glv_vs_oracle(hc):
         assert (st, out.raw) == o.ecdsa_recover(c, sig, msg)[0:1] + (o.ecdsa_recover(c, sig, msg)[1] or bytes(64),)
 
 
-def test_ed25519_weak_reduction(hc):
-    """The ed25519 field keeps values below 2^256 only: add / sub / mul / sqr /
-    neg on inputs anywhere in [0, 2^256), including the double-carry and
-    double-borrow corrections, stay below 2^256 and agree mod p."""
-    p = o.ED_P
+@pytest.mark.parametrize("field", [0, 2], ids=["secp256k1", "ed25519"])
+def test_weak_reduction(hc, field):
+    """The secp256k1 and ed25519 fields keep values below 2^256 only: add /
+    sub / mul / sqr / neg on inputs anywhere in [0, 2^256), including the
+    double-carry and double-borrow corrections, stay below 2^256 and agree mod
+    p; is_zero recognises both representations of zero."""
     top = 2**256
-    edge = [0, 1, 18, 19, 37, 38, 39, p - 1, p, p + 1, p + 37, 2**255, top - 1, top - 2, top - 37, top - 38, top - 39, top - 76]
-    rng = random.Random(41)
+    if field == 0:
+        p = o.SECP256K1.p
+        c = top - p  # 2^32 + 977
+        edge = [0, 1, 976, 977, 978, c - 1, c, c + 1, 2 * c, p - 1, p, p + 1, p + c - 1, 2**255, top - 1, top - 2, top - c, top - c - 1,
+                top - c + 1, top - 2 * c, 2**32, 2**64 - 1]
+        for v, z in ((0, 1), (p, 1), (1, 0), (p - 1, 0), (p + 1, 0), (top - 1, 0)):
+            out = ctypes.create_string_buffer(32)
+            hc.hc_weak(0, 5, le(v), le(0), out)
+            assert out.raw[0] == z, hex(v)
+    else:
+        p = o.ED_P
+        edge = [0, 1, 18, 19, 37, 38, 39, p - 1, p, p + 1, p + 37, 2**255, top - 1, top - 2, top - 37, top - 38, top - 39, top - 76]
+    rng = random.Random(41 + field)
     vals = edge + [rng.getrandbits(256) for _ in range(30)]
     for a in vals:
         for b in vals:
@@ -266,7 +278,7 @@ def test_ed25519_weak_reduction(hc):
                 if op >= 3 and b != vals[0]:
                     continue
                 out = ctypes.create_string_buffer(32)
-                hc.hc_ed_weak(op, le(a), le(b), out)
+                hc.hc_weak(field, op, le(a), le(b), out)
                 r = int.from_bytes(out.raw, "little")
                 assert r < top and r % p == f(a, b) % p, (op, hex(a), hex(b))
 

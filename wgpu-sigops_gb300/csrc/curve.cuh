@@ -117,8 +117,8 @@ struct Weier {
     u256 S2 = F::mul(q.y, F::mul(p.Z, Z1Z1));
     u256 H = F::sub(U2, p.X);
     u256 rr = F::sub(S2, p.Y);
-    if (u256_is_zero(H)) {
-      if (u256_is_zero(rr)) return dbl(from_affine(q));
+    if (F::is_zero(H)) {
+      if (F::is_zero(rr)) return dbl(from_affine(q));
       return infinity();
     }
     u256 HH = F::sqr(H);
@@ -143,8 +143,8 @@ struct Weier {
     u256 S2 = F::mul(q.Y, F::mul(p.Z, Z1Z1));
     u256 H = F::sub(U2, U1);
     u256 rr = F::sub(S2, S1);
-    if (u256_is_zero(H)) {
-      if (u256_is_zero(rr)) return dbl(p);
+    if (F::is_zero(H)) {
+      if (F::is_zero(rr)) return dbl(p);
       return infinity();
     }
     rr = F::add(rr, rr);

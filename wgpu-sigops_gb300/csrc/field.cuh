@@ -1,7 +1,7 @@
-// Prime fields for the three curves, 8 x 32-bit limbs.  FpK1, FpR1 and the
-// scalar fields keep values canonical (in [0, p)) after every operation; FpEd
-// keeps them below 2^256 only (weakly reduced) and makes them canonical where
-// a comparison or an encoding needs it.  The base-field multiply and square are
+// Prime fields for the three curves, 8 x 32-bit limbs.  FpR1 and the scalar
+// fields keep values canonical (in [0, p)) after every operation; FpK1 and
+// FpEd keep them below 2^256 only (weakly reduced) and make them canonical
+// (canon) where a comparison or an encoding needs it.  The base-field multiply and square are
 // called functions, not inlined: the hot loops then fit the instruction cache
 // (inlining them everywhere measured 4% slower overall, 19% on ed25519, and
 // took six times longer to compile).
@@ -68,7 +68,8 @@ SG_HD u256 reduce_once(const u256& x, const u256& m) {
 struct FpK1 {
   SG_HD static u256 P() { return SG_U256(0xfffffc2fu, 0xfffffffeu, 0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu); }
 
-  // t = H * 2^256 + L  ==  L + H * 977 + H * 2^32  (mod p)
+  // t = H * 2^256 + L  ==  L + H * 977 + H * 2^32  (mod p), weakly reduced
+  // (below 2^256)
   SG_HD static u256 reduce(const uint32_t t[16]) {
     uint32_t v[10];
     // v = L + lo(H_j * 977) at column j
@@ -111,29 +112,49 @@ struct FpK1 {
 #pragma unroll
     for (int j = 2; j < 8; ++j) r.w[j] = addc_cc(r.w[j], 0u);
     (void)addc(0u, 0u);
-    return reduce_once(r, P());
+    return r;
   }
 
+  SG_HD static u256 canon(const u256& x) { return reduce_once(x, P()); }  // x < 2^256 < 2p
+  SG_HD static bool is_zero(const u256& a) { return u256_is_zero(a) || u256_eq(a, P()); }  // a == 0 mod p
   SG_NOINL static u256 mul(const u256 a, const u256 b) { uint32_t t[16]; mul_wide(t, a, b); return reduce(t); }
   SG_NOINL static u256 sqr(const u256 a) { uint32_t t[16]; sqr_wide(t, a); return reduce(t); }
-  SG_HD static u256 add(const u256& a, const u256& b) { return mod_add(a, b, P()); }
-  // a - b for a, b < p: a borrow adds p = 2^256 - (2^32 + 977), i.e. takes
-  // 2^32 + 977 off the wrapped difference (at least 2^32 + 978): no select
+  // a + b for a, b < 2^256, weakly reduced: a carry out of 2^256 is worth
+  // 2^32 + 977.  Adding it back carries again only when the sum left words
+  // 2..7 zero and word 1 at most 1, so the second correction touches words 0
+  // and 1 alone.
+  SG_HD static u256 add(const u256& a, const u256& b) {
+    u256 t;
+    const uint32_t c = u256_add(t, a, b);
+    t.w[0] = add_cc(t.w[0], c * 977u);
+    t.w[1] = addc_cc(t.w[1], c);
+#pragma unroll
+    for (int j = 2; j < 8; ++j) t.w[j] = addc_cc(t.w[j], 0u);
+    const uint32_t c2 = addc(0u, 0u);
+    t.w[0] = add_cc(t.w[0], c2 * 977u);
+    t.w[1] = addc(t.w[1], c2);
+    return t;
+  }
+  // a - b for a, b < 2^256, weakly reduced: a borrow is worth -(2^32 + 977);
+  // a second borrow leaves words 2..7 all ones and word 1 at least 2^32 - 2,
+  // so its correction touches words 0 and 1 alone
   SG_HD static u256 sub(const u256& a, const u256& b) {
     u256 t;
     const uint32_t bw = u256_sub(t, a, b);
-    t.w[0] = sub_cc(t.w[0], bw ? 977u : 0u);
+    t.w[0] = sub_cc(t.w[0], bw * 977u);
     t.w[1] = subc_cc(t.w[1], bw);
 #pragma unroll
     for (int j = 2; j < 8; ++j) t.w[j] = subc_cc(t.w[j], 0u);
-    (void)subc(0u, 0u);
+    const uint32_t bw2 = subc(0u, 0u) & 1u;
+    t.w[0] = sub_cc(t.w[0], bw2 * 977u);
+    t.w[1] = subc(t.w[1], bw2);
     return t;
   }
   SG_HD static u256 neg(const u256& a) { return sub(u256_zero(), a); }  // 0 - 0 = 0 without a borrow
   SG_HD static u256 one() { return u256_small(1); }
   SG_HD static u256 zero() { return u256_zero(); }
-  SG_HD static u256 from_int(const u256& x) { return reduce_once(x, P()); }  // x < 2^256
-  SG_HD static u256 to_int(const u256& a) { return a; }
+  SG_HD static u256 from_int(const u256& x) { return canon(x); }  // x < 2^256
+  SG_HD static u256 to_int(const u256& a) { return canon(a); }
   SG_HD static u256 sqr_n(u256 a, int n) {
 #pragma unroll 1
     for (int i = 0; i < n; ++i) a = sqr(a);
@@ -155,10 +176,11 @@ struct FpK1 {
     x223 = mul(sqr_n(x220, 3), x3);
   }
 
-  // a^-1 by divsteps, verified; Fermat fallback
+  // a^-1 by divsteps (canonical result), verified; Fermat fallback
   SG_NOINL static u256 inv(const u256 a) {
-    u256 r = divstep_inverse(a, P(), 0x2ddacacfu);
-    return u256_eq(mul(a, r), one()) ? r : inv_fermat(a);
+    const u256 ac = canon(a);
+    u256 r = divstep_inverse(ac, P(), 0x2ddacacfu);
+    return u256_eq(canon(mul(ac, r)), one()) ? r : canon(inv_fermat(ac));
   }
 
   // a^(p-2): 255 squarings, 15 multiplications
@@ -505,6 +527,8 @@ struct FpR1 {
     return reduce_once(r, P());
   }
 
+  SG_HD static u256 canon(const u256& x) { return reduce_once(x, P()); }  // values are canonical already
+  SG_HD static bool is_zero(const u256& a) { return u256_is_zero(a); }
   SG_NOINL static u256 mul(const u256 a, const u256 b) { uint32_t t[16]; mul_wide(t, a, b); return reduce(t); }
   SG_NOINL static u256 sqr(const u256 a) { uint32_t t[16]; sqr_wide(t, a); return reduce(t); }
   SG_HD static u256 add(const u256& a, const u256& b) { return mod_add(a, b, P()); }

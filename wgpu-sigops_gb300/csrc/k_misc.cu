@@ -36,7 +36,7 @@ __global__ void field_test_kernel(int field, int op, const u256* a, const u256* 
     r = F::to_int(ra);                                    \
   }
   switch (field) {
-    case 0: if (op == 4) r = FpK1::sqrt_candidate(FpK1::from_int(x)); else SG_OPS(FpK1); break;
+    case 0: if (op == 4) r = FpK1::to_int(FpK1::sqrt_candidate(FpK1::from_int(x))); else SG_OPS(FpK1); break;
     case 1: if (op == 4) r = FpR1::to_int(FpR1::sqrt_candidate(FpR1::from_int(x))); else SG_OPS(FpR1); break;
     case 2: if (op == 4) r = FpEd::canon(FpEd::pow_p58(FpEd::from_int(x))); else SG_OPS(FpEd); break;
     case 3: SG_OPS(ScK1); break;

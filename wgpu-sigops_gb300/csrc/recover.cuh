@@ -328,7 +328,7 @@ SG_HD uint8_t ecdsa_recover(const uint32_t sig[16], const uint32_t msg[8], const
   u256 x = F::from_int(r);
   u256 rhs = T::rhs(x);
   u256 y = F::sqrt_candidate(rhs);
-  if (!u256_eq(F::sqr(y), rhs)) return ST_NO_POINT;
+  if (!u256_eq(F::canon(F::sqr(y)), F::canon(rhs))) return ST_NO_POINT;
   if ((F::to_int(y).w[0] & 1u) != parity) y = F::neg(y);
   APoint R;
   R.x = x;

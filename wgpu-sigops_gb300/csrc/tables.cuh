@@ -54,8 +54,8 @@ inline void weier_multiples(const u256& gx, const u256& gy, int count, APoint* o
         inv = F::mul(inv, jp[i].Z);
       }
       const u256 z2 = F::sqr(zi);
-      out[base + i].x = F::mul(jp[i].X, z2);
-      out[base + i].y = F::mul(jp[i].Y, F::mul(z2, zi));
+      out[base + i].x = F::canon(F::mul(jp[i].X, z2));
+      out[base + i].y = F::canon(F::mul(jp[i].Y, F::mul(z2, zi)));
     }
   }
 }
