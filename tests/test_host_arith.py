@@ -90,7 +90,8 @@ def test_canonical_boundaries(hc, field):
 def test_p256_reduction(hc):
     """The P-256 reduction on products of field elements and on extreme
     512-bit values (all ones, single high words), where the signed column
-    sums and the folded top word reach their bounds."""
+    sums and the folded top word reach their bounds: below 2^256 (weakly
+    reduced) and equal mod p."""
     p = o.SECP256R1.p
     rng = random.Random(70)
     xs = [0, 1, p, p * p, (p - 1) * (p - 1), 2**512 - 1, 2**511, (2**256 - 1) * (2**256 - 1)]
@@ -99,7 +100,8 @@ def test_p256_reduction(hc):
     out = ctypes.create_string_buffer(32)
     for x in xs:
         hc.hc_r1_reduce(x.to_bytes(64, "little"), out)
-        assert int.from_bytes(out.raw, "little") == x % p, hex(x)
+        r = int.from_bytes(out.raw, "little")
+        assert r < 2**256 and r % p == x % p, hex(x)
 
 
 def test_sqr_wide(hc):
@@ -251,9 +253,9 @@ def test_k1_glv_vs_oracle(hc):
         assert (st, out.raw) == o.ecdsa_recover(c, sig, msg)[0:1] + (o.ecdsa_recover(c, sig, msg)[1] or bytes(64),)
 
 
-@pytest.mark.parametrize("field", [0, 2], ids=["secp256k1", "ed25519"])
+@pytest.mark.parametrize("field", [0, 1, 2], ids=["secp256k1", "secp256r1", "ed25519"])
 def test_weak_reduction(hc, field):
-    """The secp256k1 and ed25519 fields keep values below 2^256 only: add /
+    """The three base fields keep values below 2^256 only: add /
     sub / mul / sqr / neg on inputs anywhere in [0, 2^256), including the
     double-carry and double-borrow corrections, stay below 2^256 and agree mod
     p; is_zero recognises both representations of zero."""
@@ -266,6 +268,15 @@ def test_weak_reduction(hc, field):
         for v, z in ((0, 1), (p, 1), (1, 0), (p - 1, 0), (p + 1, 0), (top - 1, 0)):
             out = ctypes.create_string_buffer(32)
             hc.hc_weak(0, 5, le(v), le(0), out)
+            assert out.raw[0] == z, hex(v)
+    elif field == 1:
+        p = o.SECP256R1.p
+        k = top - p
+        edge = [0, 1, 2, k - 1, k, k + 1, 2 * k, p - 1, p, p + 1, p + k - 1, 2**255, top - 1, top - 2, top - k, top - k - 1, top - k + 1,
+                2**224, 2**192, 2**96, 2**96 - 1, top - 2**224]
+        for v, z in ((0, 1), (p, 1), (1, 0), (p - 1, 0), (p + 1, 0), (top - 1, 0)):
+            out = ctypes.create_string_buffer(32)
+            hc.hc_weak(1, 5, le(v), le(0), out)
             assert out.raw[0] == z, hex(v)
     else:
         p = o.ED_P

@@ -1,6 +1,6 @@
-// Prime fields for the three curves, 8 x 32-bit limbs.  FpR1 and the scalar
-// fields keep values canonical (in [0, p)) after every operation; FpK1 and
-// FpEd keep them below 2^256 only (weakly reduced) and make them canonical
+// Prime fields for the three curves, 8 x 32-bit limbs.  The scalar fields
+// keep values canonical (in [0, p)) after every operation; the three base
+// fields keep them below 2^256 only (weakly reduced) and make them canonical
 // (canon) where a comparison or an encoding needs it.  The base-field multiply and square are
 // called functions, not inlined: the hot loops then fit the instruction cache
 // (inlining them everywhere measured 4% slower overall, 19% on ed25519, and
@@ -520,38 +520,67 @@ struct FpR1 {
       v >>= 32;
     }
     fold(w, v);  // |v| <= 6 -> v in {-1, 0, 1}
-    fold(w, v);  // -> v == 0, value in [0, 2^256)
+    fold(w, v);  // -> v == 0, value in [0, 2^256): weakly reduced
     u256 r;
 #pragma unroll
     for (int k = 0; k < 8; ++k) r.w[k] = w[k];
-    return reduce_once(r, P());
+    return r;
   }
 
-  SG_HD static u256 canon(const u256& x) { return reduce_once(x, P()); }  // values are canonical already
-  SG_HD static bool is_zero(const u256& a) { return u256_is_zero(a); }
+  SG_HD static u256 canon(const u256& x) { return reduce_once(x, P()); }  // x < 2^256 < 2p
+  SG_HD static bool is_zero(const u256& a) { return u256_is_zero(a) || u256_eq(a, P()); }  // a == 0 mod p
   SG_NOINL static u256 mul(const u256 a, const u256 b) { uint32_t t[16]; mul_wide(t, a, b); return reduce(t); }
   SG_NOINL static u256 sqr(const u256 a) { uint32_t t[16]; sqr_wide(t, a); return reduce(t); }
-  SG_HD static u256 add(const u256& a, const u256& b) { return mod_add(a, b, P()); }
-  // a - b for a, b < p: a borrow adds p (masked by the borrow), no select
+
+  // t += c K with K = 2^256 - p = 2^224 - 2^192 - 2^96 + 1 (words 1, 0, 0,
+  // 2^32 - 1 (three), 2^32 - 2, 0) for c in {0, 1}; returns the carry out
+  SG_HD static uint32_t add_k(u256& t, uint32_t c) {
+    const uint32_t m = 0u - c;
+    t.w[0] = add_cc(t.w[0], c);
+    t.w[1] = addc_cc(t.w[1], 0u);
+    t.w[2] = addc_cc(t.w[2], 0u);
+    t.w[3] = addc_cc(t.w[3], m);
+    t.w[4] = addc_cc(t.w[4], m);
+    t.w[5] = addc_cc(t.w[5], m);
+    t.w[6] = addc_cc(t.w[6], m - c);
+    t.w[7] = addc_cc(t.w[7], 0u);
+    return addc(0u, 0u);
+  }
+  // t -= b K for b in {0, 1}; returns the borrow out
+  SG_HD static uint32_t sub_k(u256& t, uint32_t b) {
+    const uint32_t m = 0u - b;
+    t.w[0] = sub_cc(t.w[0], b);
+    t.w[1] = subc_cc(t.w[1], 0u);
+    t.w[2] = subc_cc(t.w[2], 0u);
+    t.w[3] = subc_cc(t.w[3], m);
+    t.w[4] = subc_cc(t.w[4], m);
+    t.w[5] = subc_cc(t.w[5], m);
+    t.w[6] = subc_cc(t.w[6], m - b);
+    t.w[7] = subc_cc(t.w[7], 0u);
+    return subc(0u, 0u) & 1u;
+  }
+  // a + b for a, b < 2^256, weakly reduced: a carry out of 2^256 is worth K;
+  // when adding K carries again the sum left is below K, so a second K
+  // cannot carry
+  SG_HD static u256 add(const u256& a, const u256& b) {
+    u256 t;
+    const uint32_t c = u256_add(t, a, b);
+    (void)add_k(t, add_k(t, c));
+    return t;
+  }
+  // a - b for a, b < 2^256, weakly reduced: a borrow is worth -K; after a
+  // second borrow the value is at least p, so a second K cannot borrow
   SG_HD static u256 sub(const u256& a, const u256& b) {
     u256 t;
     const uint32_t bw = u256_sub(t, a, b);
-    const uint32_t m = 0u - bw;  // all ones on a borrow
-    t.w[0] = add_cc(t.w[0], m);
-    t.w[1] = addc_cc(t.w[1], m);
-    t.w[2] = addc_cc(t.w[2], m);
-    t.w[3] = addc_cc(t.w[3], 0u);
-    t.w[4] = addc_cc(t.w[4], 0u);
-    t.w[5] = addc_cc(t.w[5], 0u);
-    t.w[6] = addc_cc(t.w[6], bw);
-    t.w[7] = addc(t.w[7], m);
+    (void)sub_k(t, sub_k(t, bw));
     return t;
   }
   SG_HD static u256 neg(const u256& a) { return sub(u256_zero(), a); }  // 0 - 0 = 0 without a borrow
   SG_HD static u256 one() { return u256_small(1); }
   SG_HD static u256 zero() { return u256_zero(); }
-  SG_HD static u256 from_int(const u256& x) { return reduce_once(x, P()); }  // x < 2^256
-  SG_HD static u256 to_int(const u256& a) { return a; }
+  SG_HD static u256 from_int(const u256& x) { return canon(x); }  // x < 2^256
+  SG_HD static u256 to_int(const u256& a) { return canon(a); }
   SG_HD static u256 curve_b() { return SG_U256(0x27d2604bu, 0x3bce3c3eu, 0xcc53b0f6u, 0x651d06b0u, 0x769886bcu, 0xb3ebbd55u, 0xaa3a93e7u, 0x5ac635d8u); }
 
   SG_HD static u256 sqr_n(u256 a, int n) {
@@ -569,10 +598,11 @@ struct FpR1 {
     x32 = mul(sqr_n(x16, 16), x16);
   }
 
-  // a^-1 by divsteps, verified; Fermat fallback
+  // a^-1 by divsteps (canonical result), verified; Fermat fallback
   SG_NOINL static u256 inv(const u256 a) {
-    u256 r = divstep_inverse(a, P(), 0x3fffffffu);
-    return u256_eq(mul(a, r), one()) ? r : inv_fermat(a);
+    const u256 ac = canon(a);
+    u256 r = divstep_inverse(ac, P(), 0x3fffffffu);
+    return u256_eq(canon(mul(ac, r)), one()) ? r : canon(inv_fermat(ac));
   }
 
   // a^(p-2), p-2 = ones[255..224] 0^31 1 0^96 ones[95..2] 0 1 : 255 S + 13 M
