@@ -134,7 +134,7 @@ extern "C" void hc_ed_sign(const uint8_t* seed, const uint8_t* msg, uint8_t* sig
 
 // weakly reduced field operations (field 0 secp256k1, 1 P-256, 2 ed25519)
 // on raw inputs below 2^256, raw result: op 0 add, 1 sub, 2 mul, 3 sqr,
-// 4 neg, 5 is_zero (secp256k1, P-256)
+// 4 neg, 5 is_zero, 6 half (5 and 6: secp256k1, P-256)
 template <class F>
 static u256 weak_op(int op, const u256& x, const u256& y) {
   if (op == 0) return F::add(x, y);
@@ -146,6 +146,7 @@ static u256 weak_op(int op, const u256& x, const u256& y) {
 extern "C" void hc_weak(int field, int op, const uint8_t* a, const uint8_t* b, uint8_t* out) {
   u256 x = load_le(a), y = load_le(b), r = u256_zero();
   if (op == 5) r.w[0] = field == 0 ? FpK1::is_zero(x) : FpR1::is_zero(x);
+  else if (op == 6) r = field == 0 ? FpK1::half(x) : FpR1::half(x);
   else if (field == 0) r = weak_op<FpK1>(op, x, y);
   else if (field == 1) r = weak_op<FpR1>(op, x, y);
   else r = weak_op<FpEd>(op, x, y);

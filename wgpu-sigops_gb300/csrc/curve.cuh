@@ -65,46 +65,26 @@ struct Weier {
   SG_HD static bool is_inf(const JPoint& p) { return u256_is_zero(p.Z); }
   SG_HD static JPoint from_affine(const APoint& a) { JPoint r; r.X = a.x; r.Y = a.y; r.Z = F::one(); return r; }
 
+  // 2p in the form of dbl-2004-hmv: (2Y)^2 gives 4 Y^2 and, squared and
+  // halved, 8 Y^4, which saves the small multiples' additions.
+  // a = -3: M = 3 (X - Z^2)(X + Z^2), 4M + 4S; a = 0: M = 3 X^2, 3M + 4S.
   SG_HD static JPoint dbl(const JPoint& p) {
     JPoint r;
+    u256 M;
     if (A_M3) {
-      // dbl-2001-b: 3M + 5S
-      u256 delta = F::sqr(p.Z);
-      u256 gamma = F::sqr(p.Y);
-      u256 beta = F::mul(p.X, gamma);
-      u256 t0 = F::sub(p.X, delta);
-      u256 t1 = F::add(p.X, delta);
-      u256 alpha = F::mul(t0, t1);
-      alpha = F::add(F::add(alpha, alpha), alpha);
-      u256 beta4 = F::add(beta, beta);
-      beta4 = F::add(beta4, beta4);
-      u256 beta8 = F::add(beta4, beta4);
-      r.X = F::sub(F::sqr(alpha), beta8);
-      u256 yz = F::add(p.Y, p.Z);
-      r.Z = F::sub(F::sub(F::sqr(yz), gamma), delta);
-      u256 g2 = F::sqr(gamma);
-      u256 g8 = F::add(g2, g2);
-      g8 = F::add(g8, g8);
-      g8 = F::add(g8, g8);
-      r.Y = F::sub(F::mul(alpha, F::sub(beta4, r.X)), g8);
+      const u256 zz = F::sqr(p.Z);
+      M = F::mul(F::sub(p.X, zz), F::add(p.X, zz));
     } else {
-      // dbl-2009-l: 2M + 5S
-      u256 A = F::sqr(p.X);
-      u256 B = F::sqr(p.Y);
-      u256 C = F::sqr(B);
-      u256 xb = F::add(p.X, B);
-      u256 D = F::sub(F::sub(F::sqr(xb), A), C);
-      D = F::add(D, D);
-      u256 E = F::add(F::add(A, A), A);
-      u256 Fv = F::sqr(E);
-      r.X = F::sub(Fv, F::add(D, D));
-      u256 C8 = F::add(C, C);
-      C8 = F::add(C8, C8);
-      C8 = F::add(C8, C8);
-      r.Y = F::sub(F::mul(E, F::sub(D, r.X)), C8);
-      u256 yz = F::mul(p.Y, p.Z);
-      r.Z = F::add(yz, yz);
+      M = F::sqr(p.X);
     }
+    M = F::add(F::add(M, M), M);
+    const u256 y2 = F::add(p.Y, p.Y);
+    r.Z = F::mul(y2, p.Z);
+    const u256 y4 = F::sqr(y2);      // 4 Y^2
+    const u256 S = F::mul(y4, p.X);  // 4 X Y^2
+    const u256 y8 = F::half(F::sqr(y4));  // 8 Y^4
+    r.X = F::sub(F::sqr(M), F::add(S, S));
+    r.Y = F::sub(F::mul(F::sub(S, r.X), M), y8);
     return r;
   }
 

@@ -150,6 +150,21 @@ struct FpK1 {
     t.w[1] = subc(t.w[1], bw2);
     return t;
   }
+  // a / 2 mod p for a < 2^256, weakly reduced: (a + p) / 2 when a is odd
+  SG_HD static u256 half(const u256& a) {
+    const uint32_t m = 0u - (a.w[0] & 1u);
+    const u256 p = P();
+    u256 t;
+    t.w[0] = add_cc(a.w[0], p.w[0] & m);
+#pragma unroll
+    for (int j = 1; j < 8; ++j) t.w[j] = addc_cc(a.w[j], p.w[j] & m);
+    const uint32_t c = addc(0u, 0u);
+    u256 r;
+#pragma unroll
+    for (int j = 0; j < 7; ++j) r.w[j] = (t.w[j] >> 1) | (t.w[j + 1] << 31);
+    r.w[7] = (t.w[7] >> 1) | (c << 31);
+    return r;
+  }
   SG_HD static u256 neg(const u256& a) { return sub(u256_zero(), a); }  // 0 - 0 = 0 without a borrow
   SG_HD static u256 one() { return u256_small(1); }
   SG_HD static u256 zero() { return u256_zero(); }
@@ -575,6 +590,21 @@ struct FpR1 {
     const uint32_t bw = u256_sub(t, a, b);
     (void)sub_k(t, sub_k(t, bw));
     return t;
+  }
+  // a / 2 mod p for a < 2^256, weakly reduced: (a + p) / 2 when a is odd
+  SG_HD static u256 half(const u256& a) {
+    const uint32_t m = 0u - (a.w[0] & 1u);
+    const u256 p = P();
+    u256 t;
+    t.w[0] = add_cc(a.w[0], p.w[0] & m);
+#pragma unroll
+    for (int j = 1; j < 8; ++j) t.w[j] = addc_cc(a.w[j], p.w[j] & m);
+    const uint32_t c = addc(0u, 0u);
+    u256 r;
+#pragma unroll
+    for (int j = 0; j < 7; ++j) r.w[j] = (t.w[j] >> 1) | (t.w[j + 1] << 31);
+    r.w[7] = (t.w[7] >> 1) | (c << 31);
+    return r;
   }
   SG_HD static u256 neg(const u256& a) { return sub(u256_zero(), a); }  // 0 - 0 = 0 without a borrow
   SG_HD static u256 one() { return u256_small(1); }
