@@ -206,6 +206,13 @@ extern "C" void hc_r1_reduce(const uint8_t* x64, uint8_t* out) {
   store_le(FpR1::reduce(t), out);
 }
 
+// reduction of a 512-bit value in field 0 (secp256k1), 1 (P-256), 2 (ed25519)
+extern "C" void hc_reduce(int field, const uint8_t* x64, uint8_t* out) {
+  uint32_t t[16];
+  memcpy(t, x64, 64);
+  store_le(field == 0 ? FpK1::reduce(t) : field == 1 ? FpR1::reduce(t) : FpEd::reduce(t), out);
+}
+
 // multiply instructions counted since the last reset (this thread)
 extern "C" uint64_t hc_mulcount(int reset) {
   const uint64_t c = mulcount_();

@@ -254,6 +254,35 @@ def test_k1_glv_vs_oracle(hc):
 
 
 @pytest.mark.parametrize("field", [0, 1, 2], ids=["secp256k1", "secp256r1", "ed25519"])
+def test_reduce_512(hc, field):
+    """Reduction of 512-bit values, including those whose folds carry out of
+    2^256 again (low half near 2^256, high half extreme): below 2^256, equal
+    mod p."""
+    p = [o.SECP256K1.p, o.SECP256R1.p, o.ED_P][field]
+    top = 2**256
+    rng = random.Random(90 + field)
+    highs = [0, 1, 2**32 - 1, 2**32, top - 1, top - 2, 2**255, 2**224, top - 2**32, 2**64 - 1]
+    lows = [0, 1, top - 1, top - 2, top - 977, top - 2**32 - 977, top - 38, top - 39, top - 2**33, top - 2**66, top - 2**70]
+    xs = [h * top + l for h in highs for l in lows]
+    xs += [rng.getrandbits(256) * top + (top - rng.getrandbits(rng.choice([8, 40, 70, 100]))) for _ in range(400)]
+    xs += [rng.getrandbits(512) for _ in range(400)]
+    if field != 1:
+        # the first fold L + H (2^256 - p) lands just below a multiple of 2^256,
+        # so that folding its top words carries out again
+        c = top - p if field == 0 else 38
+        for _ in range(400):
+            h = rng.getrandbits(256)
+            delta = rng.randrange(1, 2**rng.choice([4, 10, 20, 40, 64]))
+            l = (top - delta - h * c) % top
+            xs.append(h * top + l)
+    out = ctypes.create_string_buffer(32)
+    for x in xs:
+        hc.hc_reduce(field, x.to_bytes(64, "little"), out)
+        r = int.from_bytes(out.raw, "little")
+        assert r < top and r % p == x % p, hex(x)
+
+
+@pytest.mark.parametrize("field", [0, 1, 2], ids=["secp256k1", "secp256r1", "ed25519"])
 def test_weak_reduction(hc, field):
     """The three base fields keep values below 2^256 only: add /
     sub / mul / sqr / neg on inputs anywhere in [0, 2^256), including the

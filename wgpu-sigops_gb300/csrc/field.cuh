@@ -87,31 +87,25 @@ struct FpK1 {
 #pragma unroll
     for (int j = 1; j < 8; ++j) v[j + 1] = addc_cc(v[j + 1], t[8 + j]);
     v[9] = addc(0u, 0u);
-    // second fold of the top 33 bits: top = v[8] + v[9] * 2^32 (v[9] <= 1)
-    // top * (2^32 + 977) = v8*977 + (v8 + v9*977) * 2^32 + v9 * 2^64
+    // second fold of the top 33 bits, top = v[8] + v[9] 2^32 (v[9] <= 1), as
+    // one three-word addend: top (2^32 + 977) = a0 + a1 2^32 + a2 2^64 with
+    // a0 = lo(v8 977), a1 = hi(v8 977) + v8 + v9 977, a2 = v9 + carry
+    const uint32_t s1 = mul_hi(v[8], 977u) + v[9] * 977u;  // < 2 * 977
+    const uint32_t a0 = mul_lo(v[8], 977u);
+    const uint32_t a1 = add_cc(v[8], s1);
+    const uint32_t a2 = addc(v[9], 0u);
     u256 r;
-    r.w[0] = mad_lo_cc(v[8], 977u, v[0]);
-    r.w[1] = madc_hi_cc(v[8], 977u, v[1]);
-    r.w[2] = addc_cc(v[2], v[9]);
+    r.w[0] = add_cc(v[0], a0);
+    r.w[1] = addc_cc(v[1], a1);
+    r.w[2] = addc_cc(v[2], a2);
 #pragma unroll
     for (int j = 3; j < 8; ++j) r.w[j] = addc_cc(v[j], 0u);
-    uint32_t c1 = addc(0u, 0u);
-    r.w[1] = add_cc(r.w[1], v[8]);
-#pragma unroll
-    for (int j = 2; j < 8; ++j) r.w[j] = addc_cc(r.w[j], 0u);
-    uint32_t c2 = addc(c1, 0u);
-    uint32_t v9m = v[9] * 977u;
-    r.w[1] = add_cc(r.w[1], v9m);
-#pragma unroll
-    for (int j = 2; j < 8; ++j) r.w[j] = addc_cc(r.w[j], 0u);
-    uint32_t c3 = addc(c2, 0u);
-    // c3 <= 1; when set the low 256 bits are tiny, so adding c once cannot carry
-    uint32_t cm = c3 * 977u;
-    r.w[0] = add_cc(r.w[0], cm);
-    r.w[1] = addc_cc(r.w[1], c3);
-#pragma unroll
-    for (int j = 2; j < 8; ++j) r.w[j] = addc_cc(r.w[j], 0u);
-    (void)addc(0u, 0u);
+    const uint32_t c = addc(0u, 0u);
+    // a carry out leaves r below 2^66: adding 2^32 + 977 back reaches word 2
+    // at most
+    r.w[0] = add_cc(r.w[0], c * 977u);
+    r.w[1] = addc_cc(r.w[1], c);
+    r.w[2] = addc(r.w[2], 0u);
     return r;
   }
 
@@ -258,11 +252,9 @@ struct FpEd {
     r.w[0] = mad_lo_cc(v[8], 38u, v[0]);
 #pragma unroll
     for (int j = 1; j < 8; ++j) r.w[j] = addc_cc(v[j], 0u);
-    uint32_t c = addc(0u, 0u);
-    r.w[0] = add_cc(r.w[0], c * 38u);
-#pragma unroll
-    for (int j = 1; j < 8; ++j) r.w[j] = addc_cc(r.w[j], 0u);
-    (void)addc(0u, 0u);
+    const uint32_t c = addc(0u, 0u);
+    // a carry out leaves r below 38 * 38 + 38: adding 38 back stays in word 0
+    r.w[0] += c * 38u;
     return r;
   }
 
