@@ -161,7 +161,10 @@ int sigops_plain_device(sigops_ctx* ctx, int curve, const uint8_t* d_sigs, const
  * those of the per-curve calls above.
  * curves: n tags (SIGOPS_SECP256K1 / SECP256R1 / ED25519); sigs n*64; msgs
  * n*32; pks n*32 (read for ed25519 items only); out n*64 (ECDSA: key bytes;
- * ed25519: byte 0 = valid, rest zero); out_status n (may be NULL). */
+ * ed25519: byte 0 = valid, rest zero); out_status n (may be NULL).  When all
+ * buffers are page-locked and n >= 131072, the call runs as two halves on
+ * two streams (the first at the highest priority), so that copies overlap
+ * the other half's kernels. */
 int sigops_verify_mixed(sigops_ctx* ctx, const uint8_t* curves, const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks, size_t n,
                         uint8_t* out, uint8_t* out_status);
 

@@ -173,3 +173,22 @@ def test_workload_generator_selfcheck(w):
     items = [(int(W.curves[i]), W.sigs[i].tobytes(), W.msgs[i].tobytes(), W.pks[i].tobytes()) for i in idx]
     for k, (exp, st) in enumerate(oracle_mixed(items)):
         assert out[idx[k]].tobytes() == exp and status[idx[k]] == st
+
+
+def test_pipelined_host_call(w):
+    """Page-locked calls of 131,072 items or more run as two halves on two
+    streams; the results match the generator-known outcomes and the
+    single-stream device call, at an odd size that splits off-centre."""
+    import torch
+    from wgpu_sig_ops import workload as wl
+
+    W = wl.config("c4", n=200003, seed=9)
+    ctx = w.default_context()
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+    h_out = torch.zeros((W.n, 64), dtype=torch.uint8).pin_memory().numpy()
+    h_st = torch.full((W.n,), 0xFF, dtype=torch.uint8).pin_memory().numpy()
+    w.batch.verify_mixed_into(ctx, pin(W.curves), pin(W.sigs), pin(W.msgs), pin(W.pks), h_out, h_st)
+    chk = wl.expected_check(W, h_out, h_st)
+    assert chk["mismatches"] == 0, chk
+    out, status = w.batch.verify_mixed(W.curves, W.sigs, W.msgs, W.pks)  # staged, one stream
+    assert (out == h_out).all() and (status == h_st).all()

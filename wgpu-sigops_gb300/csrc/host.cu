@@ -85,6 +85,13 @@ struct sigops_ctx {
   int batched_variant = 0;
   int batched_grid = 0;
   ForkStreams fork{};  // side streams of the single-curve batched variants
+  // first half of a pipelined sigops_verify_mixed: its own stream and side
+  // streams at the highest priority, its own scratch record (the index lists
+  // split the one allocation)
+  cudaStream_t stream2 = nullptr;
+  ForkStreams fork2{};
+  void* d_scratch2 = nullptr;
+  cudaEvent_t ev_order = nullptr, ev_join = nullptr;
   std::mutex mu;
 };
 
@@ -166,12 +173,17 @@ int set_variant(sigops_ctx* c, int kernel, int variant) {
   return fail(SIGOPS_E_INVAL, "kernel id %d out of range", kernel);
 }
 
-cudaError_t launch_mixed(sigops_ctx* c, const uint8_t* curves, const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks, size_t n,
-                         uint8_t* out, uint8_t* status, cudaStream_t s) {
+cudaError_t launch_mixed_on(sigops_ctx* c, const uint8_t* curves, const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks, size_t n,
+                            uint8_t* out, uint8_t* status, uint32_t* idx, void* scratch, const ForkStreams* fork, cudaStream_t s) {
   size_t cg = (n + 255) / 256;
   int classify_grid = (int)(cg < (size_t)c->num_sms * 8 ? cg : (size_t)c->num_sms * 8);
-  return launch_batched(curves, sigs, msgs, pks, n, out, status, c->d_idx, c->d_scratch, c->d_gtab[0], c->d_gtab[1], c->d_gtab[2], c->d_err,
-                        c->batched_grid, c->batched_variant, classify_grid, &c->fork, s);
+  return launch_batched(curves, sigs, msgs, pks, n, out, status, idx, scratch, c->d_gtab[0], c->d_gtab[1], c->d_gtab[2], c->d_err,
+                        c->batched_grid, c->batched_variant, classify_grid, fork, s);
+}
+
+cudaError_t launch_mixed(sigops_ctx* c, const uint8_t* curves, const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks, size_t n,
+                         uint8_t* out, uint8_t* status, cudaStream_t s) {
+  return launch_mixed_on(c, curves, sigs, msgs, pks, n, out, status, c->d_idx, c->d_scratch, &c->fork, s);
 }
 
 int check_device_errors(sigops_ctx* c) {
@@ -298,6 +310,12 @@ sigops_ctx* sigops_create(int device) {
   if ((e = cudaSetDevice(device)) != cudaSuccess) return bail("cudaSetDevice", e);
   if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess) return bail("cudaStreamCreate", e);
   if ((e = fork_streams_create(&c->fork)) != cudaSuccess) return bail("side streams", e);
+  int prio_least = 0, prio_greatest = 0;
+  if ((e = cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest)) != cudaSuccess) return bail("stream priorities", e);
+  if ((e = cudaStreamCreateWithPriority(&c->stream2, cudaStreamNonBlocking, prio_greatest)) != cudaSuccess) return bail("cudaStreamCreate", e);
+  if ((e = fork_streams_create(&c->fork2, prio_greatest)) != cudaSuccess) return bail("side streams", e);
+  if ((e = cudaEventCreateWithFlags(&c->ev_order, cudaEventDisableTiming)) != cudaSuccess) return bail("cudaEventCreate", e);
+  if ((e = cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming)) != cudaSuccess) return bail("cudaEventCreate", e);
   if ((e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device)) != cudaSuccess) return bail("attr", e);
   for (int k = 0; k < 3; ++k) {
     const auto& t = tabs.tab[k];
@@ -310,6 +328,7 @@ sigops_ctx* sigops_create(int device) {
   }
   if ((e = cudaMalloc(&c->d_err, sizeof(uint32_t))) != cudaSuccess) return bail("cudaMalloc(err)", e);
   if ((e = cudaMalloc(&c->d_scratch, batched_scratch_bytes())) != cudaSuccess) return bail("cudaMalloc(scratch)", e);
+  if ((e = cudaMalloc(&c->d_scratch2, batched_scratch_bytes())) != cudaSuccess) return bail("cudaMalloc(scratch)", e);
   if (set_variant(c, 3, 0) != SIGOPS_OK) {
     sigops_destroy(c);
     return nullptr;
@@ -325,15 +344,21 @@ void sigops_destroy(sigops_ctx* c) {
   if (!c) return;
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
+  if (c->stream2) cudaStreamSynchronize(c->stream2);
   for (int k = 0; k < 3; ++k)
     if (c->d_gtab[k]) cudaFree(c->d_gtab[k]);
   if (c->d_err) cudaFree(c->d_err);
   if (c->d_scratch) cudaFree(c->d_scratch);
+  if (c->d_scratch2) cudaFree(c->d_scratch2);
   if (c->d_idx) cudaFree(c->d_idx);
   if (c->d_buf) cudaFree(c->d_buf);
   if (c->h_buf) cudaFreeHost(c->h_buf);
   if (c->stream) cudaStreamDestroy(c->stream);
   fork_streams_destroy(&c->fork);
+  if (c->stream2) cudaStreamDestroy(c->stream2);
+  fork_streams_destroy(&c->fork2);
+  if (c->ev_order) cudaEventDestroy(c->ev_order);
+  if (c->ev_join) cudaEventDestroy(c->ev_join);
   {
     std::lock_guard<std::mutex> g(g_default_mu);
     if (g_default == c) g_default = nullptr;
@@ -482,6 +507,9 @@ int sigops_verify_mixed_device(sigops_ctx* ctx, const uint8_t* d_curves, const u
   return SIGOPS_OK;
 }
 
+// page-locked calls from this size on run as two pipelined halves
+constexpr size_t kPipelineMin = 131072;
+
 int sigops_verify_mixed(sigops_ctx* ctx, const uint8_t* curves, const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks, size_t n,
                         uint8_t* out, uint8_t* out_status) {
   if (n == 0) return SIGOPS_OK;
@@ -509,6 +537,31 @@ int sigops_verify_mixed(sigops_ctx* ctx, const uint8_t* curves, const uint8_t* s
   if (rc) return rc;
   rc = ensure_idx(c, n);
   if (rc) return rc;
+  if (pinned && n >= kPipelineMin) {
+    // two halves on two streams: the first on the high-priority stream, so
+    // its blocks go first and the second half's fill the SMs it leaves idle;
+    // the second half's inputs cross while the first half computes, and the
+    // first half's results cross while the second half computes
+    const size_t half = (n / 2 + 255) & ~(size_t)255;
+    SG_CUDA(cudaEventRecord(c->ev_order, c->stream));  // after any earlier work on the buffers
+    SG_CUDA(cudaStreamWaitEvent(c->stream2, c->ev_order, 0));
+    for (int k = 0; k < 2; ++k) {
+      const size_t b = k ? half : 0, m = k ? n - half : half;
+      cudaStream_t s = k ? c->stream : c->stream2;
+      SG_CUDA(cudaMemcpyAsync(c->d_buf + o_sig + b * 64, sigs + b * 64, m * 64, cudaMemcpyHostToDevice, s));
+      SG_CUDA(cudaMemcpyAsync(c->d_buf + o_msg + b * 32, msgs + b * 32, m * 32, cudaMemcpyHostToDevice, s));
+      SG_CUDA(cudaMemcpyAsync(c->d_buf + o_pk + b * 32, pks + b * 32, m * 32, cudaMemcpyHostToDevice, s));
+      SG_CUDA(cudaMemcpyAsync(c->d_buf + o_cur + b, curves + b, m, cudaMemcpyHostToDevice, s));
+      SG_CUDA(launch_mixed_on(c, c->d_buf + o_cur + b, c->d_buf + o_sig + b * 64, c->d_buf + o_msg + b * 32, c->d_buf + o_pk + b * 32, m,
+                              c->d_buf + o_out + b * 64, c->d_buf + o_st + b, c->d_idx + (k ? 3 * half : 0),
+                              k ? c->d_scratch : c->d_scratch2, k ? &c->fork : &c->fork2, s));
+      SG_CUDA(cudaMemcpyAsync(out + b * 64, c->d_buf + o_out + b * 64, m * 64, cudaMemcpyDeviceToHost, s));
+      if (out_status) SG_CUDA(cudaMemcpyAsync(out_status + b, c->d_buf + o_st + b, m, cudaMemcpyDeviceToHost, s));
+    }
+    SG_CUDA(cudaEventRecord(c->ev_join, c->stream2));
+    SG_CUDA(cudaStreamWaitEvent(c->stream, c->ev_join, 0));
+    return check_device_errors(c);
+  }
   if (pinned) {
     SG_CUDA(cudaMemcpyAsync(c->d_buf + o_sig, sigs, n * 64, cudaMemcpyHostToDevice, c->stream));
     SG_CUDA(cudaMemcpyAsync(c->d_buf + o_msg, msgs, n * 32, cudaMemcpyHostToDevice, c->stream));

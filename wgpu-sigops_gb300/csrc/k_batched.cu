@@ -93,11 +93,11 @@ int batched_max_blocks_per_sm(int v) {
   return m;
 }
 
-cudaError_t fork_streams_create(ForkStreams* f) {
+cudaError_t fork_streams_create(ForkStreams* f, int priority) {
   *f = ForkStreams{};
   cudaError_t e;
   for (int k = 0; k < 2; ++k)
-    if ((e = cudaStreamCreateWithFlags(&f->aux[k], cudaStreamNonBlocking)) != cudaSuccess) return e;
+    if ((e = cudaStreamCreateWithPriority(&f->aux[k], cudaStreamNonBlocking, priority)) != cudaSuccess) return e;
   for (int k = 0; k < 3; ++k)
     if ((e = cudaEventCreateWithFlags(&f->ev[k], cudaEventDisableTiming)) != cudaSuccess) return e;
   return cudaSuccess;

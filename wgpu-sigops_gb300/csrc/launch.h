@@ -56,7 +56,8 @@ struct ForkStreams {
   cudaStream_t aux[2];
   cudaEvent_t ev[3];
 };
-cudaError_t fork_streams_create(ForkStreams* f);
+// priority: as cudaStreamCreateWithPriority (0 = default)
+cudaError_t fork_streams_create(ForkStreams* f, int priority = 0);
 void fork_streams_destroy(ForkStreams* f);
 // grid: blocks of the fused kernel (the single-curve kernels size their grids
 // to the batch: one item per thread)
