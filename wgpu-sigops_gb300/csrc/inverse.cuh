@@ -159,6 +159,18 @@ SG_HD u256 divstep_inverse(const u256& x, const u256& Mu, uint32_t minv30) {
     delta2 = divsteps30(delta2, (uint32_t)f.v[0] | ((uint32_t)f.v[1] << 30), (uint32_t)g.v[0] | ((uint32_t)g.v[1] << 30), t);
     s30_update_de(d, e, t, M, minv30);
     s30_update_fg(f, g, t);
+#ifdef __CUDA_ARCH__
+    // once g = 0 further batches only keep f = +-1 and change d by multiples
+    // of M, so the warp stops when all of its lanes are there (random inputs
+    // get there after 17 or 18 batches).  The host build runs every batch, so
+    // the multiply counts taken from it stay an upper bound.
+    if (it >= 12) {
+      uint32_t nz = 0;
+#pragma unroll
+      for (int k = 0; k < 9; ++k) nz |= (uint32_t)g.v[k];
+      if (__all_sync(__activemask(), nz == 0)) break;
+    }
+#endif
   }
   // now g = 0 and f = +-1: x^-1 = sign(f) * d, with d in (-2M, M)
   u256 lo;
