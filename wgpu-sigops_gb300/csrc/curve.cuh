@@ -62,6 +62,9 @@ struct APoint {
 template <class F, bool A_M3>
 struct Weier {
   SG_HD static JPoint infinity() { JPoint r; r.X = F::one(); r.Y = F::one(); r.Z = F::zero(); return r; }
+  // Z is exactly zero (not merely p) for the point at infinity: infinity()
+  // sets it, the exceptional cases return infinity(), and every other Z is a
+  // product of nonzero factors
   SG_HD static bool is_inf(const JPoint& p) { return u256_is_zero(p.Z); }
   SG_HD static JPoint from_affine(const APoint& a) { JPoint r; r.X = a.x; r.Y = a.y; r.Z = F::one(); return r; }
 
