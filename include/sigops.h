@@ -5,8 +5,9 @@
  * (FuelLabs/wgpu-sigops): secp256k1 / secp256r1 ECDSA public-key recovery
  * (`ecrecover`), ed25519 verification (`ecverify`) and the generator-table API
  * `precompute::*_bases(log_limb_size)`.  Every entry point replaces the Rust
- * function cited beside it (paths relative to the reference repository); the
- * Rust-side binding a maintainer adds is shown in INTEGRATION.md.
+ * function cited beside it (paths relative to the reference repository); a
+ * Rust crate binds them with one `extern "C"` block and keeps its public
+ * signatures.
  *
  * Conventions
  *  - Plain pointers and sizes, caller-owned buffers, no exceptions across the
@@ -21,7 +22,7 @@
  *    status is not SIGOPS_ST_OK has a zeroed key (ECDSA) or `false` (ed25519);
  *    the Rust wrapper maps it to an empty `Vec<u8>`, matching the CPU crates'
  *    `Err` for that signature.
- *  - A context owns one CUDA stream, the device-resident generator tables and
+ *  - A context owns its CUDA streams, the device-resident generator tables and
  *    staging buffers.  Calls on one context are serialised internally; use
  *    several contexts for concurrency.  `ctx == NULL` selects a process-wide
  *    default context on device 0, created on first use.
