@@ -165,7 +165,8 @@ int sigops_plain_device(sigops_ctx* ctx, int curve, const uint8_t* d_sigs, const
  * ed25519: byte 0 = valid, rest zero); out_status n (may be NULL).  When all
  * buffers are page-locked and n >= 131072, the call runs as two halves on
  * two streams (the first at the highest priority), so that copies overlap
- * the other half's kernels. */
+ * the other half's kernels.  n < 2^32 (the index lists hold 32-bit item
+ * indices), else SIGOPS_E_RANGE. */
 int sigops_verify_mixed(sigops_ctx* ctx, const uint8_t* curves, const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks, size_t n,
                         uint8_t* out, uint8_t* out_status);
 

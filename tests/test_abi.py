@@ -71,3 +71,15 @@ def test_no_device_is_reported(lib):
 
     assert not L.lib.sigops_create(0)
     assert b"device" in L.lib.sigops_last_error()
+
+
+def test_mixed_batch_size_limit(lib):
+    """The mixed engine's index lists hold 32-bit item indices: larger batches
+    are refused before any device work (no GPU needed)."""
+    from wgpu_sig_ops import _lib as L
+
+    buf = ctypes.create_string_buffer(64)
+    n = 2**32
+    assert L.lib.sigops_verify_mixed(None, buf, buf, buf, buf, n, buf, buf) == L.SIGOPS_E_RANGE
+    assert b"32-bit" in L.lib.sigops_last_error()
+    assert L.lib.sigops_verify_mixed_device(None, buf, buf, buf, buf, n, buf, buf, None) == L.SIGOPS_E_RANGE

@@ -490,8 +490,12 @@ int sigops_reserve(sigops_ctx* ctx, size_t n) {
   return ensure_idx(c, n);
 }
 
+// largest batch of the mixed engine (32-bit item indices)
+constexpr size_t kMaxMixedItems = 0xffffffffull;
+
 int sigops_verify_mixed_device(sigops_ctx* ctx, const uint8_t* d_curves, const uint8_t* d_sigs, const uint8_t* d_msgs, const uint8_t* d_pks,
                                size_t n, uint8_t* d_out, uint8_t* d_status, void* stream) {
+  if (n > kMaxMixedItems) return fail(SIGOPS_E_RANGE, "batch of %zu items: the index lists hold 32-bit indices", n);
   if (n == 0) return SIGOPS_OK;
   auto misaligned = [](const void* p) { return ((uintptr_t)p & 15u) != 0; };
   if (!d_curves || !d_sigs || !d_msgs || !d_pks || !d_out || !d_status) return fail(SIGOPS_E_INVAL, "null device buffer");
@@ -512,6 +516,7 @@ constexpr size_t kPipelineMin = 131072;
 
 int sigops_verify_mixed(sigops_ctx* ctx, const uint8_t* curves, const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks, size_t n,
                         uint8_t* out, uint8_t* out_status) {
+  if (n > kMaxMixedItems) return fail(SIGOPS_E_RANGE, "batch of %zu items: the index lists hold 32-bit indices", n);
   if (n == 0) return SIGOPS_OK;
   if (!curves || !sigs || !msgs || !pks || !out) return fail(SIGOPS_E_INVAL, "null buffer");
   {
@@ -591,6 +596,7 @@ int sigops_verify_mixed(sigops_ctx* ctx, const uint8_t* curves, const uint8_t* s
 
 int sigops_mixed_plan_create(sigops_ctx* ctx, const uint8_t* d_curves, const uint8_t* d_sigs, const uint8_t* d_msgs, const uint8_t* d_pks,
                              size_t n, uint8_t* d_out, uint8_t* d_status, sigops_plan** plan_out) {
+  if (n > kMaxMixedItems) return fail(SIGOPS_E_RANGE, "batch of %zu items: the index lists hold 32-bit indices", n);
   if (!plan_out || n == 0) return fail(SIGOPS_E_INVAL, "plan needs n > 0 and an output pointer");
   sigops_ctx* c = resolve(ctx);
   if (!c) return SIGOPS_E_NODEV;

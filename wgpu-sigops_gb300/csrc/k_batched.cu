@@ -122,7 +122,8 @@ cudaError_t launch_batched(const uint8_t* curves, const uint8_t* sigs, const uin
                            uint8_t* status, uint32_t* idx, void* scratch, const uint32_t* gk1, const uint32_t* gr1, const uint32_t* ged,
                            uint32_t* err, int grid, int variant, int classify_grid, const ForkStreams* fork, cudaStream_t stream) {
   if (n == 0) return cudaSuccess;
-  if (variant < 0 || variant >= BATCHED_VARIANTS || grid <= 0) return cudaErrorInvalidValue;
+  // the per-curve index lists hold 32-bit item indices
+  if (variant < 0 || variant >= BATCHED_VARIANTS || grid <= 0 || n > 0xffffffffull) return cudaErrorInvalidValue;
   Scratch* sc = (Scratch*)scratch;
   cudaError_t e = cudaMemsetAsync(sc, 0, sizeof(Scratch), stream);
   if (e != cudaSuccess) return e;
