@@ -133,7 +133,6 @@ __global__ void __launch_bounds__(BLOCK, MINB) batched_kernel(MixedIO io, const 
 template <int BLOCK, int CURVE>
 __device__ __forceinline__ void curve_body(const MixedIO& io, const uint32_t* __restrict__ idx, const BatchTables& tabs, Scratch* sc,
                                            uint32_t* err) {
-  constexpr int CM = CURVE == 0 ? CM_K1 : CURVE == 1 ? CM_R1 : CM_ED;
   const uint32_t cnt = sc->count[CURVE];
   const uint32_t first = blockIdx.x * BLOCK;
   if (first >= cnt) return;
