@@ -276,6 +276,7 @@ sigops_server* sigops_server_create(sigops_ctx* ctx, int nslots, size_t slot_ite
       return nullptr;
     }
   }
+  s->reqs.reserve(1u << 14);  // in-flight handles of a typical client without a rehash
   s->worker = std::thread(worker_loop, s);
   return s;
 }
@@ -378,6 +379,13 @@ int sigops_server_run_load(sigops_server* s, const uint8_t* curves, const uint8_
   if (!s || !curves || !sigs || !msgs || !pks || !offset || !count || !arrival_s || !out || !latency_ms) return SIGOPS_E_INVAL;
   std::vector<uint64_t> handles(nreq, 0);
   int rc = SIGOPS_OK;
+  {
+    // every request of the run is registered before the first wait: size the
+    // handle table once, so that no rehash (which holds the server's lock for
+    // milliseconds at a few hundred thousand entries) stalls the worker
+    std::lock_guard<std::mutex> g(s->mu);
+    s->reqs.reserve(s->reqs.size() + nreq);
+  }
   const double t0 = now_s();
   for (size_t i = 0; i < nreq; ++i) {
     double target = t0 + arrival_s[i];

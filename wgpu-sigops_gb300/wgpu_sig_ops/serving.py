@@ -74,8 +74,12 @@ class Server:
         """Open-loop run over a pool (dict of curves/sigs/msgs/pks arrays).
         Returns (latency_ms array, wall seconds, out, status)."""
         n = len(pool["curves"])
-        out = np.zeros((n, 64), np.uint8)
-        status = np.zeros(n, np.uint8)
+        # written (not just allocated) here, so that their first-touch page
+        # faults do not land in the server's completion path during the run
+        out = np.empty((n, 64), np.uint8)
+        out.fill(0)
+        status = np.empty(n, np.uint8)
+        status.fill(0)
         offsets = np.ascontiguousarray(offsets, dtype=np.uint64)
         counts = np.ascontiguousarray(counts, dtype=np.uint32)
         arrivals = np.ascontiguousarray(arrivals, dtype=np.float64)
@@ -136,8 +140,9 @@ def request_stream(regions: dict, rate_rps: float, seconds: float, seed: int, ma
 
 
 def measure(ctx, W, loads=(0.25, 0.5, 0.75, 0.9), seconds: float = 10.0, seed: int = 5001, slots: int = 8,
-            slot_items: int = 0, sat_items: int = 2_000_000, variant: int | None = None) -> dict:
-    """Saturation, then open-loop Poisson load levels; latency percentiles in ms."""
+            slot_items: int = 0, sat_items: int = 2_000_000, variant: int | None = None, warmup_seconds: float = 1.0) -> dict:
+    """Saturation, a discarded warm-up run at half load, then open-loop Poisson
+    load levels; latency percentiles in ms."""
     pool, regions = curve_sorted_pool(W)
     srv = Server(ctx, slots=slots, slot_items=slot_items, variant=variant)
     try:
@@ -148,7 +153,10 @@ def measure(ctx, W, loads=(0.25, 0.5, 0.75, 0.9), seconds: float = 10.0, seed: i
         check(rc, "saturation run")
         sat = float(cnts.sum()) / wall
         res = {"saturation_sigs_per_s": sat, "mean_request_items": mean_size, "slot_items": srv.slot_items, "slots": slots, "variant": 1 if variant is None else variant,
-               "seconds_per_level": seconds, "levels": []}
+               "seconds_per_level": seconds, "warmup_seconds": warmup_seconds, "levels": []}
+        if warmup_seconds > 0:  # an open-loop run at half load whose latencies are discarded
+            offs, cnts, arr = request_stream(regions, 0.5 * sat / mean_size, warmup_seconds, seed + 100)
+            check(srv.run_load(pool, offs, cnts, arr)[0], "warm-up run")
         for k, load in enumerate(loads):
             rate = load * sat / mean_size
             offs, cnts, arr = request_stream(regions, rate, seconds, seed + 1 + k)
