@@ -53,7 +53,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU-baseline sample duration")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--serving-seconds", type=float, default=5.0, help="seconds per serving load level (0 = skip serving)")
+    ap.add_argument("--serving-seconds", type=float, default=60.0, help="seconds per serving load level (0 = skip serving)")
     ap.add_argument("--variant", type=int, default=-1, help="batched kernel launch variant (-1 = library default)")
     ap.add_argument("--plain-variant", type=int, default=-1, help="plain kernels launch variant (-1 = library default)")
     ap.add_argument("--no-autotune", action="store_true", help="skip the autotuner (launch variants as set)")
@@ -430,6 +430,9 @@ def main():
                   "outputs_equal_batched": plain_mismatch == 0, "per_curve": per_curve},
         "roofline": {"bound": "imad", "achieved": achieved / 1e12, "peak": mul_peak / 1e12, "unit": "Tmul32/s",
                      "frac": achieved / mul_peak, "traffic": traffic,
+                     # the same work against the plain mad.lo rate (the pipe's issue limit; half the
+                     # counted multiplies are .hi forms, which issue at about 40% of that rate)
+                     "frac_of_mad_lo": achieved / mul_forms["mad.lo"],
                      "peak_source": ("measured in-process: mad.lo.cc/madc.hi.cc carry-chain rows, the form the field "
                                      "multiplications issue (MEASURED_PEAKS.json has no integer figure)"),
                      "peak_forms_T_per_s": {k: v / 1e12 for k, v in mul_forms.items()},
@@ -448,9 +451,10 @@ def main():
     print(json.dumps(line), flush=True)
 
 
-def cpu_baseline(W, out, status, seconds):
-    import numpy as np
-
+def cpu_baseline(W, out, status, seconds, serial_seconds=3.0):
+    """All host threads on a prefix of the batch, compared bit for bit with the
+    GPU; then one core, serially, as the reference's own CPU benchmark loops
+    run (src/benchmarks/secp256k1_ecdsa.rs:117-122, src/benchmarks/ed25519_eddsa.rs:109-113)."""
     from oracle import c_oracle
 
     threads = os.cpu_count() or 1
@@ -464,8 +468,16 @@ def cpu_baseline(W, out, status, seconds):
     o_out, o_st = c_oracle.batch_mixed(W.curves[:sample], W.sigs[:sample], W.msgs[:sample], W.pks[:sample], threads=threads)
     dt = time.perf_counter() - t0
     mism = int((o_st != status[:sample]).sum() + (o_out != out[:sample]).any(axis=1).sum())
+    # one core, serially: a prefix sized to about serial_seconds
+    m = max(64, min(W.n, int(rate0 / threads * serial_seconds)))
+    t0 = time.perf_counter()
+    s_out, s_st = c_oracle.batch_mixed(W.curves[:m], W.sigs[:m], W.msgs[:m], W.pks[:m], threads=1)
+    dt1 = time.perf_counter() - t0
+    mism1 = int((s_st != status[:m]).sum() + (s_out != out[:m]).any(axis=1).sum())
     return {"value": sample / dt, "unit": "sigs/s", "cores": threads, "kind": "port",
-            "sample": f"first {sample} items of the batch (same mix), {dt:.1f} s", "bit_exact_vs_gpu": mism == 0, "mismatches": mism}
+            "sample": f"first {sample} items of the batch (same mix), {dt:.1f} s", "bit_exact_vs_gpu": mism == 0, "mismatches": mism,
+            "serial_1core": {"value": m / dt1, "unit": "sigs/s", "cores": 1, "sample": f"first {m} items, one thread, {dt1:.1f} s",
+                             "bit_exact_vs_gpu": mism1 == 0}}
 
 
 if __name__ == "__main__":

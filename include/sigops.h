@@ -185,17 +185,25 @@ int sigops_verify_mixed_device(sigops_ctx* ctx, const uint8_t* d_curves, const u
  * cudaFree: its scratch (counters and per-curve index lists), the generator
  * tables and its error word are file-scope static device arrays, which every
  * GPU that loads the library holds until the process exits (about 10 MiB,
- * mostly the generator tables).
+ * mostly the generator tables, separate from any context's tables).
  * Limit: n <= SIGOPS_NOALLOC_MAX_ITEMS, else SIGOPS_E_RANGE.  Buffers and
  * results as sigops_verify_mixed_device: device pointers (16-byte aligned)
  * on the current device, work queued on `stream`, no host synchronisation.
  * The first call on each device does a one-time set-up (symbol addresses,
- * table upload): make that first call before any stream capture.  Every call
- * shares the static scratch and clears the counters it uses, so calls whose
- * work overlaps on the GPU race: serialise them. */
+ * table upload, one device synchronisation): make that first call before any
+ * stream capture.  Every call shares the static scratch and clears the
+ * counters it uses, so calls whose work overlaps on the GPU race: serialise
+ * them. */
 #define SIGOPS_NOALLOC_MAX_ITEMS 65536
 int sigops_verify_mixed_noalloc(const uint8_t* d_curves, const uint8_t* d_sigs, const uint8_t* d_msgs, const uint8_t* d_pks, size_t n,
                                 uint8_t* d_out, uint8_t* d_status, void* stream);
+
+/* Device-side errors of the allocation-free calls on the current device: reads
+ * the static error word after the work queued on `stream`, waits for that
+ * read, and clears the word.  SIGOPS_OK, or SIGOPS_E_TIMEDOUT when a bounded
+ * device wait of an earlier call expired.  Allocates nothing.  No
+ * counterpart in the reference. */
+int sigops_noalloc_status(void* stream);
 
 /* Size the context's batched-engine scratch for batches of up to n items. */
 int sigops_reserve(sigops_ctx* ctx, size_t n);

@@ -83,3 +83,12 @@ def test_mixed_batch_size_limit(lib):
     assert L.lib.sigops_verify_mixed(None, buf, buf, buf, buf, n, buf, buf) == L.SIGOPS_E_RANGE
     assert b"32-bit" in L.lib.sigops_last_error()
     assert L.lib.sigops_verify_mixed_device(None, buf, buf, buf, buf, n, buf, buf, None) == L.SIGOPS_E_RANGE
+
+
+def test_rust_binding_covers_header():
+    """The Rust crate's raw declarations (wgpu-sigops_gb300/rust/src/ffi.rs,
+    not compiled here: no Rust toolchain) name every function the header
+    declares, and no other."""
+    src = open(os.path.join(ROOT, "wgpu-sigops_gb300", "rust", "src", "ffi.rs")).read()
+    rust = set(re.findall(r"\bpub fn (sigops_[a-z0-9_]+)\s*\(", src))
+    assert rust == set(declared_symbols())

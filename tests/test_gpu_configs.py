@@ -1,8 +1,8 @@
 """The benchmark configurations at full size: bit-exact against the C oracle
 (c1 1,024 secp256k1; c2 65,536 ed25519 with 3% tampered; c3 262,144 P-256
 with 1% r that has no curve point), and the 1,048,576-item mixed batch through
-size-independent checks (every item's known outcome, plain == batched) plus an
-oracle sample."""
+generator-known outcomes, plain == batched, and the C oracle on every one of
+its items."""
 import numpy as np
 import pytest
 
@@ -68,7 +68,7 @@ def test_c4_mixed_1m(w):
         sel = np.nonzero(W.curves == c)[0][:50000]
         keys, s2 = mod.ecrecover_arrays(W.sigs[sel], W.msgs[sel])
         assert (keys == out[sel]).all() and (s2 == st[sel]).all()
-    # oracle on a sample
-    idx = np.random.default_rng(1).choice(W.n, 20000, replace=False)
-    o_out, o_st = c_oracle.batch_mixed(W.curves[idx], W.sigs[idx], W.msgs[idx], W.pks[idx])
-    assert (o_st == st[idx]).all() and (o_out == out[idx]).all()
+    # the C oracle on all 1,048,576 items (all host threads)
+    o_out, o_st = c_oracle.batch_mixed(W.curves, W.sigs, W.msgs, W.pks)
+    bad = np.nonzero((o_st != st) | (o_out != out).any(axis=1))[0]
+    assert len(bad) == 0, f"{len(bad)} items differ from the oracle, first {bad[:5].tolist()}"

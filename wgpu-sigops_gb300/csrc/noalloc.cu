@@ -8,20 +8,28 @@
 // them: it needs no context and calls no cudaMalloc / cudaFree.  Its scratch
 // (per-curve counters and index lists), the generator tables and the device
 // error word live in the file-scope static __device__ arrays below, which every
-// GPU that loads the library holds until the process exits
-// (about 0.8 MiB for the scratch, 36 KiB for the tables).
+// GPU that loads the library holds until the process exits: about 0.75 MiB of
+// scratch and 9 MiB of generator tables (16-bit windows: 4 MiB for secp256k1
+// with its 2^128 G half, 2 MiB for P-256, 3 MiB for ed25519).  These arrays
+// are separate from the tables each context allocates; under
+// CUDA_MODULE_LOADING=EAGER every GPU of the process holds them even when this
+// entry point is never called (under the default lazy loading, from the first
+// use of the module's kernels).
 //
 // The first call on each device performs a one-time set-up with that device
 // current: cudaGetSymbolAddress for each array (host code must not use the
 // arrays' names as device addresses: on the host they are only stand-ins) and
-// an upload of the tables with cudaMemcpyToSymbol.  Make that first call before
-// any stream capture.  All calls share the arrays and each call clears the
-// counters it needs, so calls whose work overlaps on the GPU (different
-// streams, or different host threads) race with each other: serialise them.
+// an upload of the tables with cudaMemcpyToSymbol, followed by a device
+// synchronisation so that no kernel on a non-blocking stream can read a table
+// before it has landed.  Make that first call before any stream capture.  All
+// calls share the arrays and each call clears the counters it needs, so calls
+// whose work overlaps on the GPU (different streams, or different host
+// threads) race with each other: serialise them.  A device-side error of these
+// calls sets the static error word; sigops_noalloc_status reads and clears it.
 #include <cuda_runtime.h>
 
+#include <deque>
 #include <mutex>
-#include <vector>
 
 #include "../../include/sigops.h"
 #include "batched.cuh"
@@ -51,16 +59,18 @@ struct DeviceSetup {
   int num_sms = 0;
 };
 
+// one record per device; a deque never moves its elements when it grows, and
+// callers get a copy taken under the lock
 std::mutex g_mu;
-std::vector<DeviceSetup> g_dev;
+std::deque<DeviceSetup> g_dev;
 
 // once per device, with the device current; allocates no device memory
-int setup(int device, DeviceSetup** out) {
+int setup(int device, DeviceSetup* out) {
   std::lock_guard<std::mutex> g(g_mu);
-  if ((int)g_dev.size() <= device) g_dev.resize(device + 1);
+  while ((int)g_dev.size() <= device) g_dev.emplace_back();
   DeviceSetup& d = g_dev[device];
   if (d.ready) {
-    *out = &d;
+    *out = d;
     return SIGOPS_OK;
   }
   if (cudaGetSymbolAddress((void**)&d.scratch, g_noalloc_scratch) != cudaSuccess) return SIGOPS_E_CUDA;
@@ -77,12 +87,15 @@ int setup(int device, DeviceSetup** out) {
       cudaMemcpyToSymbol(g_noalloc_tab_ed, h.tab[2].data(), sizeof g_noalloc_tab_ed) != cudaSuccess ||
       cudaMemcpyToSymbol(g_noalloc_err, &zero, sizeof zero) != cudaSuccess)
     return SIGOPS_E_CUDA;
+  // a pageable upload may return before its data has landed, and the first
+  // launch may go to a non-blocking stream that does not wait for it
+  if (cudaDeviceSynchronize() != cudaSuccess) return SIGOPS_E_CUDA;
   if (cudaDeviceGetAttribute(&d.num_sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return SIGOPS_E_CUDA;
   int bps = sg::batched_max_blocks_per_sm(kVariant);
   if (bps <= 0) return SIGOPS_E_CUDA;
   d.grid = d.num_sms * bps;
   d.ready = true;
-  *out = &d;
+  *out = d;
   return SIGOPS_OK;
 }
 
@@ -97,14 +110,33 @@ extern "C" int sigops_verify_mixed_noalloc(const uint8_t* d_curves, const uint8_
   if (misaligned(d_sigs) || misaligned(d_msgs) || misaligned(d_pks) || misaligned(d_out)) return SIGOPS_E_INVAL;
   int device = 0;
   if (cudaGetDevice(&device) != cudaSuccess) return SIGOPS_E_NODEV;
-  DeviceSetup* d = nullptr;
+  DeviceSetup d;
   int rc = setup(device, &d);
   if (rc != SIGOPS_OK) return rc;
   const size_t cg = (n + 255) / 256;
-  const int classify_grid = (int)(cg < (size_t)d->num_sms * 8 ? cg : (size_t)d->num_sms * 8);
+  const int classify_grid = (int)(cg < (size_t)d.num_sms * 8 ? cg : (size_t)d.num_sms * 8);
   // the per-curve index lists follow the counters; launch_batched clears the counters
-  uint32_t* idx = reinterpret_cast<uint32_t*>(d->scratch + kScratchHead);
-  cudaError_t e = sg::launch_batched(d_curves, d_sigs, d_msgs, d_pks, n, d_out, d_status, idx, d->scratch, d->tab[0], d->tab[1], d->tab[2],
-                                     d->err, d->grid, kVariant, classify_grid, nullptr, (cudaStream_t)stream);
+  uint32_t* idx = reinterpret_cast<uint32_t*>(d.scratch + kScratchHead);
+  cudaError_t e = sg::launch_batched(d_curves, d_sigs, d_msgs, d_pks, n, d_out, d_status, idx, d.scratch, d.tab[0], d.tab[1], d.tab[2],
+                                     d.err, d.grid, kVariant, classify_grid, nullptr, (cudaStream_t)stream);
   return e == cudaSuccess ? SIGOPS_OK : SIGOPS_E_CUDA;
+}
+
+extern "C" int sigops_noalloc_status(void* stream) {
+  int device = 0;
+  if (cudaGetDevice(&device) != cudaSuccess) return SIGOPS_E_NODEV;
+  DeviceSetup d;
+  {
+    std::lock_guard<std::mutex> g(g_mu);
+    if (device >= (int)g_dev.size() || !g_dev[device].ready) return SIGOPS_OK;  // no call has run on this device
+    d = g_dev[device];
+  }
+  // read after the work queued on `stream`, then clear when set
+  uint32_t e = 0;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (cudaMemcpyAsync(&e, d.err, sizeof e, cudaMemcpyDeviceToHost, s) != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess)
+    return SIGOPS_E_CUDA;
+  if (e == 0) return SIGOPS_OK;
+  if (cudaMemsetAsync(d.err, 0, sizeof e, s) != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess) return SIGOPS_E_CUDA;
+  return SIGOPS_E_TIMEDOUT;
 }

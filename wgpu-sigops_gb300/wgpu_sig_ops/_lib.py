@@ -54,6 +54,7 @@ SIGNATURES = {
     "sigops_verify_mixed_device": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _sz, _vp, _vp, _vp]),
     "sigops_reserve": (ctypes.c_int, [_vp, _sz]),
     "sigops_verify_mixed_noalloc": (ctypes.c_int, [_vp, _vp, _vp, _vp, _sz, _vp, _vp, _vp]),
+    "sigops_noalloc_status": (ctypes.c_int, [_vp]),
     "sigops_mixed_plan_create": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _sz, _vp, _vp, ctypes.POINTER(_vp)]),
     "sigops_mixed_plan_launch": (ctypes.c_int, [_vp, _vp]),
     "sigops_mixed_plan_destroy": (None, [_vp]),
