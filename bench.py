@@ -391,8 +391,10 @@ def main():
     ms_step = dist.max(statistics.mean(ms_b))
     value = dist.sum(n) / (ms_step * 1e-3)
     plain_ms = dist.max(statistics.mean(ms_p))
-    # the batched engine runs secp256k1 with the GLV split
-    work = wm["secp256k1_glv"] * counts[0] + wm["secp256r1"] * counts[1] + wm["ed25519"] * counts[2]
+    # the batched engine runs secp256k1 with the GLV split; its single-curve
+    # variants share the inversions of r and of the result's Z across items
+    wmb = wm["batched"] if split else wm
+    work = wmb["secp256k1_glv"] * counts[0] + wmb["secp256r1"] * counts[1] + wmb["ed25519"] * counts[2]
     achieved = work / (ms_step * 1e-3)
 
     traffic = None
@@ -436,9 +438,9 @@ def main():
                      "peak_source": ("measured in-process: mad.lo.cc/madc.hi.cc carry-chain rows, the form the field "
                                      "multiplications issue (MEASURED_PEAKS.json has no integer figure)"),
                      "peak_forms_T_per_s": {k: v / 1e12 for k, v in mul_forms.items()},
-                     "work_model": ("32-bit multiply instructions per signature, counted by the host build of the kernel source: "
-                                    f"secp256k1 (GLV) {wm['secp256k1_glv']:.0f}, P-256 {wm['secp256r1']:.0f}, "
-                                    f"ed25519 {wm['ed25519']:.0f} (profiles/work_model.json)")},
+                     "work_model": ("32-bit multiply instructions per signature of the batched path, counted by the host build of "
+                                    f"the kernel source: secp256k1 (GLV) {wmb['secp256k1_glv']:.0f}, P-256 {wmb['secp256r1']:.0f}, "
+                                    f"ed25519 {wmb['ed25519']:.0f} (profiles/work_model.json)")},
         "e2e": e2e,
         "serving": serving,
         "cpu_baseline": cpu,

@@ -260,3 +260,97 @@ extern "C" void hc_divstep_inv(const uint8_t* x, const uint8_t* m, uint32_t minv
   }
   *batches_used = used;
 }
+
+// The batched engine's single-curve path with its shared inversions, on the
+// host: one curve's n items, thread t of T = ceil(n / batch) taking items
+// t, t + T, ... as rinv_kernel / finish_kernel do; r^-1 by simultaneous
+// inversion, the curve step to the projective result, then the simultaneous
+// inversion of Z and the key bytes (ECDSA) or the R comparison (ed25519).
+// out: n x 64 mixed records, status: n.
+template <class T, bool GLV>
+static void deferred_ecdsa(const uint8_t* sigs, const uint8_t* msgs, size_t n, int batch, const uint32_t* gtab, uint8_t* out,
+                           uint8_t* status) {
+  using S = typename T::S;
+  using F = typename T::F;
+  const size_t nt = (n + batch - 1) / batch;
+  std::vector<u256> rinv(n), v(batch), pre(batch);
+  std::vector<JPoint> q(n);
+  for (size_t t = 0; t < nt; ++t) {
+    int m = 0;
+    for (; m < batch && t + m * nt < n; ++m) {
+      uint32_t s[16];
+      memcpy(s, sigs + 64 * (t + m * nt), 64);
+      v[m] = ecdsa_r_factor<T>(s);
+    }
+    batch_invert<S>(v.data(), pre.data(), m, [](const u256& x) { return S::from_int(S::inv_int(S::to_int(x))); });
+    for (int j = 0; j < m; ++j) rinv[t + j * nt] = v[j];
+  }
+  for (size_t i = 0; i < n; ++i) {
+    uint32_t s[16], mw[8];
+    memcpy(s, sigs + 64 * i, 64);
+    memcpy(mw, msgs + 32 * i, 32);
+    u256 r, sv, z;
+    APoint R;
+    uint8_t st = ecdsa_prepare<T>(s, mw, r, sv, z, R);
+    if (st == ST_OK) st = ecdsa_key_jacobian<T, GLV>(sv, z, R, rinv[i], gtab, q[i]);
+    status[i] = st;
+    memset(out + 64 * i, 0, 64);
+  }
+  std::vector<size_t> item(batch);
+  for (size_t t = 0; t < nt; ++t) {
+    int m = 0;
+    for (int j = 0; j < batch && t + j * nt < n; ++j) {
+      const size_t i = t + j * nt;
+      if (status[i] != ST_OK) continue;
+      item[m] = i;
+      v[m++] = q[i].Z;
+    }
+    if (!m) continue;
+    batch_invert<F>(v.data(), pre.data(), m, [](const u256& x) { return F::inv(x); });
+    for (int j = 0; j < m; ++j) {
+      uint32_t o[16];
+      ecdsa_encode_key<T>(q[item[j]], v[j], o);
+      memcpy(out + 64 * item[j], o, 64);
+    }
+  }
+}
+
+static void deferred_ed(const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks, size_t n, int batch, uint8_t* out, uint8_t* status) {
+  const size_t nt = (n + batch - 1) / batch;
+  std::vector<EPoint> rp(n);
+  std::vector<u256> v(batch), pre(batch);
+  for (size_t i = 0; i < n; ++i) {
+    uint32_t s[16], mw[8], p[8];
+    memcpy(s, sigs + 64 * i, 64);
+    memcpy(mw, msgs + 32 * i, 32);
+    memcpy(p, pks + 32 * i, 32);
+    status[i] = ed25519_point(s, mw, p, g_ed, rp[i]);
+    memset(out + 64 * i, 0, 64);
+  }
+  std::vector<size_t> item(batch);
+  for (size_t t = 0; t < nt; ++t) {
+    int m = 0;
+    for (int j = 0; j < batch && t + j * nt < n; ++j) {
+      const size_t i = t + j * nt;
+      if (status[i] != ST_OK) continue;
+      item[m] = i;
+      v[m++] = rp[i].Z;
+    }
+    if (!m) continue;
+    batch_invert<FpEd>(v.data(), pre.data(), m, [](const u256& x) { return FpEd::inv(x); });
+    for (int j = 0; j < m; ++j) {
+      uint32_t s[16];
+      memcpy(s, sigs + 64 * item[j], 64);
+      status[item[j]] = ed25519_compare(rp[item[j]], v[j], s);
+      out[64 * item[j]] = status[item[j]] == ST_OK;
+    }
+  }
+}
+
+extern "C" void hc_batched_deferred(int curve, const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks, size_t n, int batch,
+                                    uint8_t* out, uint8_t* status) {
+  init();
+  if (curve == 0) deferred_ecdsa<K1Traits, true>(sigs, msgs, n, batch, g_k1, out, status);
+  else if (curve == 1) deferred_ecdsa<R1Traits, false>(sigs, msgs, n, batch, g_r1, out, status);
+  else deferred_ed(sigs, msgs, pks, n, batch, out, status);
+}

@@ -60,6 +60,22 @@ def compute() -> dict:
         "ed25519": per_sig(hc.hc_ed_verify, ed, lambda v: (bytes.fromhex(v["sig"]), bytes.fromhex(v["msg"]), bytes.fromhex(v["pubkey"]))),
         "samples": {"secp256k1": len(k1), "secp256r1": len(r1), "ed25519": len(ed)},
     }
+    # the batched engine's single-curve path: r^-1 and Z^-1 by simultaneous
+    # inversion over 16 items per thread (its INV_BATCH), counted per item
+    def per_sig_batched(curve, items):
+        n = len(items)
+        sigs = b"".join(bytes.fromhex(v["sig"]) for v in items)
+        msgs = b"".join(bytes.fromhex(v["msg"]) for v in items)
+        pks = b"".join(bytes.fromhex(v["pubkey"]) if curve == 2 else bytes(32) for v in items)
+        o = ctypes.create_string_buffer(64 * n)
+        st = ctypes.create_string_buffer(n)
+        hc.hc_mulcount(1)
+        hc.hc_batched_deferred(curve, sigs, msgs, pks, ctypes.c_size_t(n), 16, o, st)
+        assert st.raw == bytes(n), "work model uses valid signatures only"
+        return hc.hc_mulcount(1) / n
+
+    model["batched"] = {"secp256k1_glv": per_sig_batched(0, k1), "secp256r1": per_sig_batched(1, r1), "ed25519": per_sig_batched(2, ed),
+                        "inv_batch": 16}
     a = bytes(range(32))
     hc.hc_mulcount(1)
     hc.hc_sqr_wide(a, out)

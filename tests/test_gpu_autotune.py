@@ -20,6 +20,12 @@ def test_autotune_selects_and_caches(tmp_path, monkeypatch):
     before = w.batch.verify_mixed(W.curves, W.sigs, W.msgs, W.pks, ctx=ctx)
     rep = ctx.autotune(probe_items=152 * 256)
     assert len(rep["chosen"]) == 4 and "batched" in rep
+    # per curve: every configuration timed, with its launch shape and window widths
+    for curve in ("secp256k1", "secp256r1", "ed25519"):
+        cfgs = rep["curve_configs"][curve]
+        assert len(cfgs) == 8
+        assert {c["wr"] for c in cfgs.values()} == {4, 5, 6} and {c["wg"] for c in cfgs.values()} == {8, 16}
+        assert {c["block"] for c in cfgs.values()} == {64, 128, 256, 512}
     v = ctx.variants()
     assert [v[k]["variant"] for k in ("plain_secp256k1", "plain_secp256r1", "plain_ed25519", "batched")] == rep["chosen"]
     after = w.batch.verify_mixed(W.curves, W.sigs, W.msgs, W.pks, ctx=ctx)

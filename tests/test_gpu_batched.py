@@ -109,10 +109,17 @@ def test_matches_plain_kernels(w):
     assert (valid == out[sel, 0]).all() and (st == status[sel]).all()
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 4 + 1 + 4 * 2 + 16 * 3, 4 + 3 + 4 * 3 + 16 * 3, 4 + 2 + 4 * 1 + 16 * 0, 67])
+# single-curve variant 4 + a + 8 b + 64 c: each curve in every one of its eight
+# configurations (launch shapes, per-point windows 4 / 5 / 6, generator
+# windows 16 / 8 with the table staged into shared memory)
+SPLIT = [4 + k + 8 * ((k + 1) % 8) + 64 * ((k + 2) % 8) for k in range(8)]
+
+
+@pytest.mark.parametrize("variant", [0, 1, 2, 3] + SPLIT)
 def test_every_launch_variant(w, variant):
-    """Fused (0..3) and single-curve (4..67) variants give the oracle's results,
-    on a mixed batch and on ragged ones that leave some curves empty."""
+    """Fused (0..3) and single-curve (4..515) variants give the oracle's
+    results, on a mixed batch and on ragged ones that leave some curves
+    empty."""
     ctx = w.Context(0)
     ctx.set_variant(3, variant)
     assert ctx.variants()["batched"]["variant"] == variant
@@ -124,7 +131,7 @@ def test_every_launch_variant(w, variant):
     ctx.close()
 
 
-@pytest.mark.parametrize("variant", [0, 67])
+@pytest.mark.parametrize("variant", [0, 515])
 def test_graph_plan_replays(w, variant):
     import torch
 

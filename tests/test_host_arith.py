@@ -87,11 +87,15 @@ def test_canonical_boundaries(hc, field):
                 assert int.from_bytes(out.raw, "little") == f(a, b), (op, hex(a), hex(b))
 
 
+# the P-256 field is held in Montgomery form: its reduction returns t 2^-256 mod p
+R1_RINV = pow(2**256, -1, o.SECP256R1.p)
+
+
 def test_p256_reduction(hc):
-    """The P-256 reduction on products of field elements and on extreme
-    512-bit values (all ones, single high words), where the signed column
-    sums and the folded top word reach their bounds: below 2^256 (weakly
-    reduced) and equal mod p."""
+    """The P-256 Montgomery reduction on products of field elements and on
+    extreme 512-bit values (all ones, single high words), where the held-back
+    round carries and the final fold reach their bounds: below 2^256 (weakly
+    reduced) and equal to t 2^-256 mod p."""
     p = o.SECP256R1.p
     rng = random.Random(70)
     xs = [0, 1, p, p * p, (p - 1) * (p - 1), 2**512 - 1, 2**511, (2**256 - 1) * (2**256 - 1)]
@@ -101,7 +105,7 @@ def test_p256_reduction(hc):
     for x in xs:
         hc.hc_r1_reduce(x.to_bytes(64, "little"), out)
         r = int.from_bytes(out.raw, "little")
-        assert r < 2**256 and r % p == x % p, hex(x)
+        assert r < 2**256 and r % p == x * R1_RINV % p, hex(x)
 
 
 def test_sqr_wide(hc):
@@ -188,7 +192,8 @@ def test_random_vs_oracle(hc):
 
 
 def test_kernel_tables(hc):
-    """The device tables hold (i+1)*G for every entry (affine integers); the
+    """The device tables hold (i+1)*G for every entry (affine, in the field's
+    representation: integers for secp256k1, Montgomery form for P-256); the
     secp256k1 table continues with (i+1)*2^128*G (GLV)."""
     ne, ned = hc.hc_gtab_entries(0), hc.hc_gtab_entries(1)
     assert ne == ned == 1 << 15  # generator windows of 16 bits
@@ -201,6 +206,8 @@ def test_kernel_tables(hc):
                 e = h * ne + i
                 x = sum(words[e * 16 + k] << (32 * k) for k in range(8))
                 y = sum(words[e * 16 + 8 + k] << (32 * k) for k in range(8))
+                if curve == 1:
+                    x, y = x * R1_RINV % c.p, y * R1_RINV % c.p
                 assert (x, y) == o.ws_mul(c, (i + 1) << (128 * h), c.g), (curve, h, i)
     buf = (ctypes.c_uint32 * (ned * 24))()
     hc.hc_gtab(2, buf)
@@ -257,7 +264,7 @@ def test_k1_glv_vs_oracle(hc):
 def test_reduce_512(hc, field):
     """Reduction of 512-bit values, including those whose folds carry out of
     2^256 again (low half near 2^256, high half extreme): below 2^256, equal
-    mod p."""
+    mod p (P-256: equal to x 2^-256 mod p, its Montgomery reduction)."""
     p = [o.SECP256K1.p, o.SECP256R1.p, o.ED_P][field]
     top = 2**256
     rng = random.Random(90 + field)
@@ -279,7 +286,7 @@ def test_reduce_512(hc, field):
     for x in xs:
         hc.hc_reduce(field, x.to_bytes(64, "little"), out)
         r = int.from_bytes(out.raw, "little")
-        assert r < top and r % p == x % p, hex(x)
+        assert r < top and r % p == (x * R1_RINV if field == 1 else x) % p, hex(x)
 
 
 @pytest.mark.parametrize("field", [0, 1, 2], ids=["secp256k1", "secp256r1", "ed25519"])
@@ -312,9 +319,11 @@ def test_weak_reduction(hc, field):
         edge = [0, 1, 18, 19, 37, 38, 39, p - 1, p, p + 1, p + 37, 2**255, top - 1, top - 2, top - 37, top - 38, top - 39, top - 76]
     rng = random.Random(41 + field)
     vals = edge + [rng.getrandbits(256) for _ in range(30)]
+    mscale = R1_RINV if field == 1 else 1  # P-256 multiplies in Montgomery form
     for a in vals:
         for b in vals:
-            ops = [(0, lambda a, b: a + b), (1, lambda a, b: a - b), (2, lambda a, b: a * b), (3, lambda a, b: a * a), (4, lambda a, b: -a)]
+            ops = [(0, lambda a, b: a + b), (1, lambda a, b: a - b), (2, lambda a, b: a * b * mscale), (3, lambda a, b: a * a * mscale),
+                   (4, lambda a, b: -a)]
             if field < 2:
                 ops.append((6, lambda a, b: a * pow(2, -1, p)))
             for op, f in ops:
@@ -395,3 +404,33 @@ def test_weierstrass_exceptional_cases(hc, curve):
         if B is not None:  # mixed add: Q affine, never infinity
             assert run(1, A, za, B, 1) == add_ref(A, B)
         assert run(2, A, za, None, 0) == add_ref(A, A)
+
+
+@pytest.mark.parametrize("curve", [0, 1, 2], ids=["secp256k1", "secp256r1", "ed25519"])
+@pytest.mark.parametrize("batch", [1, 3, 16])
+def test_batched_shared_inversions(hc, curve, batch):
+    """The batched engine's single-curve path (r^-1 and the result's Z^-1 by
+    simultaneous inversion over a thread's items), host build, on golden and
+    tampered items: every record and status equals the oracle's, including
+    threads whose items all fail (nothing to invert) and sizes that leave the
+    last threads short."""
+    from tests.golden_io import load
+
+    G2 = load()
+    name = ["secp256k1", "secp256r1", "ed25519"][curve]
+    vecs = G2[name] + (G2.get(name + "_edge", []) if curve < 2 else [])
+    sigs = b"".join(bytes.fromhex(v["sig"]) for v in vecs)
+    msgs = b"".join(bytes.fromhex(v["msg"]) for v in vecs)
+    pks = b"".join(bytes.fromhex(v["pubkey"]) if curve == 2 else bytes(32) for v in vecs)
+    n = len(vecs)
+    for m in (n, 1, 17, min(n, 33)):
+        out = ctypes.create_string_buffer(64 * m)
+        st = ctypes.create_string_buffer(m)
+        hc.hc_batched_deferred(curve, sigs[:64 * m], msgs[:32 * m], pks[:32 * m], ctypes.c_size_t(m), batch, out, st)
+        for k in range(m):
+            v = vecs[k]
+            if curve == 2:
+                exp = bytes([1 if v["valid"] else 0]) + bytes(63)
+            else:
+                exp = bytes.fromhex(v["pubkey"]) if v["pubkey"] else bytes(64)
+            assert (out.raw[64 * k:64 * k + 64], st.raw[k]) == (exp, v["status"]), (m, k)

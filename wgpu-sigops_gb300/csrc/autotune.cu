@@ -9,10 +9,11 @@
 // mix: items are interleaved 4:3:3), then the twelve fastest again on the whole
 // probe, best of three.  The ranking of the concurrent single-curve kernels
 // depends on the batch size, so the probe should be as large as the batches
-// the caller runs.  The search space is the compiled variants: block shape and
-// register budget.  Window widths are fixed at compile time (5 bits for the
-// per-signature point, 8 for the generator tables), chosen by the
-// operation-count model.
+// the caller runs.  The search space is the compiled variants: for each curve,
+// block shape and register budget (256 x 1, 128 x 3, 256 x 2, 64, 512 x 1),
+// per-point window width (4, 5, 6 bits) and generator window width (16 bits
+// with tables in global memory, 8 bits with tables staged into shared memory
+// by a bulk copy); the fused mixed-curve kernel in four shapes.
 //
 // Results can be kept in a cache file (SIGOPS_TUNE_CACHE, one line per device
 // name and SM count) that sigops_create reads back.
@@ -152,7 +153,7 @@ extern "C" int sigops_autotune(sigops_ctx* ctx, size_t probe_items, char* report
   const size_t o_cur = 0, o_sec = pad, o_non = o_sec + n * 32, o_msg = o_non + n * 32, o_seed = o_msg + n * 32,
                o_sig = o_seed + n * 32, o_pub = o_sig + n * 64, o_pk = o_pub + n * 64, o_out = o_pk + n * 32, o_st = o_out + n * 64,
                o_idx = o_st + pad, o_scr = o_idx + 3 * n * 4, o_perm = o_scr + 256, o_icur = o_perm + 4 * pad, o_isig = o_icur + pad,
-               o_imsg = o_isig + n * 64, o_ipk = o_imsg + n * 32, total = o_ipk + n * 32;
+               o_imsg = o_isig + n * 64, o_ipk = o_imsg + n * 32, o_def = o_ipk + n * 32, total = o_def + sg::batched_defer_bytes(n);
   if (cudaMalloc(&d.p, total) != cudaSuccess) return SIGOPS_E_NOMEM;
   cudaStream_t st;
   if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return SIGOPS_E_CUDA;
@@ -190,6 +191,8 @@ extern "C" int sigops_autotune(sigops_ctx* ctx, size_t probe_items, char* report
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
+  auto off_of = [&](int c) { return c == 0 ? (size_t)0 : c == 1 ? n1 : n1 + n2; };
+  auto cnt_of = [&](int c) { return c == 0 ? n1 : c == 1 ? n2 : n3; };
   auto time_it = [&](auto&& launch, int reps = 3) -> float {
     launch();
     float best = 1e30f;
@@ -206,29 +209,68 @@ extern "C" int sigops_autotune(sigops_ctx* ctx, size_t probe_items, char* report
   };
   std::string rep = "{";
   int chosen[4] = {0, 0, 0, 0};
-  // batched engine: stage 1, every variant once on a prefix of the interleaved
-  // probe; stage 2, the twelve fastest on the whole probe, best of three
+  // batched engine.  Stage 0: each curve's single-curve pipeline alone, in
+  // each of its configurations (launch shape, register budget, window widths),
+  // on that curve's items of the probe.  Stage 1: the fused variants and every
+  // combination of the three best configurations per curve once on a prefix of
+  // the interleaved probe.  Stage 2: the twelve fastest on the whole probe,
+  // best of three.
   {
     const size_t n_short = std::min(n, (size_t)v.num_sms * 256 * 8);
-    auto run_batched = [&](int var, size_t items) {
+    auto run_batched = [&](int var, size_t first, size_t items, bool interleaved, int reps) {
       const int grid = v.num_sms * sg::batched_max_blocks_per_sm(var);
       const int classify_grid = (int)std::min((items + 255) / 256, (size_t)v.num_sms * 8);
+      const size_t ic = interleaved ? o_icur : o_cur, is = interleaved ? o_isig : o_sig, im = interleaved ? o_imsg : o_msg,
+                   ip = interleaved ? o_ipk : o_pk;
       return time_it(
           [&] {
-            sg::launch_batched(d.p + o_icur, d.p + o_isig, d.p + o_imsg, d.p + o_ipk, items, d.p + o_out, d.p + o_st,
-                               (uint32_t*)(d.p + o_idx), d.p + o_scr, v.gtab[0], v.gtab[1], v.gtab[2], v.d_err, grid, var, classify_grid,
+            sg::launch_batched(d.p + ic + first, d.p + is + first * 64, d.p + im + first * 32, d.p + ip + first * 32, items, d.p + o_out,
+                               d.p + o_st, (uint32_t*)(d.p + o_idx), d.p + o_scr, d.p + o_def, v.tabs, v.d_err, grid, var, classify_grid,
                                &fork, st);
           },
-          items == n ? 3 : 1);
+          reps);
     };
+    static const char* kCurve[3] = {"secp256k1", "secp256r1", "ed25519"};
+    rep += "\"curve_configs\": {";
+    std::vector<int> best_cfg[3];
+    for (int c = 0; c < 3; ++c) {
+      std::vector<std::pair<float, int>> times;
+      char b[160];
+      snprintf(b, sizeof b, "%s\"%s\": {", c ? ", " : "", kCurve[c]);
+      rep += b;
+      bool firstc = true;
+      for (int cfg = 0; cfg < sg::CURVE_CONFIGS; ++cfg) {
+        const int var = sg::split_variant(cfg, cfg, cfg);  // the other curves have no items here
+        if (sg::curve_config_occupancy(c, cfg) <= 0 || cnt_of(c) == 0) continue;
+        const float ms = run_batched(var, off_of(c), cnt_of(c), false, 2);
+        times.push_back({ms, cfg});
+        int wr, wg;
+        sg::curve_config_windows(cfg, &wr, &wg);
+        snprintf(b, sizeof b, "%s\"%d\": {\"ms\": %.3f, \"block\": %d, \"blocks_per_sm\": %d, \"wr\": %d, \"wg\": %d}",
+                 firstc ? "" : ", ", cfg, ms, sg::curve_config_block(cfg), sg::curve_config_occupancy(c, cfg), wr, wg);
+        firstc = false;
+        rep += b;
+      }
+      rep += "}";
+      std::sort(times.begin(), times.end());
+      for (size_t k = 0; k < times.size() && k < 3; ++k) best_cfg[c].push_back(times[k].second);
+      if (best_cfg[c].empty()) best_cfg[c].push_back(2);
+    }
+    rep += "}";
+    std::vector<int> cands = {0, 1, 2, 3};
+    for (int a : best_cfg[0])
+      for (int b : best_cfg[1])
+        for (int c : best_cfg[2]) cands.push_back(sg::split_variant(a, b, c));
     std::vector<std::pair<float, int>> stage1;
-    rep += "\"batched\": {";
-    for (int var = 0; var < sg::BATCHED_VARIANTS; ++var) {
+    rep += ", \"batched\": {";
+    bool firstc = true;
+    for (int var : cands) {
       if (sg::batched_max_blocks_per_sm(var) <= 0) continue;
-      const float ms = run_batched(var, n_short);
+      const float ms = run_batched(var, 0, n_short, true, 1);
       stage1.push_back({ms, var});
       char b[96];
-      snprintf(b, sizeof b, "%s\"%d\": %.3f", var ? ", " : "", var, ms);
+      snprintf(b, sizeof b, "%s\"%d\": %.3f", firstc ? "" : ", ", var, ms);
+      firstc = false;
       rep += b;
     }
     rep += "}";
@@ -238,7 +280,7 @@ extern "C" int sigops_autotune(sigops_ctx* ctx, size_t probe_items, char* report
     const size_t keep = std::min<size_t>(stage1.size(), 12);
     for (size_t k = 0; k < keep; ++k) {
       const int var = stage1[k].second;
-      const float ms = n == n_short ? stage1[k].first : run_batched(var, n);
+      const float ms = n == n_short ? stage1[k].first : run_batched(var, 0, n, true, 3);
       char b[96];
       snprintf(b, sizeof b, "%s\"%d\": %.3f", k ? ", " : "", var, ms);
       rep += b;
@@ -248,6 +290,12 @@ extern "C" int sigops_autotune(sigops_ctx* ctx, size_t probe_items, char* report
       }
     }
     rep += "}";
+    if (chosen[3] >= sg::BATCHED_FUSED_VARIANTS) {
+      char b[96];
+      snprintf(b, sizeof b, ", \"chosen_configs\": [%d, %d, %d]", sg::split_config(chosen[3], 0), sg::split_config(chosen[3], 1),
+               sg::split_config(chosen[3], 2));
+      rep += b;
+    }
   }
   // plain kernels per curve
   const size_t off[3] = {0, n1, n1 + n2}, cnt[3] = {n1, n2, n3};

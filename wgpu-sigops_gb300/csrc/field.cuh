@@ -8,7 +8,7 @@
 //
 //  * FpK1  p = 2^256 - 2^32 - 977   special-form fold (2^256 = 2^32 + 977)
 //  * FpEd  p = 2^255 - 19           special-form fold (2^256 = 38)
-//  * FpR1  p = NIST P-256           NIST fast reduction (signed word columns)
+//  * FpR1  p = NIST P-256           Montgomery form, multiply-free reduction rounds
 //  * Mont<...> generic Montgomery (CIOS) for the scalar fields mod n and mod l
 //
 // The reference does all of this with 13-bit limbs: Barrett `ff_mul`
@@ -483,54 +483,47 @@ using ScR1 = Mont<R1ScalarC>;
 using ScEd = Mont<EdScalarC>;
 
 // ---------------------------------------------------------------------------
-// P-256 base field: the NIST fast reduction (FIPS 186-4 D.2.3) on the 512-bit
-// product.  p = 2^256 - 2^224 + 2^192 + 2^96 - 1, so each result word is a
-// signed sum of product words (s1 + 2 s2 + 2 s3 + s4 + s5 - s6 - s7 - s8 - s9);
-// the sums run in 64-bit columns, then the signed top carry t (|t| <= 6) is
-// folded twice with 2^256 = 2^224 - 2^192 - 2^96 + 1.  No multiplications in
-// the reduction: it runs on the integer ALU while the products use IMAD.
+// P-256 base field in Montgomery form (R = 2^256): a value a is held as
+// a R mod p, weakly reduced (below 2^256).  p = 2^256 - 2^224 + 2^192 + 2^96 - 1
+// is -1 mod 2^32, so -p^-1 = 1 mod 2^32 and each reduction round's quotient
+// is the current low word q itself; q p = q 2^256 - q 2^224 + q 2^192 + q 2^96
+// - q then cancels that word and adds q at words +3 and +6 and q (2^32 - 1)
+// at words +7, +8 -- word-aligned additions, no multiplications (the
+// structure OpenSSL's ecp_nistz256 uses with 64-bit words).  The reduction
+// runs on the integer ALU while the products use the multiply pipe.
 // ---------------------------------------------------------------------------
 struct FpR1 {
   SG_HD static u256 P() { return SG_U256(0xffffffffu, 0xffffffffu, 0xffffffffu, 0x00000000u, 0x00000000u, 0x00000000u, 0x00000001u, 0xffffffffu); }
+  SG_HD static u256 R2() { return SG_U256(0x00000003u, 0x00000000u, 0xffffffffu, 0xfffffffbu, 0xfffffffeu, 0xffffffffu, 0xfffffffdu, 0x00000004u); }
+  SG_HD static u256 R3() { return SG_U256(0x0000000au, 0xfffffffdu, 0xfffffff7u, 0xffffffedu, 0xfffffffcu, 0x00000005u, 0x00000001u, 0x00000018u); }
 
-  // value = w + top * 2^256  ->  w + top * (2^224 - 2^192 - 2^96 + 1)
-  SG_HD static void fold(uint32_t w[8], int64_t& top) {
-    int64_t v = (int64_t)w[0] + top;
-    w[0] = (uint32_t)v; v >>= 32;
-    v += w[1]; w[1] = (uint32_t)v; v >>= 32;
-    v += w[2]; w[2] = (uint32_t)v; v >>= 32;
-    v += (int64_t)w[3] - top; w[3] = (uint32_t)v; v >>= 32;
-    v += w[4]; w[4] = (uint32_t)v; v >>= 32;
-    v += w[5]; w[5] = (uint32_t)v; v >>= 32;
-    v += (int64_t)w[6] - top; w[6] = (uint32_t)v; v >>= 32;
-    v += (int64_t)w[7] + top; w[7] = (uint32_t)v; v >>= 32;
-    top = v;
-  }
-
-  SG_HD static u256 reduce(const uint32_t c[16]) {
-    typedef int64_t I;
-    I t[8];
-    t[0] = (I)c[0] + c[8] + c[9] - c[11] - c[12] - c[13] - c[14];
-    t[1] = (I)c[1] + c[9] + c[10] - c[12] - c[13] - c[14] - c[15];
-    t[2] = (I)c[2] + c[10] + c[11] - c[13] - c[14] - c[15];
-    t[3] = (I)c[3] + 2 * (I)c[11] + 2 * (I)c[12] + c[13] - c[15] - c[8] - c[9];
-    t[4] = (I)c[4] + 2 * (I)c[12] + 2 * (I)c[13] + c[14] - c[9] - c[10];
-    t[5] = (I)c[5] + 2 * (I)c[13] + 2 * (I)c[14] + c[15] - c[10] - c[11];
-    t[6] = (I)c[6] + 3 * (I)c[14] + 2 * (I)c[15] + c[13] - c[8] - c[9];
-    t[7] = (I)c[7] + 3 * (I)c[15] + c[8] - c[10] - c[11] - c[12] - c[13];
-    uint32_t w[8];
-    I v = 0;
+  // t 2^-256 mod p for t < 2^512, weakly reduced (below 2^256).  Round i adds
+  // q p 2^(32 i) with q = t_i; its carry out of word i + 8 is held back and
+  // added with the next round's high word (hi + carry < 2^32), so every round
+  // is one carry chain over six words.  The sum (t + Q p) / 2^256 is below
+  // 2^256 + p: a carry out of 2^256 is folded as K = 2^256 - p.
+  SG_HD static u256 reduce(const uint32_t tin[16]) {
+    uint32_t t[16];
 #pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      v += t[k];
-      w[k] = (uint32_t)v;
-      v >>= 32;
+    for (int k = 0; k < 16; ++k) t[k] = tin[k];
+    uint32_t c = 0;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const uint32_t q = t[i];
+      const uint32_t lo = sub_cc(0u, q);  // q (2^32 - 1) = hi 2^32 + lo
+      const uint32_t hi = subc(q, 0u) + c;
+      t[i + 3] = add_cc(t[i + 3], q);
+      t[i + 4] = addc_cc(t[i + 4], 0u);
+      t[i + 5] = addc_cc(t[i + 5], 0u);
+      t[i + 6] = addc_cc(t[i + 6], q);
+      t[i + 7] = addc_cc(t[i + 7], lo);
+      t[i + 8] = addc_cc(t[i + 8], hi);
+      c = addc(0u, 0u);
     }
-    fold(w, v);  // |v| <= 6 -> v in {-1, 0, 1}
-    fold(w, v);  // -> v == 0, value in [0, 2^256): weakly reduced
     u256 r;
 #pragma unroll
-    for (int k = 0; k < 8; ++k) r.w[k] = w[k];
+    for (int k = 0; k < 8; ++k) r.w[k] = t[8 + k];
+    (void)add_k(r, c);  // r < p when c = 1, so r + K stays below 2^256
     return r;
   }
 
@@ -599,11 +592,17 @@ struct FpR1 {
     return r;
   }
   SG_HD static u256 neg(const u256& a) { return sub(u256_zero(), a); }  // 0 - 0 = 0 without a borrow
-  SG_HD static u256 one() { return u256_small(1); }
+  SG_HD static u256 one() { return SG_U256(0x00000001u, 0u, 0u, 0xffffffffu, 0xffffffffu, 0xffffffffu, 0xfffffffeu, 0u); }  // R mod p
   SG_HD static u256 zero() { return u256_zero(); }
-  SG_HD static u256 from_int(const u256& x) { return canon(x); }  // x < 2^256
-  SG_HD static u256 to_int(const u256& a) { return canon(a); }
-  SG_HD static u256 curve_b() { return SG_U256(0x27d2604bu, 0x3bce3c3eu, 0xcc53b0f6u, 0x651d06b0u, 0x769886bcu, 0xb3ebbd55u, 0xaa3a93e7u, 0x5ac635d8u); }
+  SG_HD static u256 from_int(const u256& x) { return mul(x, R2()); }  // any x < 2^256 -> x R mod p
+  SG_HD static u256 to_int(const u256& a) {  // a R^-1 mod p, canonical
+    uint32_t t[16];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) { t[k] = a.w[k]; t[8 + k] = 0u; }
+    return canon(reduce(t));  // (a + Q p) / 2^256 <= p
+  }
+  // b R mod p
+  SG_HD static u256 curve_b() { return SG_U256(0x29c4bddfu, 0xd89cdf62u, 0x78843090u, 0xacf005cdu, 0xf7212ed6u, 0xe5a220abu, 0x04874834u, 0xdc30061du); }
 
   SG_HD static u256 sqr_n(u256 a, int n) {
 #pragma unroll 1
@@ -620,10 +619,11 @@ struct FpR1 {
     x32 = mul(sqr_n(x16, 16), x16);
   }
 
-  // a^-1 by divsteps (canonical result), verified; Fermat fallback
+  // a^-1 by divsteps, verified; Fermat fallback.  The divsteps invert the
+  // held value a R, so one Montgomery multiply by R^3 gives a^-1 R.
   SG_NOINL static u256 inv(const u256 a) {
     const u256 ac = canon(a);
-    u256 r = divstep_inverse(ac, P(), 0x3fffffffu);
+    const u256 r = canon(mul(divstep_inverse(ac, P(), 0x3fffffffu), R3()));
     return u256_eq(canon(mul(ac, r)), one()) ? r : canon(inv_fermat(ac));
   }
 

@@ -73,6 +73,7 @@ struct sigops_ctx {
   int grid[3] = {0, 0, 0};     // plain kernels: blocks per launch, per curve
   int variant[3] = {0, 0, 0};  // plain kernel variant per curve
   uint32_t* d_gtab[3] = {nullptr, nullptr, nullptr};
+  uint32_t* d_gsmall[3] = {nullptr, nullptr, nullptr};  // 8-bit-window tables (staged into shared memory by the kernels)
   uint32_t* d_err = nullptr;
   uint8_t* d_buf = nullptr;  // inputs then outputs of host-buffer calls
   size_t d_cap = 0;
@@ -81,6 +82,7 @@ struct sigops_ctx {
   // batched engine
   void* d_scratch = nullptr;  // Scratch record
   uint32_t* d_idx = nullptr;  // 3 * idx_cap per-curve index lists
+  uint8_t* d_defer = nullptr;  // batched_defer_bytes(idx_cap): shared-inversion scratch of the single-curve variants
   size_t idx_cap = 0;
   int batched_variant = 0;
   int batched_grid = 0;
@@ -145,9 +147,16 @@ bool is_pinned(const void* p) {
 int ensure_idx(sigops_ctx* c, size_t n) {
   if (n <= c->idx_cap) return SIGOPS_OK;
   if (c->d_idx) cudaFree(c->d_idx);
+  if (c->d_defer) cudaFree(c->d_defer);
   c->d_idx = nullptr;
+  c->d_defer = nullptr;
   c->idx_cap = 0;
   if (cudaMalloc(&c->d_idx, 3 * n * sizeof(uint32_t)) != cudaSuccess) return fail(SIGOPS_E_NOMEM, "cudaMalloc(index lists, %zu)", n);
+  if (cudaMalloc(&c->d_defer, batched_defer_bytes(n)) != cudaSuccess) {
+    cudaFree(c->d_idx);
+    c->d_idx = nullptr;
+    return fail(SIGOPS_E_NOMEM, "cudaMalloc(inversion scratch, %zu)", n);
+  }
   c->idx_cap = n;
   return SIGOPS_OK;
 }
@@ -174,16 +183,18 @@ int set_variant(sigops_ctx* c, int kernel, int variant) {
 }
 
 cudaError_t launch_mixed_on(sigops_ctx* c, const uint8_t* curves, const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks, size_t n,
-                            uint8_t* out, uint8_t* status, uint32_t* idx, void* scratch, const ForkStreams* fork, cudaStream_t s) {
+                            uint8_t* out, uint8_t* status, uint32_t* idx, void* scratch, void* defer, const ForkStreams* fork,
+                            cudaStream_t s) {
   size_t cg = (n + 255) / 256;
   int classify_grid = (int)(cg < (size_t)c->num_sms * 8 ? cg : (size_t)c->num_sms * 8);
-  return launch_batched(curves, sigs, msgs, pks, n, out, status, idx, scratch, c->d_gtab[0], c->d_gtab[1], c->d_gtab[2], c->d_err,
-                        c->batched_grid, c->batched_variant, classify_grid, fork, s);
+  const GenTables tabs{{c->d_gtab[0], c->d_gtab[1], c->d_gtab[2]}, {c->d_gsmall[0], c->d_gsmall[1], c->d_gsmall[2]}};
+  return launch_batched(curves, sigs, msgs, pks, n, out, status, idx, scratch, defer, tabs, c->d_err, c->batched_grid, c->batched_variant,
+                        classify_grid, fork, s);
 }
 
 cudaError_t launch_mixed(sigops_ctx* c, const uint8_t* curves, const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks, size_t n,
                          uint8_t* out, uint8_t* status, cudaStream_t s) {
-  return launch_mixed_on(c, curves, sigs, msgs, pks, n, out, status, c->d_idx, c->d_scratch, &c->fork, s);
+  return launch_mixed_on(c, curves, sigs, msgs, pks, n, out, status, c->d_idx, c->d_scratch, c->d_defer, &c->fork, s);
 }
 
 int check_device_errors(sigops_ctx* c) {
@@ -263,7 +274,11 @@ int ctx_view(sigops_ctx* c, CtxView* v) {
   if (!c || !v) return SIGOPS_E_INVAL;
   v->device = c->device;
   v->num_sms = c->num_sms;
-  for (int k = 0; k < 3; ++k) v->gtab[k] = c->d_gtab[k];
+  for (int k = 0; k < 3; ++k) {
+    v->gtab[k] = c->d_gtab[k];
+    v->tabs.big[k] = c->d_gtab[k];
+    v->tabs.small[k] = c->d_gsmall[k];
+  }
   v->d_err = c->d_err;
   v->batched_grid = c->batched_grid;
   v->batched_variant = c->batched_variant;
@@ -321,6 +336,9 @@ sigops_ctx* sigops_create(int device) {
     const auto& t = tabs.tab[k];
     if ((e = cudaMalloc(&c->d_gtab[k], t.size() * 4)) != cudaSuccess) return bail("cudaMalloc(table)", e);
     if ((e = cudaMemcpy(c->d_gtab[k], t.data(), t.size() * 4, cudaMemcpyHostToDevice)) != cudaSuccess) return bail("table upload", e);
+    const auto& sm = tabs.small[k];
+    if ((e = cudaMalloc(&c->d_gsmall[k], sm.size() * 4)) != cudaSuccess) return bail("cudaMalloc(table)", e);
+    if ((e = cudaMemcpy(c->d_gsmall[k], sm.data(), sm.size() * 4, cudaMemcpyHostToDevice)) != cudaSuccess) return bail("table upload", e);
     if (set_variant(c, k, 0) != SIGOPS_OK) {
       sigops_destroy(c);
       return nullptr;
@@ -345,12 +363,15 @@ void sigops_destroy(sigops_ctx* c) {
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   if (c->stream2) cudaStreamSynchronize(c->stream2);
-  for (int k = 0; k < 3; ++k)
+  for (int k = 0; k < 3; ++k) {
     if (c->d_gtab[k]) cudaFree(c->d_gtab[k]);
+    if (c->d_gsmall[k]) cudaFree(c->d_gsmall[k]);
+  }
   if (c->d_err) cudaFree(c->d_err);
   if (c->d_scratch) cudaFree(c->d_scratch);
   if (c->d_scratch2) cudaFree(c->d_scratch2);
   if (c->d_idx) cudaFree(c->d_idx);
+  if (c->d_defer) cudaFree(c->d_defer);
   if (c->d_buf) cudaFree(c->d_buf);
   if (c->h_buf) cudaFreeHost(c->h_buf);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -559,7 +580,8 @@ int sigops_verify_mixed(sigops_ctx* ctx, const uint8_t* curves, const uint8_t* s
       SG_CUDA(cudaMemcpyAsync(c->d_buf + o_cur + b, curves + b, m, cudaMemcpyHostToDevice, s));
       SG_CUDA(launch_mixed_on(c, c->d_buf + o_cur + b, c->d_buf + o_sig + b * 64, c->d_buf + o_msg + b * 32, c->d_buf + o_pk + b * 32, m,
                               c->d_buf + o_out + b * 64, c->d_buf + o_st + b, c->d_idx + (k ? 3 * half : 0),
-                              k ? c->d_scratch : c->d_scratch2, k ? &c->fork : &c->fork2, s));
+                              k ? c->d_scratch : c->d_scratch2, c->d_defer + (k ? batched_defer_bytes(half) : 0),
+                              k ? &c->fork : &c->fork2, s));
       SG_CUDA(cudaMemcpyAsync(out + b * 64, c->d_buf + o_out + b * 64, m * 64, cudaMemcpyDeviceToHost, s));
       if (out_status) SG_CUDA(cudaMemcpyAsync(out_status + b, c->d_buf + o_st + b, m, cudaMemcpyDeviceToHost, s));
     }

@@ -30,42 +30,40 @@ int batched_occupancy_0();
 int batched_occupancy_1();
 int batched_occupancy_2();
 int batched_occupancy_3();
-int batched_occupancy_k1(int level);
-int batched_occupancy_r1(int level);
-int batched_occupancy_ed(int level);
+int batched_occupancy_k1(int config);
+int batched_occupancy_r1(int config);
+int batched_occupancy_ed(int config);
 cudaError_t batched_launch_0(const MixedIO&, const uint32_t*, const BatchTables&, Scratch*, uint32_t*, int, cudaStream_t);
 cudaError_t batched_launch_1(const MixedIO&, const uint32_t*, const BatchTables&, Scratch*, uint32_t*, int, cudaStream_t);
 cudaError_t batched_launch_2(const MixedIO&, const uint32_t*, const BatchTables&, Scratch*, uint32_t*, int, cudaStream_t);
 cudaError_t batched_launch_3(const MixedIO&, const uint32_t*, const BatchTables&, Scratch*, uint32_t*, int, cudaStream_t);
-cudaError_t batched_launch_k1(int, const MixedIO&, const uint32_t*, const BatchTables&, Scratch*, uint32_t*, cudaStream_t);
-cudaError_t batched_launch_r1(int, const MixedIO&, const uint32_t*, const BatchTables&, Scratch*, uint32_t*, cudaStream_t);
-cudaError_t batched_launch_ed(int, const MixedIO&, const uint32_t*, const BatchTables&, Scratch*, uint32_t*, cudaStream_t);
+cudaError_t batched_launch_k1(int, const MixedIO&, const uint32_t*, const BatchTables&, Scratch*, const DeferBufs&, uint32_t*, cudaStream_t);
+cudaError_t batched_launch_r1(int, const MixedIO&, const uint32_t*, const BatchTables&, Scratch*, const DeferBufs&, uint32_t*, cudaStream_t);
+cudaError_t batched_launch_ed(int, const MixedIO&, const uint32_t*, const BatchTables&, Scratch*, const DeferBufs&, uint32_t*, cudaStream_t);
 
 static const int kFusedBlock[BATCHED_FUSED_VARIANTS] = {256, 256, 128, 256};  // 1, 2, 3: one tile per warp, no loop
 
-// single-curve kernels: occupancy level 0 = 256 threads x 1 block per SM,
-// 1 = 128 x 3, 2 = 256 x 2 (8, 12 and 16 warps per SM), 3 = 64 threads with
-// at most 144 registers (14 warps per SM)
-constexpr int kLevels = 4;
-static const int kLevelBlock[kLevels] = {256, 128, 256, 64};
-
-// blocks per SM of curve c's single-curve kernel at an occupancy level
-// (queried once; the kernels are the same on every device of one process)
-static int curve_occupancy(int c, int level) {
-  static std::atomic<int> cache[3][kLevels];
-  int b = cache[c][level].load(std::memory_order_relaxed);
-  if (b == 0) {
-    b = c == 0 ? batched_occupancy_k1(level) : c == 1 ? batched_occupancy_r1(level) : batched_occupancy_ed(level);
-    cache[c][level].store(b, std::memory_order_relaxed);
-  }
-  return b;
+int curve_config_block(int config) {
+  static const int kBlock[CURVE_CONFIGS] = {256, 128, 256, 64, 512, 256, 256, 256};
+  return config >= 0 && config < CURVE_CONFIGS ? kBlock[config] : 0;
 }
 
-// variant 4 + a + 4 b + 16 c: levels a, b, c for secp256k1, P-256, ed25519
-static int split_level(int variant, int c) {
-  int v = variant - BATCHED_FUSED_VARIANTS;
-  for (int k = 0; k < c; ++k) v /= kLevels;
-  return v % kLevels;
+void curve_config_windows(int config, int* wr, int* wg) {
+  *wr = config == 5 ? 4 : config == 6 ? 6 : ECDSA_WR;
+  *wg = config == 7 ? SMALL_WG : ECDSA_WG;
+}
+
+// blocks per SM of curve c's kernel in a configuration (queried once; the
+// kernels are the same on every device of one process)
+int curve_config_occupancy(int c, int config) {
+  static std::atomic<int> cache[3][CURVE_CONFIGS];
+  if (c < 0 || c > 2 || config < 0 || config >= CURVE_CONFIGS) return 0;
+  int b = cache[c][config].load(std::memory_order_relaxed);
+  if (b == 0) {
+    b = c == 0 ? batched_occupancy_k1(config) : c == 1 ? batched_occupancy_r1(config) : batched_occupancy_ed(config);
+    cache[c][config].store(b, std::memory_order_relaxed);
+  }
+  return b;
 }
 
 int batched_variant_block(int v) {
@@ -85,8 +83,8 @@ int batched_max_blocks_per_sm(int v) {
   // in 256-thread blocks: the grid cap of a single-curve variant
   int m = 0;
   for (int c = 0; c < 3; ++c) {
-    const int l = split_level(v, c);
-    const int b = (curve_occupancy(c, l) * kLevelBlock[l] + 255) / 256;  // rounded up: never caps a kernel
+    const int cfg = split_config(v, c);
+    const int b = (curve_config_occupancy(c, cfg) * curve_config_block(cfg) + 255) / 256;  // rounded up: never caps a kernel
     if (b <= 0) return 0;
     m = b > m ? b : m;
   }
@@ -111,25 +109,27 @@ void fork_streams_destroy(ForkStreams* f) {
   *f = ForkStreams{};
 }
 
-static cudaError_t launch_curve(int c, int level, const MixedIO& io, const uint32_t* idx, const BatchTables& t, Scratch* sc,
-                                uint32_t* err, cudaStream_t s) {
-  if (c == 0) return batched_launch_k1(level, io, idx, t, sc, err, s);
-  if (c == 1) return batched_launch_r1(level, io, idx, t, sc, err, s);
-  return batched_launch_ed(level, io, idx, t, sc, err, s);
+static cudaError_t launch_curve(int c, int config, const MixedIO& io, const uint32_t* idx, const BatchTables& t, Scratch* sc,
+                                const DeferBufs& d, uint32_t* err, cudaStream_t s) {
+  if (c == 0) return batched_launch_k1(config, io, idx, t, sc, d, err, s);
+  if (c == 1) return batched_launch_r1(config, io, idx, t, sc, d, err, s);
+  return batched_launch_ed(config, io, idx, t, sc, d, err, s);
 }
 
 cudaError_t launch_batched(const uint8_t* curves, const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks, size_t n, uint8_t* out,
-                           uint8_t* status, uint32_t* idx, void* scratch, const uint32_t* gk1, const uint32_t* gr1, const uint32_t* ged,
-                           uint32_t* err, int grid, int variant, int classify_grid, const ForkStreams* fork, cudaStream_t stream) {
+                           uint8_t* status, uint32_t* idx, void* scratch, void* defer, const GenTables& tabs, uint32_t* err, int grid,
+                           int variant, int classify_grid, const ForkStreams* fork, cudaStream_t stream) {
   if (n == 0) return cudaSuccess;
-  // the per-curve index lists hold 32-bit item indices
+  // the per-curve index lists hold 32-bit item indices; the single-curve
+  // variants need the shared-inversion scratch
   if (variant < 0 || variant >= BATCHED_VARIANTS || grid <= 0 || n > 0xffffffffull) return cudaErrorInvalidValue;
+  if (variant >= BATCHED_FUSED_VARIANTS && !defer) return cudaErrorInvalidValue;
   Scratch* sc = (Scratch*)scratch;
   cudaError_t e = cudaMemsetAsync(sc, 0, sizeof(Scratch), stream);
   if (e != cudaSuccess) return e;
   classify_kernel<<<classify_grid, 256, 0, stream>>>(curves, n, idx, sc);
   MixedIO io{curves, sigs, msgs, pks, out, status, n};
-  BatchTables t{gk1, gr1, ged};
+  BatchTables t{tabs.big[0], tabs.big[1], tabs.big[2], {tabs.small[0], tabs.small[1], tabs.small[2]}};
   switch (variant) {
     case 0: return batched_launch_0(io, idx, t, sc, err, grid, stream);
     case 1: return batched_launch_1(io, idx, t, sc, err, grid, stream);
@@ -149,9 +149,10 @@ cudaError_t launch_batched(const uint8_t* curves, const uint8_t* sigs, const uin
     }
   }
   cudaError_t first = cudaSuccess;
+  const DeferBufs d{reinterpret_cast<uint4*>(defer), reinterpret_cast<uint4*>(defer) + 2 * n};
   for (int c = 0; c < 3; ++c) {
     // one item per thread: the kernel sizes its grid to the batch
-    e = launch_curve(c, split_level(variant, c), io, idx, t, sc, err, s[c]);
+    e = launch_curve(c, split_config(variant, c), io, idx, t, sc, d, err, s[c]);
     if (e != cudaSuccess && first == cudaSuccess) first = e;
   }
   if (fork) {  // join, even after a failed launch, so no side stream stays forked
@@ -165,5 +166,6 @@ cudaError_t launch_batched(const uint8_t* curves, const uint8_t* sigs, const uin
 }
 
 size_t batched_scratch_bytes() { return sizeof(Scratch); }
+size_t batched_defer_bytes(size_t n) { return n * DEFER_BYTES_PER_ITEM; }
 
 }  // namespace sg

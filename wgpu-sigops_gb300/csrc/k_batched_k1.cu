@@ -1,29 +1,39 @@
-// Single-curve batched kernels for secp256k1 recovery (GLV), one item per thread, at four
-// occupancy levels: 0 = 256 threads x 1 block per SM (up to 255 registers),
-// 1 = 128 x 3 (170), 2 = 256 x 2 (128), 3 = 64 threads with at most 144
-// registers.  The grid covers the whole batch; blocks past the curve's item
-// count return at once.
+// Single-curve batched kernels for secp256k1 recovery (GLV): configurations 0..3 (launch
+// shapes at the default window widths) and the simultaneous-inversion kernels
+// around the curve kernel; configurations 4..7 are in k_batched_k1_w.cu
+// (one translation unit each, so that they compile in parallel).
 #include "batched.cuh"
 
 namespace sg {
 
-int batched_occupancy_k1(int level) {
-  int b = 0;
-  if (level == 0) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, batched_curve_kernel<256, 1, 0>, 256, 0);
-  else if (level == 1) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, batched_curve_kernel<128, 3, 0>, 128, 0);
-  else if (level == 2) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, batched_curve_kernel<256, 2, 0>, 256, 0);
-  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, batched_curve_kernel_r<64, 144, 0>, 64, 0);
-  return b;
+int batched_occupancy_k1_w(int config);
+cudaError_t batched_curve_k1_w(int config, const MixedIO& io, const uint32_t* idx, const BatchTables& t, Scratch* sc, const DeferBufs& d,
+                                  uint32_t* err, cudaStream_t stream);
+
+int batched_occupancy_k1(int config) {
+  switch (config) {
+    case 0: return CurveKernel<0, 0>::occupancy();
+    case 1: return CurveKernel<0, 1>::occupancy();
+    case 2: return CurveKernel<0, 2>::occupancy();
+    case 3: return CurveKernel<0, 3>::occupancy();
+    default: return batched_occupancy_k1_w(config);
+  }
 }
 
-cudaError_t batched_launch_k1(int level, const MixedIO& io, const uint32_t* idx, const BatchTables& t, Scratch* sc, uint32_t* err,
-                              cudaStream_t stream) {
-  const int block = level == 3 ? 64 : level == 1 ? 128 : 256;
-  const unsigned grid = (unsigned)((io.n + block - 1) / block);
-  if (level == 0) batched_curve_kernel<256, 1, 0><<<grid, 256, 0, stream>>>(io, idx, t, sc, err);
-  else if (level == 1) batched_curve_kernel<128, 3, 0><<<grid, 128, 0, stream>>>(io, idx, t, sc, err);
-  else if (level == 2) batched_curve_kernel<256, 2, 0><<<grid, 256, 0, stream>>>(io, idx, t, sc, err);
-  else batched_curve_kernel_r<64, 144, 0><<<grid, 64, 0, stream>>>(io, idx, t, sc, err);
+// the curve's part of a single-curve step, on one stream
+cudaError_t batched_launch_k1(int config, const MixedIO& io, const uint32_t* idx, const BatchTables& t, Scratch* sc, const DeferBufs& d,
+                              uint32_t* err, cudaStream_t stream) {
+  launch_rinv<0>(io, idx, sc, d, stream);
+  cudaError_t e;
+  switch (config) {
+    case 0: e = CurveKernel<0, 0>::launch(io, idx, t, sc, d, err, stream); break;
+    case 1: e = CurveKernel<0, 1>::launch(io, idx, t, sc, d, err, stream); break;
+    case 2: e = CurveKernel<0, 2>::launch(io, idx, t, sc, d, err, stream); break;
+    case 3: e = CurveKernel<0, 3>::launch(io, idx, t, sc, d, err, stream); break;
+    default: e = batched_curve_k1_w(config, io, idx, t, sc, d, err, stream); break;
+  }
+  if (e != cudaSuccess) return e;
+  launch_finish<0>(io, idx, sc, d, stream);
   return cudaGetLastError();
 }
 

@@ -1,0 +1,29 @@
+// Single-curve batched kernels for secp256k1 recovery (GLV), configurations 4..7: 512-thread
+// blocks, and 256 x 2 blocks with per-point windows of 4 or 6 bits or 8-bit
+// generator windows whose table each block stages into shared memory.
+#include "batched.cuh"
+
+namespace sg {
+
+int batched_occupancy_k1_w(int config) {
+  switch (config) {
+    case 4: return CurveKernel<0, 4>::occupancy();
+    case 5: return CurveKernel<0, 5>::occupancy();
+    case 6: return CurveKernel<0, 6>::occupancy();
+    case 7: return CurveKernel<0, 7>::occupancy();
+    default: return 0;
+  }
+}
+
+cudaError_t batched_curve_k1_w(int config, const MixedIO& io, const uint32_t* idx, const BatchTables& t, Scratch* sc, const DeferBufs& d,
+                                  uint32_t* err, cudaStream_t stream) {
+  switch (config) {
+    case 4: return CurveKernel<0, 4>::launch(io, idx, t, sc, d, err, stream);
+    case 5: return CurveKernel<0, 5>::launch(io, idx, t, sc, d, err, stream);
+    case 6: return CurveKernel<0, 6>::launch(io, idx, t, sc, d, err, stream);
+    case 7: return CurveKernel<0, 7>::launch(io, idx, t, sc, d, err, stream);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+}  // namespace sg

@@ -40,15 +40,41 @@ cudaError_t launch_sign_ed(const uint8_t* seeds, const uint8_t* msgs, size_t n, 
 // batched mixed-curve engine: scratch = Scratch record + 3*n u32 index lists.
 // variants 0..3: the fused kernel (0 = persistent, 256 threads x 1 block/SM;
 // 1 = one tile per warp, 256 threads; 2 = one tile per warp, 128 x 3;
-// 3 = one tile per warp, 256 x 2); variants 4 + a + 4 b + 16 c (4..67): three
-// single-curve kernels (secp256k1 at occupancy level a, P-256 at b, ed25519
-// at c; level 0 = 256 threads x 1 block per SM, 1 = 128 x 3, 2 = 256 x 2,
-// 3 = 64 threads with at most 144 registers).
+// 3 = one tile per warp, 256 x 2); variants 4 + a + 8 b + 64 c (4..515): three
+// single-curve pipelines (secp256k1 in configuration a, P-256 in b, ed25519
+// in c).  Configurations (block x blocks per SM / register budget, per-point
+// window WR, generator window WG):
+//   0: 256 x 1 / 255, 1: 128 x 3 / 170, 2: 256 x 2 / 128, 3: 64 / 144,
+//   4: 512 x 1 / 128 (all WR 5, WG 16, tables in global memory);
+//   5: as 2 with WR 4; 6: as 2 with WR 6; 7: as 2 with WG 8 (tables staged
+//   into shared memory by a bulk copy).
 constexpr int BATCHED_FUSED_VARIANTS = 4;
-constexpr int BATCHED_VARIANTS = 68;
+constexpr int CURVE_CONFIGS = 8;
+constexpr int BATCHED_VARIANTS = BATCHED_FUSED_VARIANTS + CURVE_CONFIGS * CURVE_CONFIGS * CURVE_CONFIGS;
+inline int split_variant(int a, int b, int c) { return BATCHED_FUSED_VARIANTS + a + CURVE_CONFIGS * b + CURVE_CONFIGS * CURVE_CONFIGS * c; }
+// configuration of curve c (0..2) in a single-curve variant
+inline int split_config(int variant, int c) {
+  int v = variant - BATCHED_FUSED_VARIANTS;
+  for (int k = 0; k < c; ++k) v /= CURVE_CONFIGS;
+  return v % CURVE_CONFIGS;
+}
+// block size, window widths of a configuration
+int curve_config_block(int config);
+void curve_config_windows(int config, int* wr, int* wg);
+// blocks per SM of curve c's kernel in a configuration
+int curve_config_occupancy(int c, int config);
+// device pointers of the generator tables: 16-bit windows (global memory) and
+// 8-bit windows (staged into shared memory), per curve
+struct GenTables {
+  const uint32_t* big[3];
+  const uint32_t* small[3];
+};
 int batched_variant_block(int variant);
 int batched_max_blocks_per_sm(int variant);
 size_t batched_scratch_bytes();
+// the single-curve variants' shared-inversion scratch for n items (16-byte
+// aligned, item-indexed: r^-1 then the result points)
+size_t batched_defer_bytes(size_t n);
 // side streams and events on which the single-curve kernels run beside each
 // other (fork after the classify kernel, join before returning); without them
 // the three kernels run one after another on the caller's stream
@@ -60,15 +86,17 @@ struct ForkStreams {
 cudaError_t fork_streams_create(ForkStreams* f, int priority = 0);
 void fork_streams_destroy(ForkStreams* f);
 // grid: blocks of the fused kernel (the single-curve kernels size their grids
-// to the batch: one item per thread)
+// to the batch: one item per thread).  defer: batched_defer_bytes(n) of
+// scratch, required by the single-curve variants (NULL for the fused ones)
 cudaError_t launch_batched(const uint8_t* curves, const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks, size_t n, uint8_t* out,
-                           uint8_t* status, uint32_t* idx, void* scratch, const uint32_t* gk1, const uint32_t* gr1, const uint32_t* ged,
-                           uint32_t* err, int grid, int variant, int classify_grid, const ForkStreams* fork, cudaStream_t stream);
+                           uint8_t* status, uint32_t* idx, void* scratch, void* defer, const GenTables& tabs, uint32_t* err, int grid,
+                           int variant, int classify_grid, const ForkStreams* fork, cudaStream_t stream);
 // what the serving loop needs from a context (host.cu)
 struct CtxView {
   int device;
   int num_sms;
   const uint32_t* gtab[3];
+  GenTables tabs;
   uint32_t* d_err;
   int batched_grid;
   int batched_variant;

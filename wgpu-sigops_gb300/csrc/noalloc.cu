@@ -117,8 +117,9 @@ extern "C" int sigops_verify_mixed_noalloc(const uint8_t* d_curves, const uint8_
   const int classify_grid = (int)(cg < (size_t)d.num_sms * 8 ? cg : (size_t)d.num_sms * 8);
   // the per-curve index lists follow the counters; launch_batched clears the counters
   uint32_t* idx = reinterpret_cast<uint32_t*>(d.scratch + kScratchHead);
-  cudaError_t e = sg::launch_batched(d_curves, d_sigs, d_msgs, d_pks, n, d_out, d_status, idx, d.scratch, d.tab[0], d.tab[1], d.tab[2],
-                                     d.err, d.grid, kVariant, classify_grid, nullptr, (cudaStream_t)stream);
+  const sg::GenTables tabs{{d.tab[0], d.tab[1], d.tab[2]}, {nullptr, nullptr, nullptr}};  // the fused variant reads the 16-bit tables only
+  cudaError_t e = sg::launch_batched(d_curves, d_sigs, d_msgs, d_pks, n, d_out, d_status, idx, d.scratch, nullptr, tabs, d.err, d.grid, kVariant,
+                                     classify_grid, nullptr, (cudaStream_t)stream);
   return e == cudaSuccess ? SIGOPS_OK : SIGOPS_E_CUDA;
 }
 

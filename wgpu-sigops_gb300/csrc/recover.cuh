@@ -30,16 +30,20 @@ SG_HD void u256_to_be_words(const u256& v, uint32_t* w) {
 // ---------------------------------------------------------------------------
 // Window widths of the signed fixed windows (Booth): the per-signature point R
 // uses multiples 1..2^(WR-1) built per thread; the generator uses a
-// precomputed table of multiples 1..2^(WG-1) in global memory (2 MiB for
-// 16-bit windows, read through the read-only path and resident in L2), so
-// that a 256-bit scalar costs 17 generator additions instead of 33 with
-// 8-bit windows.
+// precomputed table of multiples 1..2^(WG-1).  The defaults: WR = 5 and WG =
+// 16, a table in global memory (2 MiB, read through the read-only path and
+// resident in L2), so that a 256-bit scalar costs 17 generator additions
+// instead of 33 with 8-bit windows.  The batched engine also compiles WR = 4
+// and 6, and WG = 8 with its 128-entry tables staged into shared memory by a
+// bulk (TMA) copy; the autotuner times them.
 constexpr int ECDSA_WR = 5;
 constexpr int ECDSA_WG = 16;
 constexpr int ECDSA_GTAB = 1 << (ECDSA_WG - 1);  // 32768 affine points
 constexpr int ED_WR = 5;
 constexpr int ED_WG = 16;
 constexpr int ED_GTAB = 1 << (ED_WG - 1);  // 32768 affine Niels points
+constexpr int SMALL_WG = 8;                      // generator windows of tables staged in shared memory
+constexpr int SMALL_GTAB = 1 << (SMALL_WG - 1);  // 128 entries
 
 struct K1Traits {
   using F = FpK1;
@@ -75,9 +79,30 @@ SG_HD void load_table_words(const uint32_t* e, int n, uint32_t* w) {
 #endif
 }
 
+// n words of a table staged in shared memory (16-byte aligned)
+SG_HD void load_smem_words(const uint32_t* e, int n, uint32_t* w) {
+#ifdef __CUDA_ARCH__
+  const uint4* q = reinterpret_cast<const uint4*>(e);
+#pragma unroll
+  for (int k = 0; k < n / 4; ++k) {
+    const uint4 v = q[k];
+    w[4 * k] = v.x;
+    w[4 * k + 1] = v.y;
+    w[4 * k + 2] = v.z;
+    w[4 * k + 3] = v.w;
+  }
+#else
+  for (int k = 0; k < n; ++k) w[k] = e[k];
+#endif
+}
+
+// entry idx of a generator table: global memory for 16-bit windows, shared
+// memory for the small tables
+template <int WG = ECDSA_WG>
 SG_HD APoint load_apoint(const uint32_t* t, uint32_t idx) {
   uint32_t w[16];
-  load_table_words(t + (size_t)idx * 16u, 16, w);
+  if constexpr (WG == ECDSA_WG) load_table_words(t + (size_t)idx * 16u, 16, w);
+  else load_smem_words(t + (size_t)idx * 16u, 16, w);
   APoint a;
 #pragma unroll
   for (int k = 0; k < 8; ++k) { a.x.w[k] = w[k]; a.y.w[k] = w[8 + k]; }
@@ -141,37 +166,37 @@ SG_HD void coz_table(const APoint R, APoint* tab) {
 }
 
 // u1 * G + u2 * R, signed fixed windows, one shared doubling chain.
-// gtab: multiples 1..ECDSA_GTAB of G, affine, field representation.
-template <class T>
+// gtab: multiples 1..2^(WG-1) of G, affine, field representation.
+template <class T, int WR = ECDSA_WR, int WG = ECDSA_WG>
 SG_NOINL JPoint ecdsa_lincomb(const u256 u1, const u256 u2, const APoint R, const uint32_t* gtab) {
   using W = Weier<typename T::F, T::A_M3>;
-  constexpr int NR = 1 << (ECDSA_WR - 1);
+  constexpr int NR = 1 << (WR - 1);
   APoint tab[NR];
   coz_table<typename T::F, T::A_M3, NR>(R, tab);
 
-  constexpr int JR = (257 + ECDSA_WR - 1) / ECDSA_WR;  // windows for a 256-bit scalar
-  constexpr int JG = (257 + ECDSA_WG - 1) / ECDSA_WG;
+  constexpr int JR = (257 + WR - 1) / WR;  // windows for a 256-bit scalar
+  constexpr int JG = (257 + WG - 1) / WG;
   // the chain starts at the highest window position that adds anything:
   // doublings above it would only double the point at infinity
-  constexpr int TOP = ((JR - 1) * ECDSA_WR > (JG - 1) * ECDSA_WG) ? (JR - 1) * ECDSA_WR : (JG - 1) * ECDSA_WG;
+  constexpr int TOP = ((JR - 1) * WR > (JG - 1) * WG) ? (JR - 1) * WR : (JG - 1) * WG;
   JPoint acc = W::infinity();
 #pragma unroll 1
   for (int pos = TOP; pos >= 0; --pos) {
     acc = W::dbl(acc);
-    if (pos % ECDSA_WR == 0) {
+    if (pos % WR == 0) {
       bool neg;
-      uint32_t d = booth_digit(u2, pos / ECDSA_WR, ECDSA_WR, neg);
+      uint32_t d = booth_digit(u2, pos / WR, WR, neg);
       if (d) {
         APoint e = tab[d - 1];
         if (neg) e = W::neg(e);
         acc = W::madd(acc, e);
       }
     }
-    if (pos % ECDSA_WG == 0) {
+    if (pos % WG == 0) {
       bool neg;
-      uint32_t d = booth_digit(u1, pos / ECDSA_WG, ECDSA_WG, neg);
+      uint32_t d = booth_digit(u1, pos / WG, WG, neg);
       if (d) {
-        APoint e = load_apoint(gtab, d - 1);
+        APoint e = load_apoint<WG>(gtab, d - 1);
         if (neg) e = W::neg(e);
         acc = W::madd(acc, e);
       }
@@ -187,7 +212,7 @@ SG_NOINL JPoint ecdsa_lincomb(const u256 u1, const u256 u2, const APoint R, cons
 // doublings instead of ~260.  Decomposition constants as in the reference's
 // src/curve_algos/secp256k1_curve.rs:47-71 (Babai rounding with g1, g2 scaled
 // by 2^384); the CPU model of GLV is src/curve_algos/secp256k1_mul.rs:38-94.
-// gtab2: multiples 1..ECDSA_GTAB of G followed by the same multiples of 2^128 G.
+// gtab2: multiples 1..2^(WG-1) of G followed by the same multiples of 2^128 G.
 // ---------------------------------------------------------------------------
 struct K1Glv {
   SG_HD static u256 LAMBDA_MONT() { return SG_U256(0xc9926c9eu, 0xf07deb3du, 0x83c6944cu, 0x2c93e7adu, 0x52697d91u, 0x73a96606u, 0x8558d639u, 0x53284017u); }
@@ -238,11 +263,12 @@ struct K1Glv {
   }
 };
 
-template <int = 0>
+template <int WR = ECDSA_WR, int WG = ECDSA_WG>
 SG_NOINL JPoint k1_glv_lincomb(const u256 u1, const u256 u2, const APoint R, const uint32_t* gtab2) {
   using F = FpK1;
   using W = Weier<F, false>;
-  constexpr int NR = 1 << (ECDSA_WR - 1);
+  constexpr int NR = 1 << (WR - 1);
+  constexpr int HALF = 1 << (WG - 1);  // entries per half of the table
   u256 k1, k2;
   bool neg1, neg2;
   K1Glv::split(u2, k1, neg1, k2, neg2);
@@ -256,24 +282,24 @@ SG_NOINL JPoint k1_glv_lincomb(const u256 u1, const u256 u2, const APoint R, con
 #pragma unroll
   for (int k = 0; k < 4; ++k) { b.w[k] = u1.w[4 + k]; a.w[4 + k] = 0; }
 
-  constexpr int JR = (130 + ECDSA_WR - 1) / ECDSA_WR;  // windows for a 129-bit magnitude
-  constexpr int JG = (129 + ECDSA_WG - 1) / ECDSA_WG;  // windows for a 128-bit half
+  constexpr int JR = (130 + WR - 1) / WR;  // windows for a 129-bit magnitude
+  constexpr int JG = (129 + WG - 1) / WG;  // windows for a 128-bit half
   // the chain starts at the highest window position that adds anything:
   // doublings above it would only double the point at infinity
-  constexpr int TOP = ((JR - 1) * ECDSA_WR > (JG - 1) * ECDSA_WG) ? (JR - 1) * ECDSA_WR : (JG - 1) * ECDSA_WG;
+  constexpr int TOP = ((JR - 1) * WR > (JG - 1) * WG) ? (JR - 1) * WR : (JG - 1) * WG;
   JPoint acc = W::infinity();
 #pragma unroll 1
   for (int pos = TOP; pos >= 0; --pos) {
     acc = W::dbl(acc);
-    if (pos % ECDSA_WR == 0) {
+    if (pos % WR == 0) {
       bool ng;
-      uint32_t d = booth_digit(k1, pos / ECDSA_WR, ECDSA_WR, ng);
+      uint32_t d = booth_digit(k1, pos / WR, WR, ng);
       if (d) {
         APoint e = tab[d - 1];
         if (ng) e = W::neg(e);
         acc = W::madd(acc, e);
       }
-      d = booth_digit(k2, pos / ECDSA_WR, ECDSA_WR, ng);
+      d = booth_digit(k2, pos / WR, WR, ng);
       if (d) {
         APoint e = tab[d - 1];
         e.x = F::mul(e.x, beta);
@@ -281,17 +307,17 @@ SG_NOINL JPoint k1_glv_lincomb(const u256 u1, const u256 u2, const APoint R, con
         acc = W::madd(acc, e);
       }
     }
-    if (pos % ECDSA_WG == 0) {
+    if (pos % WG == 0) {
       bool ng;
-      uint32_t d = booth_digit(a, pos / ECDSA_WG, ECDSA_WG, ng);
+      uint32_t d = booth_digit(a, pos / WG, WG, ng);
       if (d) {
-        APoint e = load_apoint(gtab2, d - 1);
+        APoint e = load_apoint<WG>(gtab2, d - 1);
         if (ng) e = W::neg(e);
         acc = W::madd(acc, e);
       }
-      d = booth_digit(b, pos / ECDSA_WG, ECDSA_WG, ng);
+      d = booth_digit(b, pos / WG, WG, ng);
       if (d) {
-        APoint e = load_apoint(gtab2, ECDSA_GTAB + d - 1);
+        APoint e = load_apoint<WG>(gtab2, HALF + d - 1);
         if (ng) e = W::neg(e);
         acc = W::madd(acc, e);
       }
@@ -300,28 +326,24 @@ SG_NOINL JPoint k1_glv_lincomb(const u256 u1, const u256 u2, const APoint R, con
   return acc;
 }
 
-// Recover the signer's key from a fuel-encoded signature (recovery parity in
-// bit 7 of s[0]); follows the reference's one-kernel path
-// (src/wgsl/secp256k1_ecdsa.wgsl:87-130, src/wgsl/secp256r1_ecdsa.wgsl:87-130)
-// with the validity rules of libsecp256k1 / p256 recovery: r, s in [1, n-1],
-// z = msg mod n, a checked square root for R.y, Q != infinity.
-template <class T, bool GLV = false>
-SG_HD uint8_t ecdsa_recover(const uint32_t sig[16], const uint32_t msg[8], const uint32_t* gtab, uint32_t out[16]) {
+// Decode a fuel-encoded signature (recovery parity in bit 7 of s[0]) and
+// recover R, with the validity rules of libsecp256k1 / p256 recovery: r, s in
+// [1, n-1], z = msg mod n, a checked square root for R.y.  Follows the
+// reference's one-kernel path (src/wgsl/secp256k1_ecdsa.wgsl:87-130,
+// src/wgsl/secp256r1_ecdsa.wgsl:87-130).  Returns ST_OK or the item's status.
+template <class T>
+SG_HD uint8_t ecdsa_prepare(const uint32_t sig[16], const uint32_t msg[8], u256& r, u256& s, u256& z, APoint& R) {
   using F = typename T::F;
   using S = typename T::S;
-  using W = Weier<F, T::A_M3>;
-#pragma unroll
-  for (int k = 0; k < 16; ++k) out[k] = 0;
-
   const u256 N = S::N();
-  u256 r = be_words_to_u256(sig);
+  r = be_words_to_u256(sig);
   uint32_t sw[8];
 #pragma unroll
   for (int k = 0; k < 8; ++k) sw[k] = sig[8 + k];
   const uint32_t parity = (sw[0] >> 7) & 1u;  // byte 32 is the low byte of word 8
   sw[0] &= 0xffffff7fu;
-  u256 s = be_words_to_u256(sw);
-  u256 z = reduce_once(be_words_to_u256(msg), N);
+  s = be_words_to_u256(sw);
+  z = reduce_once(be_words_to_u256(msg), N);
   if (u256_is_zero(r) || u256_gte(r, N) || u256_is_zero(s) || u256_gte(s, N)) return ST_BAD_SCALAR;
 
   // R = (r, y) with y^2 = r^3 + a r + b and the requested parity
@@ -330,31 +352,93 @@ SG_HD uint8_t ecdsa_recover(const uint32_t sig[16], const uint32_t msg[8], const
   u256 y = F::sqrt_candidate(rhs);
   if (!u256_eq(F::canon(F::sqr(y)), F::canon(rhs))) return ST_NO_POINT;
   if ((F::to_int(y).w[0] & 1u) != parity) y = F::neg(y);
-  APoint R;
   R.x = x;
   R.y = y;
+  return ST_OK;
+}
 
-  // u1 = -z / r, u2 = s / r (mod n)
-  u256 rinv_m = S::from_int(S::inv_int(r));  // r^-1 in Montgomery form
-  u256 u2 = S::mul(s, rinv_m);
-  u256 u1 = S::neg(S::mul(z, rinv_m));
+// Q = (-z / r) G + (s / r) R for a prepared signature, rinv_m = r^-1 in the
+// scalar field's Montgomery form; ST_INFINITY when Q is the point at infinity
+template <class T, bool GLV, int WR = ECDSA_WR, int WG = ECDSA_WG>
+SG_HD uint8_t ecdsa_key_jacobian(const u256& s, const u256& z, const APoint& R, const u256& rinv_m, const uint32_t* gtab, JPoint& Q) {
+  using S = typename T::S;
+  using W = Weier<typename T::F, T::A_M3>;
+  const u256 u2 = S::mul(s, rinv_m);
+  const u256 u1 = S::neg(S::mul(z, rinv_m));
+  if constexpr (GLV) Q = k1_glv_lincomb<WR, WG>(u1, u2, R, gtab);
+  else Q = ecdsa_lincomb<T, WR, WG>(u1, u2, R, gtab);
+  return W::is_inf(Q) ? ST_INFINITY : ST_OK;
+}
 
+// Recover the signer's key: out = x || y big-endian (zero unless ST_OK).
+template <class T, bool GLV = false>
+SG_HD uint8_t ecdsa_recover(const uint32_t sig[16], const uint32_t msg[8], const uint32_t* gtab, uint32_t out[16]) {
+  using F = typename T::F;
+  using S = typename T::S;
+  using W = Weier<F, T::A_M3>;
+#pragma unroll
+  for (int k = 0; k < 16; ++k) out[k] = 0;
+  u256 r, s, z;
+  APoint R;
+  uint8_t st = ecdsa_prepare<T>(sig, msg, r, s, z, R);
+  if (st != ST_OK) return st;
+  const u256 rinv_m = S::from_int(S::inv_int(r));  // r^-1 in Montgomery form
   JPoint Q;
-  if constexpr (GLV) Q = k1_glv_lincomb<>(u1, u2, R, gtab);
-  else Q = ecdsa_lincomb<T>(u1, u2, R, gtab);
-  if (W::is_inf(Q)) return ST_INFINITY;
+  st = ecdsa_key_jacobian<T, GLV>(s, z, R, rinv_m, gtab, Q);
+  if (st != ST_OK) return st;
   APoint a = W::to_affine(Q);
   u256_to_be_words(F::to_int(a.x), out);
   u256_to_be_words(F::to_int(a.y), out + 8);
   return ST_OK;
 }
 
+// r of a signature as the factor of the batched engine's simultaneous
+// inversion: r in Montgomery form when r is in [1, n-1], else one (such an
+// item fails its range check and never uses its inverse)
+template <class T>
+SG_HD u256 ecdsa_r_factor(const uint32_t sig[16]) {
+  using S = typename T::S;
+  const u256 r = be_words_to_u256(sig);
+  const bool ok = !u256_is_zero(r) && !u256_gte(r, S::N());
+  return ok ? S::from_int(r) : S::one();
+}
+
+// Montgomery's simultaneous inversion of v[0 .. m) in place (m >= 1, every
+// v[j] invertible): prefix products, one inversion of their product,
+// back-substitution -- 3 (m - 1) multiplications and one inversion for m
+// inverses.  pre: scratch of m entries.  inv_one inverts a single value.
+template <class Fd, class Inv>
+SG_HD void batch_invert(u256* v, u256* pre, int m, Inv inv_one) {
+  pre[0] = v[0];
+#pragma unroll 1
+  for (int j = 1; j < m; ++j) pre[j] = Fd::mul(pre[j - 1], v[j]);
+  u256 inv = inv_one(pre[m - 1]);
+#pragma unroll 1
+  for (int j = m - 1; j > 0; --j) {
+    const u256 vj = v[j];
+    v[j] = Fd::mul(inv, pre[j - 1]);
+    inv = Fd::mul(inv, vj);
+  }
+  v[0] = inv;
+}
+
+// the affine key of a Jacobian point given Z^-1, as 16 big-endian words
+template <class T>
+SG_HD void ecdsa_encode_key(const JPoint& Q, const u256& zi, uint32_t out[16]) {
+  using F = typename T::F;
+  const u256 zi2 = F::sqr(zi);
+  u256_to_be_words(F::to_int(F::mul(Q.X, zi2)), out);
+  u256_to_be_words(F::to_int(F::mul(Q.Y, F::mul(zi2, zi))), out + 8);
+}
+
 // ---------------------------------------------------------------------------
 // ed25519 verification (ed25519-dalek 2.1.1 VerifyingKey::verify semantics)
 // ---------------------------------------------------------------------------
+template <int WG = ED_WG>
 SG_HD EAffNiels load_eniels(const uint32_t* t, uint32_t idx) {
   uint32_t w[24];
-  load_table_words(t + (size_t)idx * 24u, 24, w);
+  if constexpr (WG == ED_WG) load_table_words(t + (size_t)idx * 24u, 24, w);
+  else load_smem_words(t + (size_t)idx * 24u, 24, w);
   EAffNiels a;
 #pragma unroll
   for (int k = 0; k < 8; ++k) { a.ypx.w[k] = w[k]; a.ymx.w[k] = w[8 + k]; a.t2d.w[k] = w[16 + k]; }
@@ -381,10 +465,10 @@ SG_HD u256 ed_challenge(const uint32_t sig[16], const uint32_t pk[8], const uint
   return reduce512_mod_l(h);
 }
 
-// [s]B + [k](-A), signed fixed windows; btab: multiples 1..ED_GTAB of B (affine Niels)
-template <int = 0>
+// [s]B + [k](-A), signed fixed windows; btab: multiples 1..2^(WG-1) of B (affine Niels)
+template <int WR = ED_WR, int WG = ED_WG>
 SG_NOINL EPoint ed_lincomb(const u256 s, const u256 k, const EPoint negA, const uint32_t* btab) {
-  constexpr int NR = 1 << (ED_WR - 1);
+  constexpr int NR = 1 << (WR - 1);
   ENiels tab[NR];
   EPoint cur = negA;
   tab[0] = Edw::to_niels(cur);
@@ -397,27 +481,27 @@ SG_NOINL EPoint ed_lincomb(const u256 s, const u256 k, const EPoint negA, const 
     tab[i] = Edw::to_niels(cur);
   }
   // both scalars are < l < 2^253
-  constexpr int JR = (254 + ED_WR - 1) / ED_WR;
-  constexpr int JG = (254 + ED_WG - 1) / ED_WG;
-  constexpr int TOP = ((JR - 1) * ED_WR > (JG - 1) * ED_WG) ? (JR - 1) * ED_WR : (JG - 1) * ED_WG;
+  constexpr int JR = (254 + WR - 1) / WR;
+  constexpr int JG = (254 + WG - 1) / WG;
+  constexpr int TOP = ((JR - 1) * WR > (JG - 1) * WG) ? (JR - 1) * WR : (JG - 1) * WG;
   EPoint acc = Edw::identity();
 #pragma unroll 1
   for (int pos = TOP; pos >= 0; --pos) {
-    acc = Edw::dbl(acc, pos % ED_WR == 0 || pos % ED_WG == 0);
-    if (pos % ED_WR == 0) {
+    acc = Edw::dbl(acc, pos % WR == 0 || pos % WG == 0);
+    if (pos % WR == 0) {
       bool neg;
-      uint32_t d = booth_digit(k, pos / ED_WR, ED_WR, neg);
+      uint32_t d = booth_digit(k, pos / WR, WR, neg);
       if (d) {
         ENiels e = tab[d - 1];
         if (neg) e = Edw::neg(e);
-        acc = Edw::add(acc, e, pos % ED_WG == 0);  // T only for a generator addition at this position
+        acc = Edw::add(acc, e, pos % WG == 0);  // T only for a generator addition at this position
       }
     }
-    if (pos % ED_WG == 0) {
+    if (pos % WG == 0) {
       bool neg;
-      uint32_t d = booth_digit(s, pos / ED_WG, ED_WG, neg);
+      uint32_t d = booth_digit(s, pos / WG, WG, neg);
       if (d) {
-        EAffNiels e = load_eniels(btab, d - 1);
+        EAffNiels e = load_eniels<WG>(btab, d - 1);
         if (neg) e = Edw::neg(e);
         acc = Edw::madd(acc, e, false);  // a doubling or the compression comes next
       }
@@ -434,8 +518,8 @@ SG_NOINL EPoint ed_lincomb(const u256 s, const u256 k, const EPoint negA, const 
 // GPU path lacks (src/wgsl/main/ed25519_eddsa_main_0.wgsl:45-54).
 // challenge(R, A) returns k = SHA-512(R || A || M) mod l; it runs only after
 // the key and S checks passed.
-template <class Challenge>
-SG_HD uint8_t ed25519_verify_with(const uint32_t sig[16], const uint32_t pk[8], const uint32_t* btab, Challenge challenge) {
+template <int WR = ED_WR, int WG = ED_WG, class Challenge>
+SG_HD uint8_t ed25519_point_with(const uint32_t sig[16], const uint32_t pk[8], const uint32_t* btab, Challenge challenge, EPoint& Rp) {
   u256 aenc;
 #pragma unroll
   for (int k = 0; k < 8; ++k) aenc.w[k] = pk[k];
@@ -451,14 +535,43 @@ SG_HD uint8_t ed25519_verify_with(const uint32_t sig[16], const uint32_t pk[8], 
   negA.Y = A.Y;
   negA.Z = A.Z;
   negA.T = FpEd::neg(A.T);
-  EPoint Rp = ed_lincomb<>(s, k, negA, btab);
+  Rp = ed_lincomb<WR, WG>(s, k, negA, btab);
+  return ST_OK;
+}
+
+// ST_OK when the encoding of R' = (X : Y : Z), given Z^-1, equals the R bytes
+SG_HD uint8_t ed25519_compare(const EPoint& Rp, const u256& zi, const uint32_t sig[16]) {
+  u256 x = FpEd::canon(FpEd::mul(Rp.X, zi));
+  u256 y = FpEd::canon(FpEd::mul(Rp.Y, zi));
+  y.w[7] |= (x.w[0] & 1u) << 31;
+  u256 renc;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) renc.w[k] = sig[k];
+  return u256_eq(y, renc) ? ST_OK : ST_MISMATCH;
+}
+
+template <class Challenge>
+SG_HD uint8_t ed25519_verify_with(const uint32_t sig[16], const uint32_t pk[8], const uint32_t* btab, Challenge challenge) {
+  EPoint Rp;
+  const uint8_t st = ed25519_point_with(sig, pk, btab, challenge, Rp);
+  if (st != ST_OK) return st;
   u256 enc = Edw::compress(Rp);
+  u256 renc;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) renc.w[k] = sig[k];
   return u256_eq(enc, renc) ? ST_OK : ST_MISMATCH;
 }
 
 // the reference's API: 32-byte (fuel) messages
 SG_HD uint8_t ed25519_verify(const uint32_t sig[16], const uint32_t msg[8], const uint32_t pk[8], const uint32_t* btab) {
   return ed25519_verify_with(sig, pk, btab, [&](const u256&, const u256&) { return ed_challenge(sig, pk, msg); });
+}
+
+// the batched engine's form: R' = [S]B - [k]A before its compression (whose
+// inversion the engine shares across items); ST_OK means "compare pending"
+template <int WR = ED_WR, int WG = ED_WG>
+SG_HD uint8_t ed25519_point(const uint32_t sig[16], const uint32_t msg[8], const uint32_t pk[8], const uint32_t* btab, EPoint& Rp) {
+  return ed25519_point_with<WR, WG>(sig, pk, btab, [&](const u256&, const u256&) { return ed_challenge(sig, pk, msg); }, Rp);
 }
 
 // a message of any length (msg: len bytes, device memory on the GPU)

@@ -56,6 +56,7 @@ struct Slot {
   uint8_t* d = nullptr;  // device buffer, same layout
   void* d_scratch = nullptr;
   uint32_t* d_idx = nullptr;
+  void* d_defer = nullptr;  // shared-inversion scratch of the single-curve variants
   std::vector<Request*> reqs;
   size_t n = 0;
   bool busy = false;
@@ -158,7 +159,7 @@ void pack_and_launch(sigops_server* s, Slot& sl) {
   const int block = sg::batched_variant_block(variant);
   const int grid = (int)std::min<size_t>((size_t)grid_cap, (n + block - 1) / block);
   keep(sg::launch_batched(sl.d + L.cur, sl.d + L.sig, sl.d + L.msg, sl.d + L.pk, n, sl.d + L.out, sl.d + L.st, sl.d_idx, sl.d_scratch,
-                          s->cv.gtab[0], s->cv.gtab[1], s->cv.gtab[2], s->cv.d_err, grid, variant, classify_grid, &sl.fork, sl.stream));
+                          sl.d_defer, s->cv.tabs, s->cv.d_err, grid, variant, classify_grid, &sl.fork, sl.stream));
   keep(cudaMemcpyAsync(sl.h + L.out, sl.d + L.out, n * 64, cudaMemcpyDeviceToHost, sl.stream));
   keep(cudaMemcpyAsync(sl.h + L.st, sl.d + L.st, n, cudaMemcpyDeviceToHost, sl.stream));
   keep(cudaEventRecord(sl.done, sl.stream));
@@ -270,7 +271,8 @@ sigops_server* sigops_server_create(sigops_ctx* ctx, int nslots, size_t slot_ite
               cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming) == cudaSuccess &&
               cudaMallocHost(&sl.h, s->lay.total) == cudaSuccess && cudaMalloc(&sl.d, s->lay.total) == cudaSuccess &&
               cudaMalloc(&sl.d_scratch, sg::batched_scratch_bytes()) == cudaSuccess &&
-              cudaMalloc(&sl.d_idx, 3 * slot_items * sizeof(uint32_t)) == cudaSuccess;
+              cudaMalloc(&sl.d_idx, 3 * slot_items * sizeof(uint32_t)) == cudaSuccess &&
+              cudaMalloc(&sl.d_defer, sg::batched_defer_bytes(slot_items)) == cudaSuccess;
     if (!ok) {
       sigops_server_destroy(s);
       return nullptr;
@@ -299,6 +301,7 @@ void sigops_server_destroy(sigops_server* s) {
     if (sl.d) cudaFree(sl.d);
     if (sl.d_scratch) cudaFree(sl.d_scratch);
     if (sl.d_idx) cudaFree(sl.d_idx);
+    if (sl.d_defer) cudaFree(sl.d_defer);
   }
   for (auto& kv : s->reqs) delete kv.second;
   delete s;

@@ -58,12 +58,12 @@ SG_HD void ed25519_sign(const uint32_t seed[8], const uint32_t msg[8], const uin
   for (int i = 0; i < 8; ++i) a.w[i] = h[i];
   u256 a_l = ScEd::to_int(ScEd::from_int(a));  // a mod l: a * B = (a mod l) * B
   EPoint id = Edw::identity();
-  u256 A = Edw::compress(ed_lincomb<>(a_l, u256_zero(), id, btab));
+  u256 A = Edw::compress(ed_lincomb(a_l, u256_zero(), id, btab));
 #pragma unroll
   for (int i = 0; i < 8; ++i) { buf[i] = h[8 + i]; buf[8 + i] = msg[i]; }
   sha512_fixed<64>(buf, hr);
   u256 r = reduce512_mod_l(hr);
-  u256 R = Edw::compress(ed_lincomb<>(r, u256_zero(), id, btab));
+  u256 R = Edw::compress(ed_lincomb(r, u256_zero(), id, btab));
 #pragma unroll
   for (int i = 0; i < 8; ++i) { sig[i] = R.w[i]; pk[i] = A.w[i]; }
   u256 k = ed_challenge(sig, pk, msg);

@@ -95,37 +95,37 @@ inline void ed_multiples(int count, u256* xs, u256* ys) {
   }
 }
 
-// kernel table for the Weierstrass curves: ECDSA_GTAB entries of 16 words (x, y)
+// kernel table for the Weierstrass curves: `count` entries of 16 words (x, y)
 template <class T>
-inline void build_weier_gtab(const u256& gx, const u256& gy, uint32_t* out) {
-  std::vector<APoint> pts(ECDSA_GTAB);
-  weier_multiples<T>(gx, gy, ECDSA_GTAB, pts.data());
-  for (int i = 0; i < ECDSA_GTAB; ++i)
+inline void build_weier_gtab(const u256& gx, const u256& gy, uint32_t* out, int count = ECDSA_GTAB) {
+  std::vector<APoint> pts(count);
+  weier_multiples<T>(gx, gy, count, pts.data());
+  for (int i = 0; i < count; ++i)
     for (int k = 0; k < 8; ++k) {
       out[i * 16 + k] = pts[i].x.w[k];
       out[i * 16 + 8 + k] = pts[i].y.w[k];
     }
 }
 
-// secp256k1 GLV table: multiples 1..32768 of G, then the same multiples of 2^128 G
-inline void build_k1_glv_gtab(uint32_t* out) {
+// secp256k1 GLV table: multiples 1..count of G, then the same multiples of 2^128 G
+inline void build_k1_glv_gtab(uint32_t* out, int count = ECDSA_GTAB) {
   using F = FpK1;
   using W = Weier<F, false>;
-  build_weier_gtab<K1Traits>(k1_gx(), k1_gy(), out);
+  build_weier_gtab<K1Traits>(k1_gx(), k1_gy(), out, count);
   APoint g;
   g.x = k1_gx();
   g.y = k1_gy();
   JPoint h = W::from_affine(g);
   for (int i = 0; i < 128; ++i) h = W::dbl(h);
   APoint ha = W::to_affine(h);
-  build_weier_gtab<K1Traits>(F::to_int(ha.x), F::to_int(ha.y), out + ECDSA_GTAB * 16);
+  build_weier_gtab<K1Traits>(F::to_int(ha.x), F::to_int(ha.y), out + (size_t)count * 16, count);
 }
 
-// kernel table for ed25519: ED_GTAB entries of 24 words (y+x, y-x, 2d*x*y)
-inline void build_ed_btab(uint32_t* out) {
-  std::vector<u256> xs(ED_GTAB), ys(ED_GTAB);
-  ed_multiples(ED_GTAB, xs.data(), ys.data());
-  for (int i = 0; i < ED_GTAB; ++i) {
+// kernel table for ed25519: `count` entries of 24 words (y+x, y-x, 2d*x*y)
+inline void build_ed_btab(uint32_t* out, int count = ED_GTAB) {
+  std::vector<u256> xs(count), ys(count);
+  ed_multiples(count, xs.data(), ys.data());
+  for (int i = 0; i < count; ++i) {
     u256 ypx = FpEd::canon(FpEd::add(ys[i], xs[i]));
     u256 ymx = FpEd::canon(FpEd::sub(ys[i], xs[i]));
     u256 t2d = FpEd::canon(FpEd::mul(FpEd::mul(xs[i], ys[i]), FpEd::D2()));
@@ -138,9 +138,12 @@ inline void build_ed_btab(uint32_t* out) {
 }
 
 // The kernels' generator tables, built once per process (thread-safe static
-// initialisation): secp256k1 (G and 2^128 G multiples), P-256, ed25519.
+// initialisation): secp256k1 (G and 2^128 G multiples), P-256, ed25519; for
+// 16-bit windows (tab, read from global memory) and 8-bit windows (small,
+// staged into shared memory)
 struct KernelTables {
   std::vector<uint32_t> tab[3];
+  std::vector<uint32_t> small[3];
 };
 inline const KernelTables& kernel_tables() {
   static const KernelTables t = [] {
@@ -151,6 +154,12 @@ inline const KernelTables& kernel_tables() {
     build_k1_glv_gtab(k.tab[CURVE_SECP256K1].data());
     build_weier_gtab<R1Traits>(r1_gx(), r1_gy(), k.tab[CURVE_SECP256R1].data());
     build_ed_btab(k.tab[CURVE_ED25519].data());
+    k.small[CURVE_SECP256K1].resize(2 * SMALL_GTAB * 16);
+    k.small[CURVE_SECP256R1].resize(SMALL_GTAB * 16);
+    k.small[CURVE_ED25519].resize(SMALL_GTAB * 24);
+    build_k1_glv_gtab(k.small[CURVE_SECP256K1].data(), SMALL_GTAB);
+    build_weier_gtab<R1Traits>(r1_gx(), r1_gy(), k.small[CURVE_SECP256R1].data(), SMALL_GTAB);
+    build_ed_btab(k.small[CURVE_ED25519].data(), SMALL_GTAB);
     return k;
   }();
   return t;

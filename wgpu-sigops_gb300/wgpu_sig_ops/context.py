@@ -51,7 +51,7 @@ class Context:
         """Time every launch variant on a device-signed probe batch and keep the fastest."""
         import json
 
-        buf = ctypes.create_string_buffer(4096)
+        buf = ctypes.create_string_buffer(16384)
         check(lib.sigops_autotune(self.ptr, probe_items, buf, len(buf)), "sigops_autotune")
         return json.loads(buf.value.decode())
 
