@@ -408,7 +408,20 @@ def main():
     if args.serving_seconds > 0:
         from wgpu_sig_ops import serving as sv
 
-        serving = sv.measure(ctx, W, seconds=args.serving_seconds)
+        # shape of the persistent kernel: a short run of each at half load;
+        # the full levels use the one with the highest saturation whose p99
+        # stays within 5 ms
+        sweep = []
+        for shape in range(3):
+            r = sv.measure(ctx, W, loads=(0.5,), seconds=min(3.0, args.serving_seconds), sat_items=1_000_000, variant=shape,
+                           warmup_seconds=0.5)
+            lv = r["levels"][0]
+            sweep.append({"kernel_shape": shape, "saturation_sigs_per_s": r["saturation_sigs_per_s"], "p50_ms_at_0.5": lv["p50_ms"],
+                          "p99_ms_at_0.5": lv["p99_ms"], "refused": lv["refused"]})
+        fit = [x for x in sweep if x["p99_ms_at_0.5"] <= 5.0 and x["refused"] == 0] or sweep
+        best = max(fit, key=lambda x: x["saturation_sigs_per_s"])["kernel_shape"]
+        serving = sv.measure(ctx, W, seconds=args.serving_seconds, variant=best)
+        serving["shape_sweep"] = sweep
         serving["workload"] = ("Poisson arrivals of single-curve requests, sizes log-uniform in 1..2048, 40/30/30 curves, "
                                "items drawn from the mixed batch; latency = submit to results in host memory")
 

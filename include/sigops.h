@@ -50,6 +50,8 @@ extern "C" {
 #define SIGOPS_E_TIMEDOUT (-110) /* a bounded device wait expired (the kernel returned instead of hanging) */
 #define SIGOPS_E_BUSY (-16)      /* serving queue full / admission refused */
 #define SIGOPS_E_RANGE (-34)     /* batch larger than the fixed capacity of an entry point */
+#define SIGOPS_E_CANCELED (-125) /* the serving request was cancelled (sigops_server_cancel) */
+#define SIGOPS_ALREADY_DONE 1    /* sigops_server_cancel: the request had finished; its results are in place */
 
 /* curves */
 #define SIGOPS_SECP256K1 0
@@ -249,47 +251,85 @@ int sigops_autotune(sigops_ctx* ctx, size_t probe_items, char* report, size_t re
 /* ------------------------------------------------------- serving loop */
 
 /* A continuous-batching server over one context (no counterpart in the
- * reference).  A dispatcher thread keeps `slots` batches in flight (each with
- * its own stream, pinned staging, device buffers and scratch); requests that
- * arrive while others run are packed into the next free slot; each launch's
- * grid is sized to its batch, so small batches from several slots share the
- * SMs.  slots <= 0 selects 8; slot_items = 0 sizes slots from free device
- * memory (hbm_fraction of cudaMemGetInfo's free bytes, default 0.25), capped
- * at 16,384 items.  Returns NULL on failure. */
+ * reference).  Its queues live with the device: submit copies a request's
+ * items into a pinned, mapped request ring and cuts them into 32-item
+ * single-curve tiles; one persistent kernel (launched cooperatively, every
+ * block resident) copies published tiles into a device-resident tile ring and
+ * works them off, results going straight to a pinned output ring; a host
+ * dispatcher thread copies each finished request's results to the caller's
+ * buffers and relaunches the kernel after it closes (20 ms idle, or 2 s of
+ * life).  Requests that arrive while others run become tiles behind them: no
+ * launch, copy or host round trip per request.  Every device-side wait is
+ * bounded; an expired one fails the requests in flight (SIGOPS_E_TIMEDOUT)
+ * instead of hanging them.  While the kernel runs it holds every SM it is
+ * resident on: other work of the context waits for its idle close.
+ * slot_items: the largest request (0 = 16,384); slots x slot_items: items in
+ * flight at most (slots <= 0 selects 32), within hbm_fraction (default 0.25)
+ * of the device memory free at creation.  Returns NULL on failure. */
 sigops_server* sigops_server_create(sigops_ctx* ctx, int slots, size_t slot_items, double hbm_fraction);
 void sigops_server_destroy(sigops_server* server);
 size_t sigops_server_slot_items(sigops_server* server);
-/* Batched-engine launch variant of the server's launches (as sigops_set_variant
- * kernel 3; default 1, the fused kernel with one tile per warp at 256
- * threads); applies from the next launch.  Variants 4..67 run their three
- * curve kernels one after another on the slot's stream.  No counterpart in the
- * reference. */
+/* Shape of the persistent kernel: 0 = 256-thread blocks, one per SM (default);
+ * 1 = 128 x 3 per SM (170 registers); 2 = 256 x 2 (128 registers).  Applies
+ * from the next launch of the kernel.  No counterpart in the reference. */
 int sigops_server_set_variant(sigops_server* server, int variant);
 
 /* Queue one request of n items.  curves: n tags, or NULL with uniform_curve
  * set for a single-curve request; pks may be NULL for ECDSA-only requests.
- * All buffers stay owned by the caller and must remain valid until
- * sigops_server_wait returns for the handle; out receives n*64 bytes (mixed
- * record layout), status n bytes (may be NULL).  Admission: SIGOPS_E_RANGE if
- * n exceeds the slot size, SIGOPS_E_BUSY if the queue bound (from device
- * memory) would be exceeded. */
+ * The inputs are copied before the call returns; out (n*64 bytes, mixed
+ * record layout) and status (n bytes, may be NULL) must stay valid until
+ * sigops_server_wait or sigops_server_cancel returns for the handle.
+ * Admission, checked now: SIGOPS_E_RANGE if n exceeds slot_items;
+ * SIGOPS_E_BUSY if the request rings have no room for it or the device's free
+ * memory is below its floor (1% of the device, at least 256 MiB; re-read every
+ * 100 ms); SIGOPS_E_CUDA if the server can no longer run requests. */
 int sigops_server_submit(sigops_server* server, const uint8_t* curves, int uniform_curve, const uint8_t* sigs, const uint8_t* msgs,
                          const uint8_t* pks, size_t n, uint8_t* out, uint8_t* status, uint64_t* handle);
 
 /* Wait for a request (timeout_ms < 0: no limit).  SIGOPS_OK when its results
- * are in place (latency_ms: submit to results, may be NULL), SIGOPS_E_TIMEDOUT
- * if still running, SIGOPS_E_INVAL for an unknown handle. */
+ * are in place (latency_ms: submit to results, may be NULL) and the handle is
+ * released; SIGOPS_E_TIMEDOUT if still running (or the server's dispatcher
+ * stopped); SIGOPS_E_CANCELED if it was cancelled; SIGOPS_E_INVAL for an
+ * unknown handle. */
 int sigops_server_wait(sigops_server* server, uint64_t handle, int timeout_ms, double* latency_ms);
+
+/* Withdraw a request: SIGOPS_OK when its results will not be written (the
+ * handle is released and the caller's out / status buffers may be freed at
+ * once; the device still works the items off and drops them);
+ * SIGOPS_ALREADY_DONE when it had finished (its results are in place; wait
+ * releases the handle); SIGOPS_E_INVAL for an unknown handle.  No
+ * counterpart in the reference. */
+int sigops_server_cancel(sigops_server* server, uint64_t handle);
 
 int sigops_server_stats(sigops_server* server, uint64_t* launches, uint64_t* requests_done, uint64_t* items_done, size_t* queued_items);
 
+/* Counters of the persistent kernel since the server was created: tiles and
+ * items verified, the time its warps spent working on tiles and looking for
+ * one (seconds, summed over warps; work / (work + idle) is how busy the GPU
+ * was while the kernel ran), and how often an SM changed the curve it works
+ * on.  Any pointer may be NULL.  No counterpart in the reference. */
+int sigops_server_kernel_stats(sigops_server* server, uint64_t* tiles, uint64_t* items, double* work_s, double* idle_s,
+                               uint64_t* sm_moves);
+
 /* Open-loop load generator: request i covers pool items
  * [offset[i], offset[i] + count[i]) and is submitted arrival_s[i] seconds after
- * the start (non-decreasing); outputs go to the same item positions of out /
- * status.  Fills latency_ms[i] (-1 when refused) and the wall time. */
+ * the start (non-decreasing) by one of four client threads (request i by
+ * thread i mod 4); outputs go to the same item positions of out / status.
+ * Fills latency_ms[i] (-1 when refused) and the wall time. */
 int sigops_server_run_load(sigops_server* server, const uint8_t* curves, const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks,
                            const uint64_t* offset, const uint32_t* count, const double* arrival_s, size_t nreq, uint8_t* out,
                            uint8_t* status, double* latency_ms, double* wall_s);
+
+/* Failure injection for tests, on the host (no device fault): fault 1 makes
+ * the server's dispatcher thread stop at its next iteration, as if it had
+ * died; waits then return SIGOPS_E_TIMEDOUT and submits SIGOPS_E_CUDA, and
+ * sigops_server_destroy still cleans up.  No counterpart in the reference. */
+int sigops_server_test_fault(sigops_server* server, int fault);
+
+/* Failure injection for tests, on the host: the next `count` device or pinned
+ * host allocations made by the library fail as if out of memory (0 clears).
+ * Returns the previous count.  No counterpart in the reference. */
+int sigops_test_fail_allocations(int count);
 
 /* ------------------------------------------- synthetic workload signing */
 

@@ -50,8 +50,8 @@ void hc_field(int field, int op, const uint8_t* a, const uint8_t* b, uint8_t* ou
     case 0: if (op == 4) r = FpK1::to_int(FpK1::sqrt_candidate(FpK1::from_int(x))); else OPS(FpK1); break;
     case 1: if (op == 4) r = FpR1::to_int(FpR1::sqrt_candidate(FpR1::from_int(x))); else OPS(FpR1); break;
     case 2: if (op == 4) r = FpEd::canon(FpEd::pow_p58(FpEd::from_int(x))); else OPS(FpEd); break;
-    case 3: OPS(ScK1); break;
-    case 4: OPS(ScR1); break;
+    case 3: if (op == 5) r = ScK1::inv_int(x); else OPS(ScK1); break;  // op 5: the kernels' r^-1 (divsteps, checked)
+    case 4: if (op == 5) r = ScR1::inv_int(x); else OPS(ScR1); break;
     case 5: OPS(ScEd); break;
   }
 #undef OPS

@@ -76,6 +76,31 @@ def compute() -> dict:
 
     model["batched"] = {"secp256k1_glv": per_sig_batched(0, k1), "secp256r1": per_sig_batched(1, r1), "ed25519": per_sig_batched(2, ed),
                         "inv_batch": 16}
+    # multiplies of the phases whose count does not depend on the batch: one
+    # inversion (divsteps, result checked by one multiplication) and one square
+    # root chain per field, less the conversions in and out of the field's
+    # representation that hc_field adds around every operation
+    x = (12345678901234567890).to_bytes(32, "little")
+
+    def op_count(field, op):
+        hc.hc_mulcount(1)
+        hc.hc_field(field, op, x, x, out)
+        n = hc.hc_mulcount(1)
+        hc.hc_field(field, 1, x, x, out)  # an addition: the conversions only
+        return n - hc.hc_mulcount(1)
+
+    def raw_count(field, op):
+        hc.hc_mulcount(1)
+        hc.hc_field(field, op, x, x, out)
+        return hc.hc_mulcount(1)
+
+    phases = {"fp_inv": {}, "sqrt": {}, "scalar_inv": {}}
+    for c, name in ((0, "secp256k1"), (1, "secp256r1"), (2, "ed25519")):
+        phases["fp_inv"][name] = op_count(c, 3)
+        phases["sqrt"][name] = op_count(c, 4)
+    for c, name in ((0, "secp256k1"), (1, "secp256r1")):
+        phases["scalar_inv"][name] = raw_count(3 + c, 5)  # r^-1 as the kernels compute it (no conversions around it)
+    model["phases"] = phases
     a = bytes(range(32))
     hc.hc_mulcount(1)
     hc.hc_sqr_wide(a, out)

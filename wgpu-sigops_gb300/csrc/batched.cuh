@@ -327,7 +327,7 @@ __global__ void __launch_bounds__(BLOCK) __maxnreg__(MAXREG) batched_curve_kerne
 // 4..7 in k_batched_<curve>_w.cu.
 template <int CURVE, int CFG>
 struct CurveKernel {
-  static constexpr int BLOCK = CFG == 1 ? 128 : CFG == 3 ? 64 : CFG == 4 ? 512 : 256;
+  static constexpr int BLOCK = CFG == 1 || CFG == 5 ? 128 : CFG == 3 ? 64 : CFG == 4 ? 512 : 256;
   static constexpr int WR = CFG == 5 ? 4 : CFG == 6 ? 6 : ECDSA_WR;
   static constexpr int WG = CFG == 7 ? SMALL_WG : ECDSA_WG;
   static auto fn() {
@@ -335,7 +335,8 @@ struct CurveKernel {
     else if constexpr (CFG == 1) return batched_curve_kernel<128, 3, CURVE>;
     else if constexpr (CFG == 3) return batched_curve_kernel_r<64, 144, CURVE>;
     else if constexpr (CFG == 4) return batched_curve_kernel<512, 1, CURVE>;
-    else return batched_curve_kernel<256, 2, CURVE, WR, WG>;  // 2, 5, 6, 7
+    else if constexpr (CFG == 5) return batched_curve_kernel<128, 3, CURVE, WR, WG>;
+    else return batched_curve_kernel<256, 2, CURVE, WR, WG>;  // 2, 6, 7
   }
   static int occupancy() {
     int b = 0;

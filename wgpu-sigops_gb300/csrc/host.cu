@@ -10,6 +10,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <atomic>
 #include <map>
 #include <mutex>
 #include <string>
@@ -66,6 +67,37 @@ bool valid_L(uint32_t L) { return L >= MIN_LOG_LIMB && L <= MAX_LOG_LIMB; }
 
 }  // namespace
 
+namespace sg {
+
+// allocations that the failure-injection hook may refuse
+static std::atomic<int> g_fail_allocs{0};
+
+static bool take_injected_failure() {
+  int v = g_fail_allocs.load();
+  while (v > 0)
+    if (g_fail_allocs.compare_exchange_weak(v, v - 1)) return true;
+  return false;
+}
+
+cudaError_t dev_alloc(void** p, size_t bytes) {
+  *p = nullptr;
+  if (take_injected_failure()) return cudaErrorMemoryAllocation;
+  return cudaMalloc(p, bytes);
+}
+void dev_free(void* p) {
+  if (p) cudaFree(p);
+}
+cudaError_t host_alloc(void** p, size_t bytes, unsigned flags) {
+  *p = nullptr;
+  if (take_injected_failure()) return cudaErrorMemoryAllocation;
+  return cudaHostAlloc(p, bytes, flags);
+}
+void host_free(void* p) {
+  if (p) cudaFreeHost(p);
+}
+
+}  // namespace sg
+
 struct sigops_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -108,17 +140,17 @@ namespace {
 int ensure_buffers(sigops_ctx* c, size_t bytes) {
   bytes = (bytes + 255) & ~(size_t)255;
   if (bytes > c->d_cap) {
-    if (c->d_buf) cudaFree(c->d_buf);
+    dev_free(c->d_buf);
     c->d_buf = nullptr;
     c->d_cap = 0;
-    if (cudaMalloc(&c->d_buf, bytes) != cudaSuccess) return fail(SIGOPS_E_NOMEM, "cudaMalloc(%zu) failed", bytes);
+    if (dev_alloc((void**)&c->d_buf, bytes) != cudaSuccess) return fail(SIGOPS_E_NOMEM, "cudaMalloc(%zu) failed", bytes);
     c->d_cap = bytes;
   }
   if (bytes > c->h_cap) {
-    if (c->h_buf) cudaFreeHost(c->h_buf);
+    host_free(c->h_buf);
     c->h_buf = nullptr;
     c->h_cap = 0;
-    if (cudaMallocHost(&c->h_buf, bytes) != cudaSuccess) return fail(SIGOPS_E_NOMEM, "cudaMallocHost(%zu) failed", bytes);
+    if (host_alloc((void**)&c->h_buf, bytes) != cudaSuccess) return fail(SIGOPS_E_NOMEM, "cudaMallocHost(%zu) failed", bytes);
     c->h_cap = bytes;
   }
   return SIGOPS_OK;
@@ -127,10 +159,10 @@ int ensure_buffers(sigops_ctx* c, size_t bytes) {
 int ensure_device(sigops_ctx* c, size_t bytes) {
   bytes = (bytes + 255) & ~(size_t)255;
   if (bytes <= c->d_cap) return SIGOPS_OK;
-  if (c->d_buf) cudaFree(c->d_buf);
+  dev_free(c->d_buf);
   c->d_buf = nullptr;
   c->d_cap = 0;
-  if (cudaMalloc(&c->d_buf, bytes) != cudaSuccess) return fail(SIGOPS_E_NOMEM, "cudaMalloc(%zu) failed", bytes);
+  if (dev_alloc((void**)&c->d_buf, bytes) != cudaSuccess) return fail(SIGOPS_E_NOMEM, "cudaMalloc(%zu) failed", bytes);
   c->d_cap = bytes;
   return SIGOPS_OK;
 }
@@ -146,14 +178,14 @@ bool is_pinned(const void* p) {
 
 int ensure_idx(sigops_ctx* c, size_t n) {
   if (n <= c->idx_cap) return SIGOPS_OK;
-  if (c->d_idx) cudaFree(c->d_idx);
-  if (c->d_defer) cudaFree(c->d_defer);
+  dev_free(c->d_idx);
+  dev_free(c->d_defer);
   c->d_idx = nullptr;
   c->d_defer = nullptr;
   c->idx_cap = 0;
-  if (cudaMalloc(&c->d_idx, 3 * n * sizeof(uint32_t)) != cudaSuccess) return fail(SIGOPS_E_NOMEM, "cudaMalloc(index lists, %zu)", n);
-  if (cudaMalloc(&c->d_defer, batched_defer_bytes(n)) != cudaSuccess) {
-    cudaFree(c->d_idx);
+  if (dev_alloc((void**)&c->d_idx, 3 * n * sizeof(uint32_t)) != cudaSuccess) return fail(SIGOPS_E_NOMEM, "cudaMalloc(index lists, %zu)", n);
+  if (dev_alloc((void**)&c->d_defer, batched_defer_bytes(n)) != cudaSuccess) {
+    dev_free(c->d_idx);
     c->d_idx = nullptr;
     return fail(SIGOPS_E_NOMEM, "cudaMalloc(inversion scratch, %zu)", n);
   }
@@ -303,6 +335,8 @@ const char* sigops_strerror(int code) {
     case SIGOPS_E_TIMEDOUT: return "device wait timed out";
     case SIGOPS_E_BUSY: return "busy";
     case SIGOPS_E_RANGE: return "batch exceeds capacity";
+    case SIGOPS_E_CANCELED: return "request cancelled";
+    case SIGOPS_ALREADY_DONE: return "request already finished";
     default: return "unknown error";
   }
 }
@@ -334,19 +368,19 @@ sigops_ctx* sigops_create(int device) {
   if ((e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device)) != cudaSuccess) return bail("attr", e);
   for (int k = 0; k < 3; ++k) {
     const auto& t = tabs.tab[k];
-    if ((e = cudaMalloc(&c->d_gtab[k], t.size() * 4)) != cudaSuccess) return bail("cudaMalloc(table)", e);
+    if ((e = dev_alloc((void**)&c->d_gtab[k], t.size() * 4)) != cudaSuccess) return bail("cudaMalloc(table)", e);
     if ((e = cudaMemcpy(c->d_gtab[k], t.data(), t.size() * 4, cudaMemcpyHostToDevice)) != cudaSuccess) return bail("table upload", e);
     const auto& sm = tabs.small[k];
-    if ((e = cudaMalloc(&c->d_gsmall[k], sm.size() * 4)) != cudaSuccess) return bail("cudaMalloc(table)", e);
+    if ((e = dev_alloc((void**)&c->d_gsmall[k], sm.size() * 4)) != cudaSuccess) return bail("cudaMalloc(table)", e);
     if ((e = cudaMemcpy(c->d_gsmall[k], sm.data(), sm.size() * 4, cudaMemcpyHostToDevice)) != cudaSuccess) return bail("table upload", e);
     if (set_variant(c, k, 0) != SIGOPS_OK) {
       sigops_destroy(c);
       return nullptr;
     }
   }
-  if ((e = cudaMalloc(&c->d_err, sizeof(uint32_t))) != cudaSuccess) return bail("cudaMalloc(err)", e);
-  if ((e = cudaMalloc(&c->d_scratch, batched_scratch_bytes())) != cudaSuccess) return bail("cudaMalloc(scratch)", e);
-  if ((e = cudaMalloc(&c->d_scratch2, batched_scratch_bytes())) != cudaSuccess) return bail("cudaMalloc(scratch)", e);
+  if ((e = dev_alloc((void**)&c->d_err, sizeof(uint32_t))) != cudaSuccess) return bail("cudaMalloc(err)", e);
+  if ((e = dev_alloc(&c->d_scratch, batched_scratch_bytes())) != cudaSuccess) return bail("cudaMalloc(scratch)", e);
+  if ((e = dev_alloc(&c->d_scratch2, batched_scratch_bytes())) != cudaSuccess) return bail("cudaMalloc(scratch)", e);
   if (set_variant(c, 3, 0) != SIGOPS_OK) {
     sigops_destroy(c);
     return nullptr;
@@ -364,16 +398,16 @@ void sigops_destroy(sigops_ctx* c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   if (c->stream2) cudaStreamSynchronize(c->stream2);
   for (int k = 0; k < 3; ++k) {
-    if (c->d_gtab[k]) cudaFree(c->d_gtab[k]);
-    if (c->d_gsmall[k]) cudaFree(c->d_gsmall[k]);
+    dev_free(c->d_gtab[k]);
+    dev_free(c->d_gsmall[k]);
   }
-  if (c->d_err) cudaFree(c->d_err);
-  if (c->d_scratch) cudaFree(c->d_scratch);
-  if (c->d_scratch2) cudaFree(c->d_scratch2);
-  if (c->d_idx) cudaFree(c->d_idx);
-  if (c->d_defer) cudaFree(c->d_defer);
-  if (c->d_buf) cudaFree(c->d_buf);
-  if (c->h_buf) cudaFreeHost(c->h_buf);
+  dev_free(c->d_err);
+  dev_free(c->d_scratch);
+  dev_free(c->d_scratch2);
+  dev_free(c->d_idx);
+  dev_free(c->d_defer);
+  dev_free(c->d_buf);
+  host_free(c->h_buf);
   if (c->stream) cudaStreamDestroy(c->stream);
   fork_streams_destroy(&c->fork);
   if (c->stream2) cudaStreamDestroy(c->stream2);
@@ -794,6 +828,8 @@ int sigops_test_wait_expiry(sigops_ctx* ctx, uint32_t max_polls) {
   SG_CUDA(launch_wait_expiry(max_polls, c->d_err, c->stream));
   return check_device_errors(c);
 }
+
+int sigops_test_fail_allocations(int count) { return g_fail_allocs.exchange(count < 0 ? 0 : count); }
 
 int sigops_test_sha512(sigops_ctx* ctx, const uint8_t* in, uint8_t* out, size_t n) {
   if (!in || !out) return fail(SIGOPS_E_INVAL, "null buffer");

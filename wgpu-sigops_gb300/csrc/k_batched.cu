@@ -44,7 +44,7 @@ cudaError_t batched_launch_ed(int, const MixedIO&, const uint32_t*, const BatchT
 static const int kFusedBlock[BATCHED_FUSED_VARIANTS] = {256, 256, 128, 256};  // 1, 2, 3: one tile per warp, no loop
 
 int curve_config_block(int config) {
-  static const int kBlock[CURVE_CONFIGS] = {256, 128, 256, 64, 512, 256, 256, 256};
+  static const int kBlock[CURVE_CONFIGS] = {256, 128, 256, 64, 512, 128, 256, 256};
   return config >= 0 && config < CURVE_CONFIGS ? kBlock[config] : 0;
 }
 

@@ -1,6 +1,7 @@
 // Single-curve batched kernels for P-256 recovery, configurations 4..7: 512-thread
-// blocks, and 256 x 2 blocks with per-point windows of 4 or 6 bits or 8-bit
-// generator windows whose table each block stages into shared memory.
+// blocks, 128 x 3 blocks with 4-bit per-point windows, and 256 x 2 blocks with
+// 6-bit per-point windows or 8-bit generator windows whose table each block
+// stages into shared memory.
 #include "batched.cuh"
 
 namespace sg {

@@ -46,8 +46,9 @@ cudaError_t launch_sign_ed(const uint8_t* seeds, const uint8_t* msgs, size_t n, 
 // window WR, generator window WG):
 //   0: 256 x 1 / 255, 1: 128 x 3 / 170, 2: 256 x 2 / 128, 3: 64 / 144,
 //   4: 512 x 1 / 128 (all WR 5, WG 16, tables in global memory);
-//   5: as 2 with WR 4; 6: as 2 with WR 6; 7: as 2 with WG 8 (tables staged
-//   into shared memory by a bulk copy).
+//   5: as 1 with WR 4 (half the per-signature table: 12 warps' stacks stay in
+//   L2); 6: as 2 with WR 6; 7: as 2 with WG 8 (tables staged into shared
+//   memory by a bulk copy).
 constexpr int BATCHED_FUSED_VARIANTS = 4;
 constexpr int CURVE_CONFIGS = 8;
 constexpr int BATCHED_VARIANTS = BATCHED_FUSED_VARIANTS + CURVE_CONFIGS * CURVE_CONFIGS * CURVE_CONFIGS;
@@ -91,6 +92,13 @@ void fork_streams_destroy(ForkStreams* f);
 cudaError_t launch_batched(const uint8_t* curves, const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks, size_t n, uint8_t* out,
                            uint8_t* status, uint32_t* idx, void* scratch, void* defer, const GenTables& tabs, uint32_t* err, int grid,
                            int variant, int classify_grid, const ForkStreams* fork, cudaStream_t stream);
+// Device and pinned host allocations of the library (host.cu).  A test hook
+// (sigops_test_fail_allocations) makes the next ones fail as if out of memory.
+cudaError_t dev_alloc(void** p, size_t bytes);
+void dev_free(void* p);
+cudaError_t host_alloc(void** p, size_t bytes, unsigned flags = cudaHostAllocDefault);
+void host_free(void* p);
+
 // what the serving loop needs from a context (host.cu)
 struct CtxView {
   int device;

@@ -1,20 +1,35 @@
 // Serving loop: continuous batching of verification requests on one GPU.
 //
 // No counterpart in the reference (each call there builds a device and runs
-// one batch, src/gpu.rs:5-35).  Requests (single- or mixed-curve batches of
-// any size up to the slot capacity) are queued by sigops_server_submit; a
-// dispatcher thread keeps K slots in flight, each with its own stream, pinned
-// staging, device buffers and batched-engine scratch.  Whenever a slot is free
-// and requests are waiting, it packs as many queued requests as fit into the
-// slot and launches one batched step (H2D copy, classify, the fused kernel,
-// D2H copy) on the slot's stream, so new arrivals join the next launch while
-// earlier launches are still running and their kernels overlap on the device.
-// Completed slots scatter results back to each request's output buffers.
+// one batch, src/gpu.rs:5-35).  The queues live with the device:
 //
-// Admission: slot capacity and the queue bound come from free device memory
-// at creation (cudaMemGetInfo x hbm_fraction); a request larger than a slot
-// is refused with SIGOPS_E_RANGE and a submission that would push the queued
-// items past the bound with SIGOPS_E_BUSY.
+//  * a pinned, mapped request ring on the host: sigops_server_submit copies a
+//    request's items (signatures, messages, keys) into the item ring grouped
+//    by curve, cuts them into 32-item single-curve tiles in the pinned tile
+//    ring and publishes them (ServeCtl::tile_tail);
+//  * one persistent kernel (serve.cuh, launched cooperatively so that all its
+//    blocks are resident): a feeder warp copies published tiles into three
+//    device-resident tile rings, one per curve, and every other warp claims
+//    tiles of its SM's current curve, copies their items from the pinned
+//    rings into shared memory, verifies them and copies the results into the
+//    pinned output ring; the warp whose tile completes a request appends it
+//    to a pinned completion ring.
+//
+// Requests that arrive while others run become tiles behind them, and the
+// warps of the one kernel take them up as they free: continuous batching with
+// no launch, copy or host round trip per request.  A dispatcher thread on the
+// host copies each finished request's results to the caller's buffers,
+// relaunches the kernel when it has closed (idle or its lifetime cap) and work
+// is waiting, and fails the requests in flight if the kernel reports an
+// expired device wait.
+//
+// Admission is live, at submit time: a request is admitted when the item ring
+// (pinned; its tiles and counters in device memory, within hbm_fraction of
+// the free device memory at creation), the tile rings and the request slots
+// have room for it now, and while the device's free memory, re-read every
+// 100 ms, stays above a floor (1% of the device, at least 256 MiB); else
+// SIGOPS_E_BUSY.  A request larger than the per-request limit is refused with
+// SIGOPS_E_RANGE.
 #include <cuda_runtime.h>
 #include <string.h>
 
@@ -23,6 +38,7 @@
 #include <chrono>
 #include <condition_variable>
 #include <deque>
+#include <memory>
 #include <mutex>
 #include <thread>
 #include <unordered_map>
@@ -30,6 +46,7 @@
 
 #include "../../include/sigops.h"
 #include "launch.h"
+#include "serve.cuh"
 
 namespace {
 
@@ -37,250 +54,324 @@ using Clock = std::chrono::steady_clock;
 
 double now_s() { return std::chrono::duration<double>(Clock::now().time_since_epoch()).count(); }
 
+enum class RState { Copying, Running, Finishing, Done, Canceled };
+
 struct Request {
-  uint64_t id;
-  const uint8_t *curves, *sigs, *msgs, *pks;
-  int uniform_curve;  // >= 0 when `curves` is NULL
-  size_t n;
-  uint8_t *out, *status;
+  uint64_t id = 0;
+  uint32_t slot = 0, seq = 0;
+  size_t off = 0, n = 0;
+  uint64_t ring_end = 0;                  // item-ring position after this request (reclaimed in submission order)
+  uint64_t tile_first = 0, tile_end = 0;  // its tiles in the tile rings
+  uint8_t *out = nullptr, *status = nullptr;
+  std::vector<uint32_t> perm;  // regrouped by curve: ring position -> the caller's item index (empty: same order)
   double t_submit = 0, t_done = 0;
   int rc = SIGOPS_OK;
-  bool done = false;
+  RState state = RState::Copying;
+  bool ready = false;     // inputs copied, tiles written
+  bool canceled = false;  // withdrawn by the caller: its results are dropped
 };
+using ReqPtr = std::shared_ptr<Request>;
 
-struct Slot {
-  cudaStream_t stream = nullptr;
-  sg::ForkStreams fork{};  // side streams: the single-curve variants run their three kernels side by side
-  cudaEvent_t done = nullptr;
-  uint8_t* h = nullptr;  // pinned staging: inputs then outputs
-  uint8_t* d = nullptr;  // device buffer, same layout
-  void* d_scratch = nullptr;
-  uint32_t* d_idx = nullptr;
-  void* d_defer = nullptr;  // shared-inversion scratch of the single-curve variants
-  std::vector<Request*> reqs;
-  size_t n = 0;
-  bool busy = false;
-};
-
-struct Layout {
-  size_t cur, sig, msg, pk, out, st, total;
-};
-Layout layout(size_t cap) {
-  auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
-  Layout l;
-  l.cur = 0;
-  l.sig = al(cap);
-  l.msg = l.sig + al(cap * 64);
-  l.pk = l.msg + al(cap * 32);
-  l.out = l.pk + al(cap * 32);
-  l.st = l.out + al(cap * 64);
-  l.total = l.st + al(cap);
-  return l;
-}
+// shapes of the persistent kernel (sigops_server_set_variant)
+constexpr int kServeShapes = 3;
+const int kServeBlock[kServeShapes] = {256, 128, 256};
 
 }  // namespace
 
 struct sigops_server {
   sigops_ctx* ctx = nullptr;
   sg::CtxView cv{};
-  std::vector<Slot> slots;
-  size_t cap = 0;          // items per slot
-  // batched-engine launch variant and its grid cap, packed in one word so the
-  // worker reads a consistent pair (variant << 16 | blocks per launch at most).
-  // Default: variant 1, the fused kernel with one tile per warp at 256 threads
-  // (measured: the highest saturation).  The single-curve variants run their
-  // three kernels side by side on the slot's side streams: lower latency at
-  // light load, about 18% less saturation.  sigops_server_set_variant changes
-  // it between launches.
-  std::atomic<uint32_t> shape{0};
-  size_t queue_bound = 0;  // max queued (not yet launched) items
-  Layout lay{};
+  size_t max_items = 0;  // per request
+  uint32_t C = 0;        // items in the rings
+  uint32_t R = 0;        // request slots
+  uint32_t tile_cap = 0;
+  // pinned, mapped host memory
+  sg::ServeCtl* ctl = nullptr;
+  sg::ServeTile* htiles = nullptr;
+  uint64_t* comp = nullptr;  // completion ring, R entries
+  uint64_t comp_head = 0;    // entries consumed (dispatcher)
+  uint8_t *sig = nullptr, *msg = nullptr, *pk = nullptr, *out = nullptr, *st = nullptr;
+  void* host_block = nullptr;
+  // device memory
+  void* dev_block = nullptr;
+  sg::ServeDev* dev = nullptr;
+  sg::ServeTile* tiles = nullptr;
+  uint32_t* count = nullptr;
+  cudaStream_t stream = nullptr;
+  cudaStream_t stat_stream = nullptr;  // reads of the kernel counters while it runs
+  cudaEvent_t ev_exit = nullptr;
+  bool running = false;
+  std::atomic<int> shape{0};
+  // host state, under mu
   std::mutex mu;
   std::condition_variable cond;
-  std::deque<Request*> queue;
-  size_t queued_items = 0;
-  std::unordered_map<uint64_t, Request*> reqs;
+  std::unordered_map<uint64_t, ReqPtr> handles;
+  std::vector<ReqPtr> by_slot;
+  std::vector<uint32_t> slot_total;  // running item count of each request slot (the device's count)
+  std::deque<ReqPtr> inflight;       // published, in submission order
   uint64_t next_id = 1;
+  uint32_t next_seq = 1;
+  uint64_t slots_taken = 0, published = 0;
+  uint64_t item_head = 0, item_tail = 0;  // ring positions in use: [item_head, item_tail)
+  uint64_t tile_head = 0, tile_alloc = 0, tiles_published = 0;
+  size_t queued_items = 0;
+  bool hbm_ok = true;
+  size_t hbm_floor = 0;
+  double hbm_checked = 0;
   std::thread worker;
   bool stop = false;
+  bool alive = true;    // the dispatcher runs
+  bool broken = false;  // the kernel reported an expired wait, or could not launch: requests were failed
+  int fault = 0;        // test hook: 1 = the dispatcher stops
   // stats
   uint64_t launches = 0, items_done = 0, requests_done = 0;
 };
 
 namespace {
 
+int grid_for(sigops_server* s, int shape, int* block) {
+  int b = 0;
+  cudaError_t e;
+  *block = kServeBlock[shape];
+  if (shape == 0) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, sg::serve_kernel<256, 1>, 256, 0);
+  else if (shape == 1) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, sg::serve_kernel<128, 3>, 128, 0);
+  else e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, sg::serve_kernel<256, 2>, 256, 0);
+  return e == cudaSuccess ? b * s->cv.num_sms : 0;
+}
 
-// caller holds s->mu: move queued requests into the slot while they fit
-void take_requests(sigops_server* s, Slot& sl) {
-  sl.reqs.clear();
-  size_t n = 0;
-  while (!s->queue.empty() && n + s->queue.front()->n <= s->cap) {
-    Request* r = s->queue.front();
-    s->queue.pop_front();
+// caller holds mu; the kernel is not running
+cudaError_t launch_kernel(sigops_server* s) {
+  const int shape = s->shape.load(std::memory_order_relaxed);
+  int block = 0;
+  const int grid = grid_for(s, shape, &block);
+  if (grid <= 0) return cudaErrorInvalidConfiguration;
+  sg::ServeArgs a{};
+  a.ctl = s->ctl;
+  a.htiles = s->htiles;
+  a.comp = s->comp;
+  a.sig = s->sig;
+  a.msg = s->msg;
+  a.pk = s->pk;
+  a.out = s->out;
+  a.st = s->st;
+  a.dev = s->dev;
+  a.tiles = s->tiles;
+  a.count = s->count;
+  a.R = s->R;
+  a.C = s->C;
+  a.tile_cap = s->tile_cap;
+  a.tabs = sg::BatchTables{s->cv.tabs.big[0], s->cv.tabs.big[1], s->cv.tabs.big[2], {nullptr, nullptr, nullptr}};
+  a.idle_ns = 20ull * 1000 * 1000;    // close after 20 ms without a tile
+  a.life_ns = 2000ull * 1000 * 1000;  // and after 2 s in all (the dispatcher relaunches)
+  a.warps_per_sm = (uint32_t)(grid / s->cv.num_sms) * (uint32_t)(block / 32);
+  sg::serve_reset_kernel<<<1, 1, 0, s->stream>>>(s->dev);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  void* args[] = {&a};
+  if (shape == 0) e = cudaLaunchCooperativeKernel((const void*)sg::serve_kernel<256, 1>, grid, block, args, 0, s->stream);
+  else if (shape == 1) e = cudaLaunchCooperativeKernel((const void*)sg::serve_kernel<128, 3>, grid, block, args, 0, s->stream);
+  else e = cudaLaunchCooperativeKernel((const void*)sg::serve_kernel<256, 2>, grid, block, args, 0, s->stream);
+  if (e != cudaSuccess) return e;
+  return cudaEventRecord(s->ev_exit, s->stream);
+}
+
+// caller holds mu: every request in flight fails with rc (its results are not copied)
+void fail_inflight(sigops_server* s, int rc) {
+  const double t = now_s();
+  for (ReqPtr& r : s->inflight) {
+    if (r->state == RState::Running) {
+      r->rc = rc;
+      r->state = RState::Done;
+      r->t_done = t;
+    } else if (r->state == RState::Canceled) {
+      r->state = RState::Done;
+    }
+  }
+}
+
+// caller holds mu: release finished requests at the front, in submission order
+void reclaim(sigops_server* s) {
+  while (!s->inflight.empty()) {
+    ReqPtr& r = s->inflight.front();
+    if (r->state != RState::Done) break;
+    s->item_head = r->ring_end;
+    s->tile_head = r->tile_end;
     s->queued_items -= r->n;
-    sl.reqs.push_back(r);
-    n += r->n;
+    s->by_slot[r->slot].reset();
+    s->inflight.pop_front();
   }
-  sl.n = n;
-  sl.busy = n > 0;
-}
-
-// without the lock: pack the slot's requests into pinned staging and launch
-void pack_and_launch(sigops_server* s, Slot& sl) {
-  const size_t n = sl.n;
-  const Layout& L = s->lay;
-  size_t off = 0;
-  for (Request* r : sl.reqs) {
-    if (r->curves) memcpy(sl.h + L.cur + off, r->curves, r->n);
-    else memset(sl.h + L.cur + off, r->uniform_curve, r->n);
-    memcpy(sl.h + L.sig + off * 64, r->sigs, r->n * 64);
-    memcpy(sl.h + L.msg + off * 32, r->msgs, r->n * 32);
-    if (r->pks) memcpy(sl.h + L.pk + off * 32, r->pks, r->n * 32);
-    else memset(sl.h + L.pk + off * 32, 0, r->n * 32);
-    off += r->n;
-  }
-  cudaSetDevice(s->cv.device);
-  // every call's status is kept: the first failure fails the slot's requests
-  cudaError_t e = cudaSuccess;
-  auto keep = [&e](cudaError_t r) {
-    if (e == cudaSuccess) e = r;
-  };
-  keep(cudaMemcpyAsync(sl.d + L.cur, sl.h + L.cur, n, cudaMemcpyHostToDevice, sl.stream));
-  keep(cudaMemcpyAsync(sl.d + L.sig, sl.h + L.sig, n * 64, cudaMemcpyHostToDevice, sl.stream));
-  keep(cudaMemcpyAsync(sl.d + L.msg, sl.h + L.msg, n * 32, cudaMemcpyHostToDevice, sl.stream));
-  keep(cudaMemcpyAsync(sl.d + L.pk, sl.h + L.pk, n * 32, cudaMemcpyHostToDevice, sl.stream));
-  size_t cg = (n + 255) / 256;
-  int classify_grid = (int)std::min(cg, (size_t)s->cv.num_sms * 8);
-  // grid sized to the batch (the persistent variants: one item per thread up
-  // to a full grid; the others size themselves): a light batch occupies few
-  // SMs and launches from other slots run beside it
-  const uint32_t shape = s->shape.load(std::memory_order_relaxed);
-  const int variant = (int)(shape >> 16), grid_cap = (int)(shape & 0xffffu);
-  const int block = sg::batched_variant_block(variant);
-  const int grid = (int)std::min<size_t>((size_t)grid_cap, (n + block - 1) / block);
-  keep(sg::launch_batched(sl.d + L.cur, sl.d + L.sig, sl.d + L.msg, sl.d + L.pk, n, sl.d + L.out, sl.d + L.st, sl.d_idx, sl.d_scratch,
-                          sl.d_defer, s->cv.tabs, s->cv.d_err, grid, variant, classify_grid, &sl.fork, sl.stream));
-  keep(cudaMemcpyAsync(sl.h + L.out, sl.d + L.out, n * 64, cudaMemcpyDeviceToHost, sl.stream));
-  keep(cudaMemcpyAsync(sl.h + L.st, sl.d + L.st, n, cudaMemcpyDeviceToHost, sl.stream));
-  keep(cudaEventRecord(sl.done, sl.stream));
-  if (e != cudaSuccess) {
-    for (Request* r : sl.reqs) r->rc = SIGOPS_E_CUDA;
-  }
-}
-
-void finish(sigops_server* s, Slot& sl) {
-  // caller holds s->mu
-  const Layout& L = s->lay;
-  cudaError_t e = cudaEventSynchronize(sl.done);
-  double t = now_s();
-  size_t off = 0;
-  for (Request* r : sl.reqs) {
-    if (e != cudaSuccess && r->rc == SIGOPS_OK) r->rc = SIGOPS_E_CUDA;
-    memcpy(r->out, sl.h + L.out + off * 64, r->n * 64);
-    if (r->status) memcpy(r->status, sl.h + L.st + off, r->n);
-    off += r->n;
-    r->t_done = t;
-    r->done = true;
-    s->requests_done++;
-  }
-  s->items_done += sl.n;
-  sl.reqs.clear();
-  sl.n = 0;
-  sl.busy = false;
 }
 
 void worker_loop(sigops_server* s) {
   cudaSetDevice(s->cv.device);
   std::unique_lock<std::mutex> lk(s->mu);
+  std::vector<ReqPtr> finished;
   while (!s->stop) {
-    bool progressed = false;
-    for (Slot& sl : s->slots) {
-      if (sl.busy && cudaEventQuery(sl.done) != cudaErrorNotReady) {
-        finish(s, sl);
-        progressed = true;
+    if (s->fault == 1) break;  // test hook: the dispatcher stops as if it had died
+    // completions: the kernel appends each finished request to the completion
+    // ring once its results are in the output ring
+    finished.clear();
+    for (;;) {
+      const uint64_t e = __atomic_load_n(&s->comp[s->comp_head % s->R], __ATOMIC_ACQUIRE);
+      if ((uint32_t)e != (uint32_t)(s->comp_head + 1)) break;  // not written yet
+      s->comp_head++;
+      ReqPtr& r = s->by_slot[(e >> 32) & 0xffffu];
+      if (!r || (r->seq & 0xffffu) != (uint32_t)(e >> 48)) continue;  // a request already failed on the host
+      if (r->state == RState::Canceled) {
+        r->state = RState::Done;  // results discarded
+      } else if (r->state == RState::Running) {
+        r->state = RState::Finishing;
+        finished.push_back(r);
       }
     }
-    if (progressed) s->cond.notify_all();
-    for (Slot& sl : s->slots) {
-      if (!sl.busy && !s->queue.empty()) {
-        take_requests(s, sl);
-        if (!sl.busy) continue;
+    if (!finished.empty()) {
+      lk.unlock();
+      const double t = now_s();
+      for (ReqPtr& r : finished) {
+        if (r->perm.empty()) {
+          memcpy(r->out, s->out + r->off * 64, r->n * 64);
+          if (r->status) memcpy(r->status, s->st + r->off, r->n);
+        } else {
+          for (size_t p = 0; p < r->n; ++p) {
+            memcpy(r->out + (size_t)r->perm[p] * 64, s->out + (r->off + p) * 64, 64);
+            if (r->status) r->status[r->perm[p]] = s->st[r->off + p];
+          }
+        }
+        r->t_done = t;
+      }
+      lk.lock();
+      for (ReqPtr& r : finished) {
+        r->state = RState::Done;
+        s->requests_done++;
+        s->items_done += r->n;
+      }
+    }
+    bool changed = !finished.empty();
+    // the persistent kernel: notice its exit, relaunch it when work waits
+    if (s->running && cudaEventQuery(s->ev_exit) != cudaErrorNotReady) {
+      s->running = false;
+      const uint32_t err = __atomic_exchange_n(&s->ctl->err, 0u, __ATOMIC_ACQ_REL);
+      if (err) {
+        // a device wait expired: tiles may be lost, so nothing in flight can be trusted
+        s->broken = true;
+        fail_inflight(s, SIGOPS_E_TIMEDOUT);
+        changed = true;
+      }
+    }
+    if (!s->running && !s->broken && __atomic_load_n(&s->ctl->tiles_fed, __ATOMIC_ACQUIRE) < s->tiles_published) {
+      if (launch_kernel(s) == cudaSuccess) {
+        s->running = true;
         s->launches++;
-        lk.unlock();
-        pack_and_launch(s, sl);  // request buffers stay valid until completion
-        lk.lock();
-        progressed = true;
+      } else {
+        s->broken = true;
+        fail_inflight(s, SIGOPS_E_CUDA);
+        changed = true;
       }
     }
-    if (!progressed) {
-      bool any_busy = false;
-      for (Slot& sl : s->slots) any_busy |= sl.busy;
-      // poll completions every 20 us while work is in flight; otherwise sleep until a submit
-      if (any_busy) s->cond.wait_for(lk, std::chrono::microseconds(20));
-      else s->cond.wait_for(lk, std::chrono::milliseconds(5));
+    reclaim(s);
+    if (changed) s->cond.notify_all();
+    // admission by device memory: free memory re-read every 100 ms
+    const double t = now_s();
+    if (t - s->hbm_checked > 0.1) {
+      size_t free_b = 0, total_b = 0;
+      if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess) s->hbm_ok = free_b >= s->hbm_floor;
+      s->hbm_checked = t;
     }
+    // poll completions every 20 us while requests are in flight
+    if (!s->inflight.empty()) s->cond.wait_for(lk, std::chrono::microseconds(20));
+    else s->cond.wait_for(lk, std::chrono::milliseconds(5));
   }
-  for (Slot& sl : s->slots)
-    if (sl.busy) finish(s, sl);
+  s->alive = false;
+  s->cond.notify_all();
+}
+
+template <class T>
+T* carve(uint8_t*& p, size_t count) {
+  T* r = reinterpret_cast<T*>(p);
+  p += (count * sizeof(T) + 255) & ~(size_t)255;
+  return r;
 }
 
 }  // namespace
 
 extern "C" {
 
-static int set_shape(sigops_server* s, int variant) {
-  const int bps = sg::batched_max_blocks_per_sm(variant);
-  if (bps <= 0) return SIGOPS_E_INVAL;
-  const uint32_t grid_cap = std::min<uint32_t>(0xffffu, (uint32_t)(s->cv.num_sms * bps));
-  s->shape.store(((uint32_t)variant << 16) | grid_cap, std::memory_order_relaxed);
-  return SIGOPS_OK;
-}
-
 int sigops_server_set_variant(sigops_server* s, int variant) {
-  if (!s || variant < 0 || variant >= sg::BATCHED_VARIANTS) return SIGOPS_E_INVAL;
-  return set_shape(s, variant);
+  if (!s || variant < 0 || variant >= kServeShapes) return SIGOPS_E_INVAL;
+  s->shape.store(variant, std::memory_order_relaxed);
+  return SIGOPS_OK;
 }
 
 sigops_server* sigops_server_create(sigops_ctx* ctx, int nslots, size_t slot_items, double hbm_fraction) {
   sg::CtxView v;
   if (!ctx || sg::ctx_view(ctx, &v) != SIGOPS_OK) return nullptr;
-  if (nslots <= 0) nslots = 8;
-  if (nslots > 16) nslots = 16;
+  if (nslots <= 0) nslots = 32;
+  if (slot_items == 0) slot_items = 16384;
   if (hbm_fraction <= 0 || hbm_fraction > 0.9) hbm_fraction = 0.25;
+  if (slot_items > (1u << 20) || (size_t)nslots * slot_items > (1u << 24)) return nullptr;
   cudaSetDevice(v.device);
   size_t free_b = 0, total_b = 0;
   if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return nullptr;
-  const size_t per_item = 1 + 64 + 32 + 32 + 64 + 1 + 3 * 4;
-  size_t budget_items = (size_t)(free_b * hbm_fraction) / per_item;
-  if (slot_items == 0) slot_items = std::min<size_t>(budget_items / nslots, 1u << 14);
-  if (slot_items == 0 || slot_items * nslots > budget_items) return nullptr;
-  sigops_server* s = new sigops_server();
+  std::unique_ptr<sigops_server> s(new sigops_server());
   s->ctx = ctx;
   s->cv = v;
-  s->cap = slot_items;
-  s->queue_bound = std::max<size_t>(slot_items * 64, budget_items);
-  s->lay = layout(slot_items);
-  if (set_shape(s, 1) != SIGOPS_OK) {
-    delete s;
+  s->max_items = slot_items;
+  s->R = 1u << 16;
+  // items in the rings: slots x slot_items, within hbm_fraction of free device
+  // memory (a share of the device tile ring per item)
+  const size_t per_item_dev = 2 * sizeof(sg::ServeTile) / 32 + 1;
+  size_t C = (size_t)nslots * slot_items;
+  C = std::min(C, (size_t)(free_b * hbm_fraction) / per_item_dev);
+  if (C < slot_items) return nullptr;
+  s->C = (uint32_t)C;
+  uint32_t cap = 1;
+  while (cap < C / 32 + 3ull * std::min<size_t>(s->R, C) + 64) cap <<= 1;  // never the limit before the item ring
+  s->tile_cap = cap;
+  s->hbm_floor = std::max<size_t>(256ull << 20, total_b / 100);
+  // pinned, mapped host rings
+  const size_t host_bytes = 4096 + (((size_t)cap * sizeof(sg::ServeTile) + 255) & ~(size_t)255) + ((s->R * 8 + 255) & ~(size_t)255) +
+                            C * (64 + 32 + 32 + 64 + 1) + 5 * 256;
+  if (sg::host_alloc(&s->host_block, host_bytes, cudaHostAllocMapped | cudaHostAllocPortable) != cudaSuccess) return nullptr;
+  memset(s->host_block, 0, host_bytes);
+  uint8_t* hp = static_cast<uint8_t*>(s->host_block);
+  s->ctl = carve<sg::ServeCtl>(hp, 1);
+  hp = static_cast<uint8_t*>(s->host_block) + 4096;
+  s->htiles = carve<sg::ServeTile>(hp, cap);
+  s->comp = carve<uint64_t>(hp, s->R);
+  s->sig = carve<uint8_t>(hp, C * 64);
+  s->msg = carve<uint8_t>(hp, C * 32);
+  s->pk = carve<uint8_t>(hp, C * 32);
+  s->out = carve<uint8_t>(hp, C * 64);
+  s->st = carve<uint8_t>(hp, C);
+  // device-resident queue
+  auto rounded = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  const size_t dev_bytes = rounded(sizeof(sg::ServeDev)) + rounded(3 * (size_t)cap * sizeof(sg::ServeTile)) + rounded(s->R * 4);
+  if (sg::dev_alloc(&s->dev_block, dev_bytes) != cudaSuccess) {
+    sg::host_free(s->host_block);
+    s->host_block = nullptr;
     return nullptr;
   }
-  s->slots.resize(nslots);
-  for (Slot& sl : s->slots) {
-    bool ok = cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking) == cudaSuccess &&
-              sg::fork_streams_create(&sl.fork) == cudaSuccess &&
-              cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming) == cudaSuccess &&
-              cudaMallocHost(&sl.h, s->lay.total) == cudaSuccess && cudaMalloc(&sl.d, s->lay.total) == cudaSuccess &&
-              cudaMalloc(&sl.d_scratch, sg::batched_scratch_bytes()) == cudaSuccess &&
-              cudaMalloc(&sl.d_idx, 3 * slot_items * sizeof(uint32_t)) == cudaSuccess &&
-              cudaMalloc(&sl.d_defer, sg::batched_defer_bytes(slot_items)) == cudaSuccess;
-    if (!ok) {
-      sigops_server_destroy(s);
-      return nullptr;
-    }
+  uint8_t* dp = static_cast<uint8_t*>(s->dev_block);
+  s->dev = carve<sg::ServeDev>(dp, 1);
+  s->tiles = carve<sg::ServeTile>(dp, 3 * (size_t)cap);
+  s->count = carve<uint32_t>(dp, s->R);
+  int block = 0;
+  const bool ok = cudaMemset(s->dev_block, 0, dev_bytes) == cudaSuccess &&
+                  cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) == cudaSuccess &&
+                  cudaStreamCreateWithFlags(&s->stat_stream, cudaStreamNonBlocking) == cudaSuccess &&
+                  cudaEventCreateWithFlags(&s->ev_exit, cudaEventDisableTiming) == cudaSuccess && grid_for(s.get(), 0, &block) > 0 &&
+                  cudaDeviceSynchronize() == cudaSuccess;
+  if (!ok) {
+    s->alive = false;
+    sigops_server_destroy(s.release());
+    return nullptr;
   }
-  s->reqs.reserve(1u << 14);  // in-flight handles of a typical client without a rehash
-  s->worker = std::thread(worker_loop, s);
-  return s;
+  s->by_slot.resize(s->R);
+  s->slot_total.assign(s->R, 0);
+  s->handles.reserve(1u << 14);  // in-flight handles of a typical client without a rehash
+  sigops_server* p = s.release();
+  p->worker = std::thread(worker_loop, p);
+  return p;
 }
 
 void sigops_server_destroy(sigops_server* s) {
@@ -292,72 +383,152 @@ void sigops_server_destroy(sigops_server* s) {
   s->cond.notify_all();
   if (s->worker.joinable()) s->worker.join();
   cudaSetDevice(s->cv.device);
-  for (Slot& sl : s->slots) {
-    if (sl.stream) cudaStreamSynchronize(sl.stream);
-    if (sl.done) cudaEventDestroy(sl.done);
-    sg::fork_streams_destroy(&sl.fork);
-    if (sl.stream) cudaStreamDestroy(sl.stream);
-    if (sl.h) cudaFreeHost(sl.h);
-    if (sl.d) cudaFree(sl.d);
-    if (sl.d_scratch) cudaFree(sl.d_scratch);
-    if (sl.d_idx) cudaFree(sl.d_idx);
-    if (sl.d_defer) cudaFree(sl.d_defer);
-  }
-  for (auto& kv : s->reqs) delete kv.second;
+  if (s->ctl) __atomic_store_n(&s->ctl->stop, 1u, __ATOMIC_RELEASE);  // the kernel closes within microseconds
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  if (s->ev_exit) cudaEventDestroy(s->ev_exit);
+  if (s->stream) cudaStreamDestroy(s->stream);
+  if (s->stat_stream) cudaStreamDestroy(s->stat_stream);
+  if (s->dev_block) sg::dev_free(s->dev_block);
+  if (s->host_block) sg::host_free(s->host_block);
   delete s;
 }
 
-size_t sigops_server_slot_items(sigops_server* s) { return s ? s->cap : 0; }
+size_t sigops_server_slot_items(sigops_server* s) { return s ? s->max_items : 0; }
 
 int sigops_server_submit(sigops_server* s, const uint8_t* curves, int uniform_curve, const uint8_t* sigs, const uint8_t* msgs,
                          const uint8_t* pks, size_t n, uint8_t* out, uint8_t* status, uint64_t* handle) {
   if (!s || !sigs || !msgs || !out || !handle || n == 0) return SIGOPS_E_INVAL;
   if (!curves && (uniform_curve < 0 || uniform_curve > 2)) return SIGOPS_E_INVAL;
   if (!curves && uniform_curve == SIGOPS_ED25519 && !pks) return SIGOPS_E_INVAL;
-  if (n > s->cap) return SIGOPS_E_RANGE;
-  Request* r = new Request();
-  r->curves = curves;
-  r->uniform_curve = curves ? -1 : uniform_curve;
-  r->sigs = sigs;
-  r->msgs = msgs;
-  r->pks = pks;
-  r->n = n;
-  r->out = out;
-  r->status = status;
+  if (n > s->max_items) return SIGOPS_E_RANGE;
+  // items per curve; a request already in curve order is copied as it is
+  size_t cnt[3] = {0, 0, 0};
+  bool grouped = true;
+  if (curves) {
+    for (size_t i = 0; i < n; ++i) {
+      if (curves[i] > 2) return SIGOPS_E_INVAL;
+      cnt[curves[i]]++;
+      if (i && curves[i] < curves[i - 1]) grouped = false;
+    }
+  } else {
+    cnt[uniform_curve] = n;
+  }
+  ReqPtr r = std::make_shared<Request>();
   {
     std::lock_guard<std::mutex> g(s->mu);
-    if (s->queued_items + n > s->queue_bound) {
-      delete r;
-      return SIGOPS_E_BUSY;
-    }
+    if (!s->alive || s->broken) return SIGOPS_E_CUDA;
+    if (!s->hbm_ok) return SIGOPS_E_BUSY;
+    const uint32_t slot = (uint32_t)(s->slots_taken % s->R);
+    if (s->by_slot[slot]) return SIGOPS_E_BUSY;  // request slots full
+    // a contiguous run of n items in the rings, wrapping to the start when the end is short
+    const uint64_t pos = s->item_tail % s->C;
+    const uint64_t skip = pos + n > s->C ? s->C - pos : 0;
+    if (s->item_tail - s->item_head + skip + n > s->C) return SIGOPS_E_BUSY;  // item rings full
+    const uint64_t ntiles = (cnt[0] + 31) / 32 + (cnt[1] + 31) / 32 + (cnt[2] + 31) / 32;
+    if (s->tile_alloc - s->tile_head + ntiles > s->tile_cap) return SIGOPS_E_BUSY;  // tile rings full
+    r->tile_first = s->tile_alloc;
+    s->tile_alloc += ntiles;
+    r->tile_end = s->tile_alloc;
     r->id = s->next_id++;
-    r->t_submit = now_s();
-    s->reqs[r->id] = r;
-    s->queue.push_back(r);
+    r->slot = slot;
+    r->seq = s->next_seq++;
+    r->off = (size_t)((pos + skip) % s->C);
+    r->n = n;
+    s->item_tail += skip + n;
+    r->ring_end = s->item_tail;
+    r->out = out;
+    r->status = status;
+    s->by_slot[slot] = r;
+    s->handles[r->id] = r;
+    s->slots_taken++;
     s->queued_items += n;
     *handle = r->id;
+  }
+  // inputs into the pinned ring grouped by curve (secp256k1, P-256, ed25519),
+  // outside the lock: the slot, the items and the tiles are this request's
+  const size_t o = r->off;
+  if (grouped) {
+    memcpy(s->sig + o * 64, sigs, n * 64);
+    memcpy(s->msg + o * 32, msgs, n * 32);
+    if (pks) memcpy(s->pk + o * 32, pks, n * 32);
+    else memset(s->pk + o * 32, 0, n * 32);
+  } else {
+    r->perm.resize(n);
+    size_t pos[3] = {0, cnt[0], cnt[0] + cnt[1]};
+    for (size_t i = 0; i < n; ++i) {
+      const size_t p = pos[curves[i]]++;
+      r->perm[p] = (uint32_t)i;
+      memcpy(s->sig + (o + p) * 64, sigs + i * 64, 64);
+      memcpy(s->msg + (o + p) * 32, msgs + i * 32, 32);
+      if (pks) memcpy(s->pk + (o + p) * 32, pks + i * 32, 32);
+      else memset(s->pk + (o + p) * 32, 0, 32);
+    }
+  }
+  // tiles of at most 32 items of one curve; the last one of the request to
+  // finish brings the slot's running count to the target
+  const uint32_t target = s->slot_total[r->slot] + (uint32_t)n;  // wraps like the device's counter
+  s->slot_total[r->slot] = target;
+  {
+    uint64_t t = r->tile_first;
+    size_t base = o;
+    for (uint32_t k = 0; k < 3; ++k) {
+      for (size_t b = 0; b < cnt[k]; b += 32, ++t) {
+        const uint32_t c = (uint32_t)std::min<size_t>(32, cnt[k] - b);
+        s->htiles[t % s->tile_cap] = sg::ServeTile{r->slot | (c << 16) | (k << 24), (uint32_t)(base + b), r->seq, target};
+      }
+      base += cnt[k];
+    }
+  }
+  {
+    // publish in submission order: the tile tail advances over the ready prefix
+    std::lock_guard<std::mutex> g(s->mu);
+    r->ready = true;
+    r->t_submit = now_s();
+    while (s->published < s->slots_taken) {
+      ReqPtr& q = s->by_slot[s->published % s->R];
+      if (!q || !q->ready) break;
+      if (q->state == RState::Copying) q->state = RState::Running;  // (a request cancelled while copying stays Canceled)
+      s->inflight.push_back(q);
+      s->published++;
+      s->tiles_published = q->tile_end;
+    }
+    __atomic_store_n(&s->ctl->tile_tail, s->tiles_published, __ATOMIC_RELEASE);
+    if (s->broken) fail_inflight(s, SIGOPS_E_CUDA);  // admitted before the kernel failed: nothing will run it
   }
   s->cond.notify_all();
   return SIGOPS_OK;
 }
 
-// Wait for a request; returns its result code (SIGOPS_OK), SIGOPS_E_TIMEDOUT
-// if it is still running after timeout_ms (< 0: wait indefinitely), or
-// SIGOPS_E_INVAL for an unknown handle.  A finished request is released.
 int sigops_server_wait(sigops_server* s, uint64_t handle, int timeout_ms, double* latency_ms) {
   if (!s) return SIGOPS_E_INVAL;
   std::unique_lock<std::mutex> lk(s->mu);
-  auto it = s->reqs.find(handle);
-  if (it == s->reqs.end()) return SIGOPS_E_INVAL;
-  Request* r = it->second;
-  auto pred = [&] { return r->done; };
+  auto it = s->handles.find(handle);
+  if (it == s->handles.end()) return SIGOPS_E_INVAL;
+  ReqPtr r = it->second;
+  auto pred = [&] { return r->state == RState::Done || r->canceled || !s->alive; };
   if (timeout_ms < 0) s->cond.wait(lk, pred);
   else if (!s->cond.wait_for(lk, std::chrono::milliseconds(timeout_ms), pred)) return SIGOPS_E_TIMEDOUT;
+  if (r->canceled) return SIGOPS_E_CANCELED;
+  if (r->state != RState::Done) return SIGOPS_E_TIMEDOUT;  // the dispatcher stopped: the request cannot finish
   if (latency_ms) *latency_ms = (r->t_done - r->t_submit) * 1e3;
-  int rc = r->rc;
-  s->reqs.erase(it);
-  delete r;
-  return rc;
+  s->handles.erase(handle);
+  return r->rc;
+}
+
+int sigops_server_cancel(sigops_server* s, uint64_t handle) {
+  if (!s) return SIGOPS_E_INVAL;
+  std::unique_lock<std::mutex> lk(s->mu);
+  auto it = s->handles.find(handle);
+  if (it == s->handles.end()) return SIGOPS_E_INVAL;
+  ReqPtr r = it->second;
+  // results being copied into the caller's buffers: let the copy finish
+  s->cond.wait(lk, [&] { return r->state != RState::Finishing || !s->alive; });
+  if (r->state == RState::Done) return SIGOPS_ALREADY_DONE;
+  r->canceled = true;
+  if (r->state == RState::Running || r->state == RState::Copying) r->state = RState::Canceled;  // the device still works it off
+  s->handles.erase(it);
+  s->cond.notify_all();
+  return SIGOPS_OK;
 }
 
 int sigops_server_stats(sigops_server* s, uint64_t* launches, uint64_t* requests_done, uint64_t* items_done, size_t* queued_items) {
@@ -370,53 +541,89 @@ int sigops_server_stats(sigops_server* s, uint64_t* launches, uint64_t* requests
   return SIGOPS_OK;
 }
 
+int sigops_server_kernel_stats(sigops_server* s, uint64_t* tiles, uint64_t* items, double* work_s, double* idle_s, uint64_t* sm_moves) {
+  if (!s) return SIGOPS_E_INVAL;
+  unsigned long long v[6] = {0, 0, 0, 0, 0, 0};
+  cudaSetDevice(s->cv.device);
+  if (cudaMemcpyAsync(v, &s->dev->tiles_done, sizeof(v), cudaMemcpyDeviceToHost, s->stat_stream) != cudaSuccess ||
+      cudaStreamSynchronize(s->stat_stream) != cudaSuccess)
+    return SIGOPS_E_CUDA;
+  if (tiles) *tiles = v[0];
+  if (items) *items = v[1];
+  if (work_s) *work_s = v[2] * 1e-9;
+  if (idle_s) *idle_s = v[3] * 1e-9;
+  if (sm_moves) *sm_moves = v[4] + v[5];
+  return SIGOPS_OK;
+}
+
+int sigops_server_test_fault(sigops_server* s, int fault) {
+  if (!s || fault < 0 || fault > 1) return SIGOPS_E_INVAL;
+  {
+    std::lock_guard<std::mutex> g(s->mu);
+    s->fault = fault;
+  }
+  s->cond.notify_all();
+  return SIGOPS_OK;
+}
+
 // Open-loop load: request i covers items [offset[i], offset[i] + count[i]) of
 // the pool and is submitted at arrival_s[i] seconds after the start (arrivals
-// in non-decreasing order); outputs land at the same item positions.  Fills
-// latency_ms[i] (submit -> results in host memory) and the wall time from
-// the first submission to the last completion.  Returns SIGOPS_E_BUSY if
-// admission refused a request (its latency is set to -1).
+// in non-decreasing order) by client thread i mod kLoadClients, as concurrent
+// clients of a server would; outputs land at the same item positions.  Fills
+// latency_ms[i] (submit -> results in host memory) and the wall time from the
+// start to the last completion.  Returns SIGOPS_E_BUSY if admission refused a
+// request (its latency is set to -1).
 int sigops_server_run_load(sigops_server* s, const uint8_t* curves, const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks,
                            const uint64_t* offset, const uint32_t* count, const double* arrival_s, size_t nreq, uint8_t* out,
                            uint8_t* status, double* latency_ms, double* wall_s) {
   if (!s || !curves || !sigs || !msgs || !pks || !offset || !count || !arrival_s || !out || !latency_ms) return SIGOPS_E_INVAL;
+  constexpr size_t kLoadClients = 4;
   std::vector<uint64_t> handles(nreq, 0);
-  int rc = SIGOPS_OK;
   {
     // every request of the run is registered before the first wait: size the
-    // handle table once, so that no rehash (which holds the server's lock for
-    // milliseconds at a few hundred thousand entries) stalls the worker
+    // handle table once, so that no rehash stalls the dispatcher
     std::lock_guard<std::mutex> g(s->mu);
-    s->reqs.reserve(s->reqs.size() + nreq);
+    s->handles.reserve(s->handles.size() + nreq);
   }
+  std::atomic<int> rc{SIGOPS_OK};
   const double t0 = now_s();
-  for (size_t i = 0; i < nreq; ++i) {
-    double target = t0 + arrival_s[i];
-    for (;;) {
-      double t = now_s();
-      if (t >= target) break;
-      if (target - t > 200e-6) std::this_thread::sleep_for(std::chrono::microseconds((int)((target - t - 100e-6) * 1e6)));
+  auto client = [&](size_t first) {
+    for (size_t i = first; i < nreq; i += kLoadClients) {
+      const double target = t0 + arrival_s[i];
+      for (;;) {
+        const double t = now_s();
+        if (t >= target) break;
+        if (target - t > 200e-6) std::this_thread::sleep_for(std::chrono::microseconds((int)((target - t - 100e-6) * 1e6)));
+      }
+      const size_t o = offset[i];
+      const int r = sigops_server_submit(s, curves + o, -1, sigs + o * 64, msgs + o * 32, pks + o * 32, count[i], out + o * 64,
+                                         status ? status + o : nullptr, &handles[i]);
+      if (r != SIGOPS_OK) {
+        handles[i] = 0;
+        int ok = SIGOPS_OK;
+        rc.compare_exchange_strong(ok, r);
+      }
     }
-    size_t o = offset[i];
-    int r = sigops_server_submit(s, curves + o, -1, sigs + o * 64, msgs + o * 32, pks + o * 32, count[i], out + o * 64,
-                                 status ? status + o : nullptr, &handles[i]);
-    if (r != SIGOPS_OK) {
-      handles[i] = 0;
-      rc = r;
-    }
-  }
+  };
+  std::vector<std::thread> clients;
+  for (size_t j = 1; j < std::min(kLoadClients, nreq); ++j) clients.emplace_back(client, j);
+  client(0);
+  for (std::thread& c : clients) c.join();
   for (size_t i = 0; i < nreq; ++i) {
     if (!handles[i]) {
       latency_ms[i] = -1;
       continue;
     }
     double lat = 0;
-    int r = sigops_server_wait(s, handles[i], -1, &lat);
+    const int r = sigops_server_wait(s, handles[i], -1, &lat);
     latency_ms[i] = lat;
-    if (r != SIGOPS_OK && rc == SIGOPS_OK) rc = r;
+    if (r != SIGOPS_OK) {
+      int ok = SIGOPS_OK;
+      rc.compare_exchange_strong(ok, r);
+    }
   }
   if (wall_s) *wall_s = now_s() - t0;
-  return rc;
+  return rc.load();
 }
 
 }  // extern "C"

@@ -28,6 +28,8 @@ pub const SIGOPS_E_TABLE: c_int = -74;
 pub const SIGOPS_E_TIMEDOUT: c_int = -110;
 pub const SIGOPS_E_BUSY: c_int = -16;
 pub const SIGOPS_E_RANGE: c_int = -34;
+pub const SIGOPS_E_CANCELED: c_int = -125;
+pub const SIGOPS_ALREADY_DONE: c_int = 1;
 
 pub const SIGOPS_SECP256K1: c_int = 0;
 pub const SIGOPS_SECP256R1: c_int = 1;
@@ -100,6 +102,10 @@ extern "C" {
     pub fn sigops_server_submit(server: *mut SigopsServer, curves: *const u8, uniform_curve: c_int, sigs: *const u8, msgs: *const u8,
                                 pks: *const u8, n: usize, out: *mut u8, status: *mut u8, handle: *mut u64) -> c_int;
     pub fn sigops_server_wait(server: *mut SigopsServer, handle: u64, timeout_ms: c_int, latency_ms: *mut f64) -> c_int;
+    pub fn sigops_server_cancel(server: *mut SigopsServer, handle: u64) -> c_int;
+    pub fn sigops_server_kernel_stats(server: *mut SigopsServer, tiles: *mut u64, items: *mut u64, work_s: *mut f64,
+        idle_s: *mut f64, sm_moves: *mut u64) -> c_int;
+    pub fn sigops_server_test_fault(server: *mut SigopsServer, fault: c_int) -> c_int;
     pub fn sigops_server_stats(server: *mut SigopsServer, launches: *mut u64, requests_done: *mut u64, items_done: *mut u64,
                                queued_items: *mut usize) -> c_int;
     pub fn sigops_server_run_load(server: *mut SigopsServer, curves: *const u8, sigs: *const u8, msgs: *const u8, pks: *const u8,
@@ -121,4 +127,5 @@ extern "C" {
     pub fn sigops_test_field(ctx: *mut SigopsCtx, field: c_int, op: c_int, a: *const u8, b: *const u8, out: *mut u8, n: usize) -> c_int;
     pub fn sigops_test_sha512(ctx: *mut SigopsCtx, input: *const u8, out: *mut u8, n: usize) -> c_int;
     pub fn sigops_test_wait_expiry(ctx: *mut SigopsCtx, max_polls: u32) -> c_int;
+    pub fn sigops_test_fail_allocations(count: c_int) -> c_int;
 }

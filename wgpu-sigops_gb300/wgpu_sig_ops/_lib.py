@@ -22,6 +22,8 @@ SIGOPS_E_TABLE = -74
 SIGOPS_E_TIMEDOUT = -110
 SIGOPS_E_BUSY = -16
 SIGOPS_E_RANGE = -34
+SIGOPS_E_CANCELED = -125
+SIGOPS_ALREADY_DONE = 1
 
 SECP256K1, SECP256R1, ED25519 = 0, 1, 2
 
@@ -69,6 +71,10 @@ SIGNATURES = {
     "sigops_server_set_variant": (ctypes.c_int, [_vp, ctypes.c_int]),
     "sigops_server_submit": (ctypes.c_int, [_vp, _vp, ctypes.c_int, _vp, _vp, _vp, _sz, _vp, _vp, ctypes.POINTER(ctypes.c_uint64)]),
     "sigops_server_wait": (ctypes.c_int, [_vp, ctypes.c_uint64, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
+    "sigops_server_cancel": (ctypes.c_int, [_vp, ctypes.c_uint64]),
+    "sigops_server_kernel_stats": (ctypes.c_int, [_vp, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "sigops_server_test_fault": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "sigops_test_fail_allocations": (ctypes.c_int, [ctypes.c_int]),
     "sigops_server_stats": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64),
                                            ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(_sz)]),
     "sigops_server_run_load": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp, _vp, _vp, ctypes.POINTER(ctypes.c_double)]),

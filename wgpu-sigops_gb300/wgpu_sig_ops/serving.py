@@ -1,10 +1,15 @@
 """Continuous-batching serving loop (``sigops_server_*`` in libsigops.so).
 
-``Server`` queues verification requests; a native dispatcher thread keeps
-several batches in flight and packs requests that arrive meanwhile into the
-next free slot.  ``measure`` drives the serving benchmark: saturation
-throughput first (a closed backlog), then Poisson arrivals at fractions of it,
-reporting throughput and p50 / p99 / p99.9 request latency per load level.
+``Server`` queues verification requests.  Submit copies a request into
+pinned, mapped request rings and cuts it into 32-item single-curve tiles; one
+persistent kernel, resident on every SM, pulls published tiles into a
+device-resident tile ring and works them off, so requests that arrive while
+others run cost no launch and no host round trip.  A native dispatcher thread
+copies finished requests' results out and relaunches the kernel after it
+closes (20 ms idle or 2 s of life).  ``measure`` drives the serving
+benchmark: saturation throughput first (a closed backlog), then Poisson
+arrivals at fractions of it, reporting throughput and p50 / p99 / p99.9
+request latency per load level.
 """
 
 from __future__ import annotations
@@ -14,14 +19,18 @@ import ctypes
 import numpy as np
 
 from ._batch import ptr
-from ._lib import check, lib
+from ._lib import SIGOPS_ALREADY_DONE, SIGOPS_OK, check, lib
 
 _u64p = ctypes.POINTER(ctypes.c_uint64)
 _dblp = ctypes.POINTER(ctypes.c_double)
 
 
 class Server:
-    def __init__(self, ctx, slots: int = 8, slot_items: int = 0, hbm_fraction: float = 0.25, variant: int | None = None):
+    """slot_items: the largest request (0 = 16,384); slots x slot_items items
+    may be in flight.  variant: shape of the persistent kernel, 0 = 256-thread
+    blocks one per SM, 1 = 128 x 3 per SM, 2 = 256 x 2 per SM."""
+
+    def __init__(self, ctx, slots: int = 32, slot_items: int = 0, hbm_fraction: float = 0.25, variant: int | None = None):
         self.ctx = ctx
         self.ptr = lib.sigops_server_create(ctx.ptr, slots, slot_items, hbm_fraction)
         if not self.ptr:
@@ -32,7 +41,7 @@ class Server:
             self.set_variant(variant)
 
     def set_variant(self, variant: int):
-        """Batched-engine launch variant of the server's launches (next launch on)."""
+        """Shape of the persistent kernel (0..2), from its next launch on."""
         check(lib.sigops_server_set_variant(self.ptr, variant), "sigops_server_set_variant")
 
     def submit(self, curves, sigs: np.ndarray, msgs: np.ndarray, pks: np.ndarray | None = None) -> int:
@@ -63,6 +72,33 @@ class Server:
         check(lib.sigops_server_wait(self.ptr, handle, timeout_ms, ctypes.byref(lat)), "sigops_server_wait")
         bufs = self._live.pop(handle)
         return bufs[4], bufs[5], lat.value
+
+    def cancel(self, handle: int) -> bool:
+        """Withdraw a request.  True when it was cancelled (its buffers are
+        released), False when it had already finished (wait() returns it)."""
+        rc = lib.sigops_server_cancel(self.ptr, handle)
+        if rc == SIGOPS_OK:
+            self._live.pop(handle, None)
+            return True
+        if rc == SIGOPS_ALREADY_DONE:
+            return False
+        check(rc, "sigops_server_cancel")
+        return False
+
+    def kernel_stats(self) -> dict:
+        """Counters of the persistent kernel: tiles, items, warp-seconds working
+        and looking for work, and the busy fraction."""
+        t, i, mv = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
+        w, d = ctypes.c_double(), ctypes.c_double()
+        check(lib.sigops_server_kernel_stats(self.ptr, ctypes.byref(t), ctypes.byref(i), ctypes.byref(w), ctypes.byref(d),
+                                             ctypes.byref(mv)), "sigops_server_kernel_stats")
+        tot = w.value + d.value
+        return {"tiles": t.value, "items": i.value, "work_s": w.value, "idle_s": d.value, "sm_moves": mv.value,
+                "busy_fraction": w.value / tot if tot > 0 else 0.0}
+
+    def test_fault(self, fault: int):
+        """Failure injection on the host (1: the dispatcher thread stops)."""
+        check(lib.sigops_server_test_fault(self.ptr, fault), "sigops_server_test_fault")
 
     def stats(self) -> dict:
         a, b, c = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
@@ -139,20 +175,26 @@ def request_stream(regions: dict, rate_rps: float, seconds: float, seed: int, ma
     return offsets, sizes.astype(np.uint32), arrivals
 
 
-def measure(ctx, W, loads=(0.25, 0.5, 0.75, 0.9), seconds: float = 10.0, seed: int = 5001, slots: int = 8,
+def measure(ctx, W, loads=(0.25, 0.5, 0.75, 0.9), seconds: float = 10.0, seed: int = 5001, slots: int = 0,
             slot_items: int = 0, sat_items: int = 2_000_000, variant: int | None = None, warmup_seconds: float = 1.0) -> dict:
     """Saturation, a discarded warm-up run at half load, then open-loop Poisson
-    load levels; latency percentiles in ms."""
+    load levels; latency percentiles in ms.  slots = 0 sizes the request rings
+    to hold the whole saturation backlog (plus 10%)."""
     pool, regions = curve_sorted_pool(W)
+    per = slot_items or 16384
+    if slots <= 0:
+        slots = max(8, int(np.ceil(1.1 * sat_items / per)))
     srv = Server(ctx, slots=slots, slot_items=slot_items, variant=variant)
     try:
         mean_size = float(np.mean(np.clip(np.floor(np.exp(np.random.default_rng(1).uniform(0, np.log(2048), 200000))), 1, 2048)))
-        n_sat = max(64, int(sat_items / mean_size))
+        # the backlog must fit the rings, or its tail is refused
+        cap_items = 0.9 * slots * srv.slot_items
+        n_sat = max(64, int(min(sat_items, cap_items) / mean_size))
         offs, cnts, arr = request_stream(regions, 0.0, 0.0, seed, n_requests=n_sat)
         rc, lat, wall, out, st = srv.run_load(pool, offs, cnts, arr)
         check(rc, "saturation run")
-        sat = float(cnts.sum()) / wall
-        res = {"saturation_sigs_per_s": sat, "mean_request_items": mean_size, "slot_items": srv.slot_items, "slots": slots, "variant": 1 if variant is None else variant,
+        sat = float(cnts[lat >= 0].sum()) / wall
+        res = {"saturation_sigs_per_s": sat, "mean_request_items": mean_size, "slot_items": srv.slot_items, "slots": slots, "kernel_shape": 0 if variant is None else variant,
                "seconds_per_level": seconds, "warmup_seconds": warmup_seconds, "levels": []}
         if warmup_seconds > 0:  # an open-loop run at half load whose latencies are discarded
             offs, cnts, arr = request_stream(regions, 0.5 * sat / mean_size, warmup_seconds, seed + 100)
@@ -160,14 +202,20 @@ def measure(ctx, W, loads=(0.25, 0.5, 0.75, 0.9), seconds: float = 10.0, seed: i
         for k, load in enumerate(loads):
             rate = load * sat / mean_size
             offs, cnts, arr = request_stream(regions, rate, seconds, seed + 1 + k)
+            k0 = srv.kernel_stats()
             rc, lat, wall, out, st = srv.run_load(pool, offs, cnts, arr)
+            k1 = srv.kernel_stats()
             ok = lat >= 0
+            work, idle, tiles = k1["work_s"] - k0["work_s"], k1["idle_s"] - k0["idle_s"], k1["tiles"] - k0["tiles"]
             res["levels"].append({
                 "load": load, "offered_sigs_per_s": float(cnts.sum()) / seconds, "achieved_sigs_per_s": float(cnts[ok].sum()) / wall,
                 "requests": int(len(lat)), "refused": int((~ok).sum()),
                 "p50_ms": float(np.percentile(lat[ok], 50)), "p99_ms": float(np.percentile(lat[ok], 99)),
-                "p999_ms": float(np.percentile(lat[ok], 99.9)), "rc": int(rc)})
+                "p999_ms": float(np.percentile(lat[ok], 99.9)), "rc": int(rc),
+                "kernel_busy": work / (work + idle) if work + idle > 0 else 0.0,
+                "warp_ms_per_tile": 1e3 * work / tiles if tiles else 0.0, "sm_moves": k1["sm_moves"] - k0["sm_moves"]})
         res["stats"] = srv.stats()
+        res["kernel_stats"] = srv.kernel_stats()
         return res
     finally:
         srv.close()
