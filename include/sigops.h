@@ -311,11 +311,19 @@ int sigops_server_stats(sigops_server* server, uint64_t* launches, uint64_t* req
 int sigops_server_kernel_stats(sigops_server* server, uint64_t* tiles, uint64_t* items, double* work_s, double* idle_s,
                                uint64_t* sm_moves);
 
+/* The dispatcher thread: iterations so far, the longest time between two
+ * iterations with requests in flight and the longest driver call it made
+ * (kernel relaunch, exit check), both since the previous call (ms; waiting
+ * threads also collect completions, so a late dispatcher delays relaunches
+ * rather than results).  No counterpart in the reference. */
+int sigops_server_dispatch_stats(sigops_server* server, uint64_t* iterations, double* max_gap_ms, double* max_driver_ms);
+
 /* Open-loop load generator: request i covers pool items
  * [offset[i], offset[i] + count[i]) and is submitted arrival_s[i] seconds after
  * the start (non-decreasing) by one of four client threads (request i by
- * thread i mod 4); outputs go to the same item positions of out / status.
- * Fills latency_ms[i] (-1 when refused) and the wall time. */
+ * thread i mod 4), while the calling thread waits for the requests in order;
+ * outputs go to the same item positions of out / status.  Fills
+ * latency_ms[i] (-1 when refused) and the wall time. */
 int sigops_server_run_load(sigops_server* server, const uint8_t* curves, const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks,
                            const uint64_t* offset, const uint32_t* count, const double* arrival_s, size_t nreq, uint8_t* out,
                            uint8_t* status, double* latency_ms, double* wall_s);

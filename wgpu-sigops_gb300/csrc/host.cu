@@ -37,6 +37,14 @@ int fail(int code, const char* fmt, ...) {
   return code;
 }
 
+}  // namespace
+
+namespace sg {
+int report(int code, const char* what) { return fail(code, "%s", what); }
+}  // namespace sg
+
+namespace {
+
 #define SG_CUDA(call)                                                                                 \
   do {                                                                                                \
     cudaError_t e_ = (call);                                                                          \

@@ -92,6 +92,10 @@ void fork_streams_destroy(ForkStreams* f);
 cudaError_t launch_batched(const uint8_t* curves, const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks, size_t n, uint8_t* out,
                            uint8_t* status, uint32_t* idx, void* scratch, void* defer, const GenTables& tabs, uint32_t* err, int grid,
                            int variant, int classify_grid, const ForkStreams* fork, cudaStream_t stream);
+// Record the calling thread's last-error message (sigops_last_error) and
+// return code (host.cu).
+int report(int code, const char* what);
+
 // Device and pinned host allocations of the library (host.cu).  A test hook
 // (sigops_test_fail_allocations) makes the next ones fail as if out of memory.
 cudaError_t dev_alloc(void** p, size_t bytes);

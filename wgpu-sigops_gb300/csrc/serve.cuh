@@ -8,37 +8,39 @@
 //   host (sigops_server_submit)          device (serve_kernel)
 //   ---------------------------          ---------------------
 //   copies a request's items into the    feeder warp (block 0, warp 0): polls
-//   pinned item ring grouped by curve,   the host's tile tail; copies new tiles
+//   pinned item ring grouped by curve,   the host's tile tail, copies new tiles
 //   writes its 32-item single-curve      into three device-resident rings, one
 //   tiles into the pinned tile ring,     per curve, 32 per round (one per
-//   then publishes the host tile tail    lane), and publishes their tails
-//   (release)                            (release)
-//                                        and every 100 us moves SMs to the
-//                                        curve whose backlog needs them
+//   then publishes the host tile tail    lane), publishes their tails
+//   (release)                            (release), and every 100 us moves
+//                                        TPCs to a curve whose backlog needs
+//                                        them
 //                                        consumer warps (all others): claim the
-//                                        next tile of their SM's curve, copy its
-//                                        items from the pinned
-//                                        rings into shared memory (whole lines),
-//                                        verify them, copy the results back
-//                                        (whole lines); the warp whose tile
-//                                        completes a request appends it to the
-//                                        pinned completion ring (release, system
-//                                        scope)
+//                                        next tile of their TPC's curve, read
+//                                        its items from the pinned rings in
+//                                        whole lines into shared memory,
+//                                        verify them, write the
+//                                        results back in whole lines; the warp
+//                                        whose tile completes a request
+//                                        appends it to the pinned completion
+//                                        ring (release, system scope)
 //
 // The feeder does no per-request work (the host cut the tiles), so it keeps up
 // although it shares an SM with compute-bound warps.  Host memory is only
 // touched in whole, coalesced lines: a lane reading its own 64-byte signature
 // and writing its own record would cost some 25 small transactions per item
 // across the chip-to-chip link, and those, not the arithmetic, would bound
-// the rate.  An SM works on one curve at a time: each curve's code is large,
-// and warps of one SM running two or three at once thrash its instruction
-// cache (a mixed stream of requests ran at a third of the single-curve rate
-// with no affinity, and 30-40% slower per tile when SMs took other curves'
-// tiles whenever their own ring ran dry).  An SM changes curve when its own
-// curve has nothing left for it (serve_next) or when the feeder moves it to a
-// curve whose backlog needs it (serve_balance); a moved SM finishes the tiles
-// its warps hold.  Within a curve, tiles are claimed in the order they were
-// published.
+// the rate.
+//
+// The two SMs of a TPC work on one curve at a time: each curve's code is
+// large, and SMs of one TPC running different curves thrash the instruction
+// fetch path they share (a mixed stream of requests ran at a third of the
+// single-curve rate with no affinity, and 15-25% slower per tile with the
+// curve kept per SM instead of per TPC).  A TPC changes curve when its own
+// curve has nothing left for it and its warps are all done (serve_next) or
+// when the feeder moves it to a curve whose backlog needs it (serve_balance);
+// a moved TPC finishes the tiles its warps hold.  Within a curve, tiles are
+// claimed in the order they were published.
 //
 // A slot of a device ring is reused only after the request owning its
 // previous tile has completed (the host reclaims ring space in submission
@@ -66,7 +68,8 @@ struct ServeCtl {
   uint64_t tiles_fed;  // tiles copied into the device ring (feeder)
   uint32_t stop;       // host: close the kernel
   uint32_t err;        // device error bits of the serving kernel
-  uint32_t pad[2];
+  uint32_t exited;     // the launch number of the last kernel whose warps have all left
+  uint32_t pad;
 };
 
 struct ServeTile {
@@ -77,17 +80,18 @@ struct ServeTile {
 };
 
 // device-resident queue state (kept across launches)
-constexpr int SERVE_MODE_SLOTS = 256;  // per-SM current curve, indexed by %smid modulo this
+constexpr int SERVE_MODE_SLOTS = 256;   // curve assignment slots, indexed by %smid / SERVE_SMS_PER_SLOT modulo this
+constexpr uint32_t SERVE_SMS_PER_SLOT = 2;  // the two SMs of a TPC work on one curve
 struct ServeDev {
   uint64_t fed;           // tiles of the host ring copied (feeder)
   uint64_t ring_tail[3];  // tiles published in each curve's device ring (feeder)
   uint64_t ring_head[3];  // tiles claimed from each curve's ring (consumers)
   uint64_t comp_tail;     // completion entries written
   uint32_t closing;       // the feeder publishes no more tiles in this launch
-  uint32_t pad;
-  uint32_t mode[SERVE_MODE_SLOTS];  // the curve each SM works on (set by the feeder)
-  uint32_t busy[SERVE_MODE_SLOTS];  // warps of each SM holding a tile (or claiming one)
-  uint32_t seen[SERVE_MODE_SLOTS];  // 1 for the SMs the kernel runs on
+  uint32_t live_warps;    // warps of this launch still running
+  uint32_t mode[SERVE_MODE_SLOTS];  // the curve each slot (TPC) works on
+  uint32_t busy[SERVE_MODE_SLOTS];  // warps of each slot holding a tile (or claiming one)
+  uint32_t seen[SERVE_MODE_SLOTS];  // 1 for the slots the kernel runs on
   // kernel counters: tiles and items done, warp time working on tiles and
   // looking for one (globaltimer ns, summed over warps)
   unsigned long long tiles_done, items_done, work_ns, idle_ns;
@@ -117,11 +121,12 @@ struct ServeArgs {
   BatchTables tabs;
   uint64_t idle_ns, life_ns;  // feeder: close after this long without a tile / in all
   uint32_t warps_per_sm;      // consumer warps an SM holds (a round of tiles)
+  uint32_t launch;            // this launch's number (ServeCtl::exited)
 };
 
 constexpr uint32_t SERVE_FEED_MAX_ITERS = 1u << 26;  // feeder polls per launch (bounds the loop; time limits end it first)
 constexpr uint32_t SERVE_WAIT_MAX_POLLS = 1u << 21;  // consumer polls for one tile (about 4 s with the back-off)
-constexpr uint64_t SERVE_BALANCE_NS = 100000;       // the feeder re-divides the SMs between the curves this often
+constexpr uint64_t SERVE_BALANCE_NS = 100000;       // the feeder balances the curves' TPCs this often
 
 __device__ __forceinline__ uint64_t globaltimer_ns() {
   uint64_t t;
@@ -168,60 +173,27 @@ __device__ __forceinline__ uint4 ld_sys_v4(const void* p) {
 }
 
 // A warp's staging area: 32 items x 32 words (signature 0-15, message 16-23,
-// key 24-31); a result record replaces its item's signature words.
+// key 24-31); a result record replaces its item's signature words.  Items are
+// read from and written to the pinned rings as consecutive 16-byte chunks
+// (lane + 32 j: whole 128-byte lines).  (Exchanging them by shuffles instead,
+// with no shared memory, doubled a lone request's latency: measured.)
 constexpr int SERVE_STAGE_WORDS = 32 * 32;
 
-// One item of a served request: inputs and result in the warp's staging area
+// One item of a served request
 template <int CURVE>
-__device__ __noinline__ uint32_t serve_item(uint32_t* w, const uint32_t* tab) {
-  uint32_t s[16], m[8], o[16];
-#pragma unroll
-  for (int k = 0; k < 16; ++k) s[k] = w[k];
-#pragma unroll
-  for (int k = 0; k < 8; ++k) m[k] = w[16 + k];
+__device__ __noinline__ uint32_t serve_item(const uint32_t* s, const uint32_t* m, const uint32_t* p, const uint32_t* tab, uint32_t* o) {
   uint8_t st;
   if constexpr (CURVE == 0) {
     st = ecdsa_recover<K1Traits, true>(s, m, tab, o);
   } else if constexpr (CURVE == 1) {
     st = ecdsa_recover<R1Traits>(s, m, tab, o);
   } else {
-    uint32_t p[8];
-#pragma unroll
-    for (int k = 0; k < 8; ++k) p[k] = w[24 + k];
     st = ed25519_verify(s, m, p, tab);
 #pragma unroll
     for (int k = 0; k < 16; ++k) o[k] = 0;
     o[0] = st == ST_OK;
   }
-#pragma unroll
-  for (int k = 0; k < 16; ++k) w[k] = o[k];
   return st;
-}
-
-// Inputs of items [first, first + n) of one curve into the staging area:
-// each 16-byte chunk of the rings is read once, 32 consecutive chunks per
-// instruction (whole 128-byte lines)
-__device__ __forceinline__ void serve_stage_in(const ServeArgs& a, uint32_t first, uint32_t n, bool keys, uint32_t* stage, unsigned lane) {
-  uint4* st4 = reinterpret_cast<uint4*>(stage);
-  const uint8_t* sig = a.sig + (size_t)first * 64;
-  const uint8_t* msg = a.msg + (size_t)first * 32;
-  const uint8_t* pk = a.pk + (size_t)first * 32;
-#pragma unroll 1
-  for (uint32_t c = lane; c < 4 * n; c += 32) st4[(c >> 2) * 8 + (c & 3)] = ld_sys_v4(sig + 16 * c);
-#pragma unroll 1
-  for (uint32_t c = lane; c < 2 * n; c += 32) st4[(c >> 1) * 8 + 4 + (c & 1)] = ld_sys_v4(msg + 16 * c);
-  if (keys) {
-#pragma unroll 1
-    for (uint32_t c = lane; c < 2 * n; c += 32) st4[(c >> 1) * 8 + 6 + (c & 1)] = ld_sys_v4(pk + 16 * c);
-  }
-}
-
-// Result records of the staged items into the pinned output ring, whole lines
-__device__ __forceinline__ void serve_stage_out(const ServeArgs& a, uint32_t first, uint32_t n, const uint32_t* stage, unsigned lane) {
-  const uint4* st4 = reinterpret_cast<const uint4*>(stage);
-  uint4* out = reinterpret_cast<uint4*>(a.out + (size_t)first * 64);
-#pragma unroll 1
-  for (uint32_t c = lane; c < 4 * n; c += 32) out[c] = st4[(c >> 2) * 8 + (c & 3)];
 }
 
 __device__ __forceinline__ uint32_t smid() {
@@ -236,16 +208,16 @@ __device__ __forceinline__ uint32_t warp_sum(uint32_t v) {
   return v;
 }
 
-// The feeder warp's SM assignment, every SERVE_BALANCE_NS.  A curve's
-// pressure is its tiles waiting x the time a tile of it takes, per SM
+// The feeder warp's TPC assignment, every SERVE_BALANCE_NS.  A curve's
+// pressure is its tiles waiting x the time a tile of it takes, per TPC
 // working on it.  When the highest pressure exceeds twice the lowest plus one
-// round of tiles (a tile per warp of an SM), an eighth of the low-pressure
-// curve's SMs (at least one, idle ones first) move to the high-pressure
-// curve; every curve keeps at least one SM.  Together with the per-SM rule in
-// serve_next (an SM whose ring is empty and whose warps are all done moves to
-// the curve with the most tiles waiting) the SMs follow the mix within a
-// millisecond, while an SM changes curve only when the backlog asks for it:
-// every move runs two curves on one SM for up to a tile's time.
+// round of tiles (a tile per warp of a TPC), an eighth of the low-pressure
+// curve's TPCs (at least one, idle ones first) move to the high-pressure
+// curve; every curve keeps at least one TPC.  Together with the rule in
+// serve_next (a TPC whose ring is empty and whose warps are all done moves to
+// the curve with the most tiles waiting) the TPCs follow the mix within a
+// millisecond, while a TPC changes curve only when the backlog asks for it:
+// every move runs two curves on one TPC for up to a tile's time.
 __device__ __forceinline__ void serve_balance(const ServeArgs& a, unsigned lane, const uint64_t tail[3]) {
   constexpr uint64_t kCost[3] = {100, 140, 90};  // relative time of a tile: secp256k1 (GLV), P-256, ed25519
   constexpr int PER = SERVE_MODE_SLOTS / 32;
@@ -282,7 +254,7 @@ __device__ __forceinline__ void serve_balance(const ServeArgs& a, unsigned lane,
     if (k != hi && n[k] > 1 && (lo < 0 || p[k] < p[lo])) lo = k;
   }
   if (lo < 0) return;
-  const uint64_t round = kCost[hi] * 64 * a.warps_per_sm;
+  const uint64_t round = kCost[hi] * 64 * a.warps_per_sm * SERVE_SMS_PER_SLOT;
   if (n[hi] > 0 && p[hi] <= 2 * p[lo] + round) return;
   const uint32_t m = min(max(n[lo] / 8, 1u), n[lo] - 1);
   // the first m slots of curve lo in slot order, idle ones first
@@ -316,13 +288,15 @@ __device__ __forceinline__ void serve_feeder(const ServeArgs& a) {
   uint32_t backoff = 64;
 #pragma unroll 1
   for (uint32_t it = 0; it < SERVE_FEED_MAX_ITERS; ++it) {
-    const uint64_t now = globaltimer_ns();
-    if (ld_acquire_sys_u32(&a.ctl->stop) || now - last > a.idle_ns || now - t0 > a.life_ns) break;
+    // the warp decides together: lane 0's clock and reads
+    const uint64_t now = __shfl_sync(0xffffffffu, globaltimer_ns(), 0);
+    const uint32_t stop = __shfl_sync(0xffffffffu, ld_acquire_sys_u32(&a.ctl->stop), 0);
+    if (stop || now - last > a.idle_ns || now - t0 > a.life_ns) break;
     if (now - balanced > SERVE_BALANCE_NS) {
       serve_balance(a, lane, tail);
       balanced = now;
     }
-    const uint64_t avail = ld_acquire_sys_u64(&a.ctl->tile_tail);
+    const uint64_t avail = __shfl_sync(0xffffffffu, ld_acquire_sys_u64(&a.ctl->tile_tail), 0);
     if (fed >= avail) {
       __nanosleep(backoff);
       backoff = backoff < 1024 ? 2 * backoff : 1024;
@@ -387,8 +361,8 @@ __device__ __forceinline__ uint64_t ring_waiting(const ServeArgs& a, uint32_t k)
   return tail > head ? tail - head : 0;
 }
 
-// lane 0: a tile of this SM's curve (1), closed and empty (2), or the poll
-// budget spent (0).  An SM whose curve has no tile waiting and whose warps
+// lane 0: a tile of this TPC's curve (1), closed and empty (2), or the poll
+// budget spent (0).  A TPC whose curve has no tile waiting and whose warps
 // all finished theirs moves to the curve with the most tiles waiting.  After
 // the close any ring's tile is taken: every published tile is processed
 // before the kernel exits.
@@ -399,7 +373,7 @@ __device__ __forceinline__ uint32_t serve_next(const ServeArgs& a, uint32_t sm, 
   for (uint32_t p = 0; p < SERVE_WAIT_MAX_POLLS; ++p) {
     const uint32_t cur = min(*(volatile uint32_t*)&a.dev->mode[sm], 2u);
     if (ring_waiting(a, cur)) {
-      atomicAdd(busy, 1u);  // counted from the claim on: the feeder sees the SM's running tiles
+      atomicAdd(busy, 1u);  // counted from the claim on: the feeder sees the TPC's running tiles
       if (serve_claim(a, cur, pos)) {
         curve = cur;
         return 1;
@@ -408,7 +382,7 @@ __device__ __forceinline__ uint32_t serve_next(const ServeArgs& a, uint32_t sm, 
       continue;
     }
     if (*(volatile uint32_t*)busy == 0) {
-      // the SM has no tile of its curve left: it moves to the curve with the most tiles waiting
+      // the TPC has no tile of its curve left: it moves to the curve with the most tiles waiting
       uint32_t best = cur;
       uint64_t most = 0;
 #pragma unroll 1
@@ -447,7 +421,7 @@ __device__ __forceinline__ uint32_t serve_next(const ServeArgs& a, uint32_t sm, 
 // consumer warps: one tile at a time until the feeder closes and the rings are empty
 __device__ __forceinline__ void serve_consumer(const ServeArgs& a, uint32_t* stage) {
   const unsigned lane = threadIdx.x & 31u;
-  const uint32_t sm = smid() % SERVE_MODE_SLOTS;
+  const uint32_t sm = (smid() / SERVE_SMS_PER_SLOT) % SERVE_MODE_SLOTS;
   if (lane == 0) *(volatile uint32_t*)&a.dev->seen[sm] = 1u;
 #pragma unroll 1
   for (;;) {
@@ -466,17 +440,38 @@ __device__ __forceinline__ void serve_consumer(const ServeArgs& a, uint32_t* sta
     pos = __shfl_sync(0xffffffffu, pos, 0);
     const ServeTile tl = a.tiles[(size_t)curve * a.tile_cap + (uint32_t)(pos % a.tile_cap)];
     const uint32_t req = tl.shape & 0xffffu, n = min((tl.shape >> 16) & 0xffu, 32u);
-    serve_stage_in(a, tl.first, n, curve == 2, stage, lane);
+    {  // inputs into the staging area
+      uint4* st4 = reinterpret_cast<uint4*>(stage);
+      const uint8_t* sig = a.sig + (size_t)tl.first * 64;
+      const uint8_t* msg = a.msg + (size_t)tl.first * 32;
+      const uint8_t* pk = a.pk + (size_t)tl.first * 32;
+#pragma unroll 1
+      for (uint32_t c = lane; c < 4 * n; c += 32) st4[(c >> 2) * 8 + (c & 3)] = ld_sys_v4(sig + 16 * c);
+#pragma unroll 1
+      for (uint32_t c = lane; c < 2 * n; c += 32) st4[(c >> 1) * 8 + 4 + (c & 1)] = ld_sys_v4(msg + 16 * c);
+      if (curve == 2) {
+#pragma unroll 1
+        for (uint32_t c = lane; c < 2 * n; c += 32) st4[(c >> 1) * 8 + 6 + (c & 1)] = ld_sys_v4(pk + 16 * c);
+      }
+    }
     __syncwarp();
     uint32_t st = 0;
     if (lane < n) {
       uint32_t* w = stage + lane * 32;
-      if (curve == 0) st = serve_item<0>(w, a.tabs.k1);
-      else if (curve == 1) st = serve_item<1>(w, a.tabs.r1);
-      else st = serve_item<2>(w, a.tabs.ed);
+      uint32_t o[16];
+      if (curve == 0) st = serve_item<0>(w, w + 16, w + 24, a.tabs.k1, o);
+      else if (curve == 1) st = serve_item<1>(w, w + 16, w + 24, a.tabs.r1, o);
+      else st = serve_item<2>(w, w + 16, w + 24, a.tabs.ed, o);
+#pragma unroll
+      for (int k = 0; k < 16; ++k) w[k] = o[k];
     }
     __syncwarp();
-    serve_stage_out(a, tl.first, n, stage, lane);
+    {  // result records into the pinned output ring
+      const uint4* st4 = reinterpret_cast<const uint4*>(stage);
+      uint4* out = reinterpret_cast<uint4*>(a.out + (size_t)tl.first * 64);
+#pragma unroll 1
+      for (uint32_t c = lane; c < 4 * n; c += 32) out[c] = st4[(c >> 2) * 8 + (c & 3)];
+    }
     if (lane < n) a.st[tl.first + lane] = (uint8_t)st;
     __threadfence_system();  // this lane's stores before the request's completion entry
     __syncwarp();
@@ -496,15 +491,23 @@ __device__ __forceinline__ void serve_consumer(const ServeArgs& a, uint32_t* sta
 
 template <int BLOCK, int MINB>
 __global__ void __launch_bounds__(BLOCK, MINB) serve_kernel(ServeArgs a) {
-  __shared__ __align__(16) uint32_t stage[BLOCK / 32][SERVE_STAGE_WORDS];
-  const unsigned warp = threadIdx.x >> 5;
-  if (blockIdx.x == 0 && warp == 0) serve_feeder(a);
-  else serve_consumer(a, stage[warp]);
+  __shared__ __align__(16) uint32_t stage_all[BLOCK / 32][SERVE_STAGE_WORDS];
+  if (blockIdx.x == 0 && threadIdx.x < 32) serve_feeder(a);
+  else serve_consumer(a, stage_all[threadIdx.x >> 5]);
+  // the last warp out tells the host, which then needs no driver call to see the exit
+  if ((threadIdx.x & 31u) == 0) {
+    __threadfence_system();
+    if (atomicSub(&a.dev->live_warps, 1u) == 1u) {
+      __threadfence_system();
+      st_release_sys_u32(&a.ctl->exited, a.launch);
+    }
+  }
 }
 
-// before each launch: the queue is open; SMs start spread over the curves
-__global__ void serve_reset_kernel(ServeDev* d) {
+// before each launch: the queue is open; TPCs start spread over the curves
+__global__ void serve_reset_kernel(ServeDev* d, uint32_t warps) {
   d->closing = 0;
+  d->live_warps = warps;
   for (int i = threadIdx.x; i < SERVE_MODE_SLOTS; i += blockDim.x) {
     d->mode[i] = i % 3;
     d->busy[i] = 0;

@@ -101,6 +101,8 @@ struct sigops_server {
   cudaStream_t stat_stream = nullptr;  // reads of the kernel counters while it runs
   cudaEvent_t ev_exit = nullptr;
   bool running = false;
+  uint32_t launch_no = 0;    // number of the running (or last) launch
+  double exit_checked = 0;   // last driver-side look at the kernel (a fault would leave ServeCtl::exited unset)
   std::atomic<int> shape{0};
   // host state, under mu
   std::mutex mu;
@@ -115,16 +117,19 @@ struct sigops_server {
   uint64_t item_head = 0, item_tail = 0;  // ring positions in use: [item_head, item_tail)
   uint64_t tile_head = 0, tile_alloc = 0, tiles_published = 0;
   size_t queued_items = 0;
-  bool hbm_ok = true;
+  std::atomic<bool> hbm_ok{true};  // free device memory above the floor (monitor thread)
   size_t hbm_floor = 0;
-  double hbm_checked = 0;
   std::thread worker;
+  std::thread monitor;  // re-reads free device memory every 100 ms (a driver call that can take milliseconds)
   bool stop = false;
   bool alive = true;    // the dispatcher runs
   bool broken = false;  // the kernel reported an expired wait, or could not launch: requests were failed
   int fault = 0;        // test hook: 1 = the dispatcher stops
   // stats
   uint64_t launches = 0, items_done = 0, requests_done = 0;
+  uint64_t iterations = 0;
+  double max_gap = 0;     // longest time between two dispatcher iterations since the last read (s)
+  double max_driver = 0;  // longest driver call of the dispatcher since the last read (s)
 };
 
 namespace {
@@ -164,7 +169,8 @@ cudaError_t launch_kernel(sigops_server* s) {
   a.idle_ns = 20ull * 1000 * 1000;    // close after 20 ms without a tile
   a.life_ns = 2000ull * 1000 * 1000;  // and after 2 s in all (the dispatcher relaunches)
   a.warps_per_sm = (uint32_t)(grid / s->cv.num_sms) * (uint32_t)(block / 32);
-  sg::serve_reset_kernel<<<1, 1, 0, s->stream>>>(s->dev);
+  a.launch = ++s->launch_no;
+  sg::serve_reset_kernel<<<1, 1, 0, s->stream>>>(s->dev, (uint32_t)grid * (uint32_t)(block / 32));
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   void* args[] = {&a};
@@ -202,53 +208,88 @@ void reclaim(sigops_server* s) {
   }
 }
 
+// Completions: the kernel appends each finished request to the completion
+// ring once its results are in the output ring.  The ring is read under the
+// lock and the results are copied to the callers' buffers outside it.  The
+// dispatcher calls this, and so does every thread waiting in
+// sigops_server_wait: a dispatcher the OS leaves unscheduled for a few
+// milliseconds then delays nothing.  Each caller copies its own disjoint set.
+// Returns whether any request finished.
+bool collect_completions(sigops_server* s, std::unique_lock<std::mutex>& lk, std::vector<ReqPtr>& finished) {
+  finished.clear();
+  bool changed = false;
+  for (;;) {
+    const uint64_t e = __atomic_load_n(&s->comp[s->comp_head % s->R], __ATOMIC_ACQUIRE);
+    if ((uint32_t)e != (uint32_t)(s->comp_head + 1)) break;  // not written yet
+    s->comp_head++;
+    ReqPtr& r = s->by_slot[(e >> 32) & 0xffffu];
+    if (!r || (r->seq & 0xffffu) != (uint32_t)(e >> 48)) continue;  // a request already failed on the host
+    if (r->state == RState::Canceled) {
+      r->state = RState::Done;  // results discarded
+      changed = true;
+    } else if (r->state == RState::Running) {
+      r->state = RState::Finishing;
+      finished.push_back(r);
+    }
+  }
+  if (!finished.empty()) {
+    lk.unlock();
+    for (ReqPtr& r : finished) {
+      if (r->perm.empty()) {
+        memcpy(r->out, s->out + r->off * 64, r->n * 64);
+        if (r->status) memcpy(r->status, s->st + r->off, r->n);
+      } else {
+        for (size_t p = 0; p < r->n; ++p) {
+          memcpy(r->out + (size_t)r->perm[p] * 64, s->out + (r->off + p) * 64, 64);
+          if (r->status) r->status[r->perm[p]] = s->st[r->off + p];
+        }
+      }
+      r->t_done = now_s();
+    }
+    lk.lock();
+    for (ReqPtr& r : finished) {
+      r->state = RState::Done;
+      s->requests_done++;
+      s->items_done += r->n;
+    }
+    changed = true;
+  }
+  if (changed) {
+    reclaim(s);
+    s->cond.notify_all();
+  }
+  return changed;
+}
+
 void worker_loop(sigops_server* s) {
   cudaSetDevice(s->cv.device);
   std::unique_lock<std::mutex> lk(s->mu);
   std::vector<ReqPtr> finished;
+  double t_iter = now_s();
+  bool busy = false;  // requests were in flight at the end of the previous iteration
   while (!s->stop) {
     if (s->fault == 1) break;  // test hook: the dispatcher stops as if it had died
-    // completions: the kernel appends each finished request to the completion
-    // ring once its results are in the output ring
-    finished.clear();
-    for (;;) {
-      const uint64_t e = __atomic_load_n(&s->comp[s->comp_head % s->R], __ATOMIC_ACQUIRE);
-      if ((uint32_t)e != (uint32_t)(s->comp_head + 1)) break;  // not written yet
-      s->comp_head++;
-      ReqPtr& r = s->by_slot[(e >> 32) & 0xffffu];
-      if (!r || (r->seq & 0xffffu) != (uint32_t)(e >> 48)) continue;  // a request already failed on the host
-      if (r->state == RState::Canceled) {
-        r->state = RState::Done;  // results discarded
-      } else if (r->state == RState::Running) {
-        r->state = RState::Finishing;
-        finished.push_back(r);
-      }
-    }
-    if (!finished.empty()) {
-      lk.unlock();
+    {
       const double t = now_s();
-      for (ReqPtr& r : finished) {
-        if (r->perm.empty()) {
-          memcpy(r->out, s->out + r->off * 64, r->n * 64);
-          if (r->status) memcpy(r->status, s->st + r->off, r->n);
-        } else {
-          for (size_t p = 0; p < r->n; ++p) {
-            memcpy(r->out + (size_t)r->perm[p] * 64, s->out + (r->off + p) * 64, 64);
-            if (r->status) r->status[r->perm[p]] = s->st[r->off + p];
-          }
-        }
-        r->t_done = t;
-      }
-      lk.lock();
-      for (ReqPtr& r : finished) {
-        r->state = RState::Done;
-        s->requests_done++;
-        s->items_done += r->n;
+      if (busy) s->max_gap = std::max(s->max_gap, t - t_iter);
+      t_iter = t;
+      s->iterations++;
+    }
+    bool changed = collect_completions(s, lk, finished);
+    // the persistent kernel: notice its exit (its last warp writes ServeCtl::exited;
+    // the driver is asked only every 50 ms: its calls from other threads can hold
+    // this one for milliseconds), relaunch it when work waits
+    bool exited = false;
+    if (s->running) {
+      exited = __atomic_load_n(&s->ctl->exited, __ATOMIC_ACQUIRE) == s->launch_no;
+      const double t = now_s();
+      if (!exited && t - s->exit_checked > 0.05) {
+        s->exit_checked = t;
+        exited = cudaEventQuery(s->ev_exit) != cudaErrorNotReady;
+        s->max_driver = std::max(s->max_driver, now_s() - t);
       }
     }
-    bool changed = !finished.empty();
-    // the persistent kernel: notice its exit, relaunch it when work waits
-    if (s->running && cudaEventQuery(s->ev_exit) != cudaErrorNotReady) {
+    if (exited) {
       s->running = false;
       const uint32_t err = __atomic_exchange_n(&s->ctl->err, 0u, __ATOMIC_ACQ_REL);
       if (err) {
@@ -259,7 +300,10 @@ void worker_loop(sigops_server* s) {
       }
     }
     if (!s->running && !s->broken && __atomic_load_n(&s->ctl->tiles_fed, __ATOMIC_ACQUIRE) < s->tiles_published) {
-      if (launch_kernel(s) == cudaSuccess) {
+      const double t = now_s();
+      const cudaError_t e = launch_kernel(s);
+      s->max_driver = std::max(s->max_driver, now_s() - t);
+      if (e == cudaSuccess) {
         s->running = true;
         s->launches++;
       } else {
@@ -270,19 +314,27 @@ void worker_loop(sigops_server* s) {
     }
     reclaim(s);
     if (changed) s->cond.notify_all();
-    // admission by device memory: free memory re-read every 100 ms
-    const double t = now_s();
-    if (t - s->hbm_checked > 0.1) {
-      size_t free_b = 0, total_b = 0;
-      if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess) s->hbm_ok = free_b >= s->hbm_floor;
-      s->hbm_checked = t;
-    }
     // poll completions every 20 us while requests are in flight
-    if (!s->inflight.empty()) s->cond.wait_for(lk, std::chrono::microseconds(20));
+    busy = !s->inflight.empty();
+    if (busy) s->cond.wait_for(lk, std::chrono::microseconds(20));
     else s->cond.wait_for(lk, std::chrono::milliseconds(5));
   }
   s->alive = false;
   s->cond.notify_all();
+}
+
+// admission by device memory: free memory re-read every 100 ms, on a thread
+// of its own (the dispatcher makes no driver call while requests flow)
+void monitor_loop(sigops_server* s) {
+  cudaSetDevice(s->cv.device);
+  std::unique_lock<std::mutex> lk(s->mu);
+  while (!s->stop) {
+    lk.unlock();
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess) s->hbm_ok.store(free_b >= s->hbm_floor);
+    lk.lock();
+    s->cond.wait_for(lk, std::chrono::milliseconds(100), [s] { return s->stop; });
+  }
 }
 
 template <class T>
@@ -371,6 +423,7 @@ sigops_server* sigops_server_create(sigops_ctx* ctx, int nslots, size_t slot_ite
   s->handles.reserve(1u << 14);  // in-flight handles of a typical client without a rehash
   sigops_server* p = s.release();
   p->worker = std::thread(worker_loop, p);
+  p->monitor = std::thread(monitor_loop, p);
   return p;
 }
 
@@ -382,6 +435,7 @@ void sigops_server_destroy(sigops_server* s) {
   }
   s->cond.notify_all();
   if (s->worker.joinable()) s->worker.join();
+  if (s->monitor.joinable()) s->monitor.join();
   cudaSetDevice(s->cv.device);
   if (s->ctl) __atomic_store_n(&s->ctl->stop, 1u, __ATOMIC_RELEASE);  // the kernel closes within microseconds
   if (s->stream) cudaStreamSynchronize(s->stream);
@@ -400,7 +454,7 @@ int sigops_server_submit(sigops_server* s, const uint8_t* curves, int uniform_cu
   if (!s || !sigs || !msgs || !out || !handle || n == 0) return SIGOPS_E_INVAL;
   if (!curves && (uniform_curve < 0 || uniform_curve > 2)) return SIGOPS_E_INVAL;
   if (!curves && uniform_curve == SIGOPS_ED25519 && !pks) return SIGOPS_E_INVAL;
-  if (n > s->max_items) return SIGOPS_E_RANGE;
+  if (n > s->max_items) return sg::report(SIGOPS_E_RANGE, "server: request larger than slot_items");
   // items per curve; a request already in curve order is copied as it is
   size_t cnt[3] = {0, 0, 0};
   bool grouped = true;
@@ -416,16 +470,16 @@ int sigops_server_submit(sigops_server* s, const uint8_t* curves, int uniform_cu
   ReqPtr r = std::make_shared<Request>();
   {
     std::lock_guard<std::mutex> g(s->mu);
-    if (!s->alive || s->broken) return SIGOPS_E_CUDA;
-    if (!s->hbm_ok) return SIGOPS_E_BUSY;
+    if (!s->alive || s->broken) return sg::report(SIGOPS_E_CUDA, "server: the dispatcher or the kernel has failed");
+    if (!s->hbm_ok.load()) return sg::report(SIGOPS_E_BUSY, "server: free device memory below the floor");
     const uint32_t slot = (uint32_t)(s->slots_taken % s->R);
-    if (s->by_slot[slot]) return SIGOPS_E_BUSY;  // request slots full
+    if (s->by_slot[slot]) return sg::report(SIGOPS_E_BUSY, "server: all request slots in flight");
     // a contiguous run of n items in the rings, wrapping to the start when the end is short
     const uint64_t pos = s->item_tail % s->C;
     const uint64_t skip = pos + n > s->C ? s->C - pos : 0;
-    if (s->item_tail - s->item_head + skip + n > s->C) return SIGOPS_E_BUSY;  // item rings full
+    if (s->item_tail - s->item_head + skip + n > s->C) return sg::report(SIGOPS_E_BUSY, "server: item rings full");
     const uint64_t ntiles = (cnt[0] + 31) / 32 + (cnt[1] + 31) / 32 + (cnt[2] + 31) / 32;
-    if (s->tile_alloc - s->tile_head + ntiles > s->tile_cap) return SIGOPS_E_BUSY;  // tile rings full
+    if (s->tile_alloc - s->tile_head + ntiles > s->tile_cap) return sg::report(SIGOPS_E_BUSY, "server: tile rings full");
     r->tile_first = s->tile_alloc;
     s->tile_alloc += ntiles;
     r->tile_end = s->tile_alloc;
@@ -506,8 +560,15 @@ int sigops_server_wait(sigops_server* s, uint64_t handle, int timeout_ms, double
   if (it == s->handles.end()) return SIGOPS_E_INVAL;
   ReqPtr r = it->second;
   auto pred = [&] { return r->state == RState::Done || r->canceled || !s->alive; };
-  if (timeout_ms < 0) s->cond.wait(lk, pred);
-  else if (!s->cond.wait_for(lk, std::chrono::milliseconds(timeout_ms), pred)) return SIGOPS_E_TIMEDOUT;
+  // the waiting thread also collects completions (collect_completions)
+  std::vector<ReqPtr> finished;
+  const auto deadline = Clock::now() + std::chrono::milliseconds(timeout_ms < 0 ? 0 : timeout_ms);
+  while (!pred()) {
+    collect_completions(s, lk, finished);
+    if (pred()) break;
+    if (timeout_ms >= 0 && Clock::now() >= deadline) return SIGOPS_E_TIMEDOUT;
+    s->cond.wait_for(lk, std::chrono::microseconds(50));
+  }
   if (r->canceled) return SIGOPS_E_CANCELED;
   if (r->state != RState::Done) return SIGOPS_E_TIMEDOUT;  // the dispatcher stopped: the request cannot finish
   if (latency_ms) *latency_ms = (r->t_done - r->t_submit) * 1e3;
@@ -556,6 +617,17 @@ int sigops_server_kernel_stats(sigops_server* s, uint64_t* tiles, uint64_t* item
   return SIGOPS_OK;
 }
 
+int sigops_server_dispatch_stats(sigops_server* s, uint64_t* iterations, double* max_gap_ms, double* max_driver_ms) {
+  if (!s) return SIGOPS_E_INVAL;
+  std::lock_guard<std::mutex> g(s->mu);
+  if (iterations) *iterations = s->iterations;
+  if (max_gap_ms) *max_gap_ms = s->max_gap * 1e3;
+  if (max_driver_ms) *max_driver_ms = s->max_driver * 1e3;
+  s->max_gap = 0;
+  s->max_driver = 0;
+  return SIGOPS_OK;
+}
+
 int sigops_server_test_fault(sigops_server* s, int fault) {
   if (!s || fault < 0 || fault > 1) return SIGOPS_E_INVAL;
   {
@@ -569,16 +641,20 @@ int sigops_server_test_fault(sigops_server* s, int fault) {
 // Open-loop load: request i covers items [offset[i], offset[i] + count[i]) of
 // the pool and is submitted at arrival_s[i] seconds after the start (arrivals
 // in non-decreasing order) by client thread i mod kLoadClients, as concurrent
-// clients of a server would; outputs land at the same item positions.  Fills
-// latency_ms[i] (submit -> results in host memory) and the wall time from the
-// start to the last completion.  Returns SIGOPS_E_BUSY if admission refused a
-// request (its latency is set to -1).
+// clients of a server would; the calling thread waits for the requests in
+// order, each as soon as it is submitted (and so collects completions while
+// the run goes on, as the request threads of a server do).  Outputs land at
+// the same item positions.  Fills latency_ms[i] (submit -> results in host
+// memory) and the wall time from the start to the last completion.  Returns
+// SIGOPS_E_BUSY if admission refused a request (its latency is set to -1).
 int sigops_server_run_load(sigops_server* s, const uint8_t* curves, const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks,
                            const uint64_t* offset, const uint32_t* count, const double* arrival_s, size_t nreq, uint8_t* out,
                            uint8_t* status, double* latency_ms, double* wall_s) {
   if (!s || !curves || !sigs || !msgs || !pks || !offset || !count || !arrival_s || !out || !latency_ms) return SIGOPS_E_INVAL;
   constexpr size_t kLoadClients = 4;
   std::vector<uint64_t> handles(nreq, 0);
+  std::unique_ptr<std::atomic<int>[]> state(new std::atomic<int>[nreq]);  // 0 pending, 1 submitted, 2 refused
+  for (size_t i = 0; i < nreq; ++i) state[i].store(0);
   {
     // every request of the run is registered before the first wait: size the
     // handle table once, so that no rehash stalls the dispatcher
@@ -586,42 +662,39 @@ int sigops_server_run_load(sigops_server* s, const uint8_t* curves, const uint8_
     s->handles.reserve(s->handles.size() + nreq);
   }
   std::atomic<int> rc{SIGOPS_OK};
+  auto record = [&](int r) {
+    int ok = SIGOPS_OK;
+    rc.compare_exchange_strong(ok, r);
+  };
   const double t0 = now_s();
   auto client = [&](size_t first) {
     for (size_t i = first; i < nreq; i += kLoadClients) {
       const double target = t0 + arrival_s[i];
-      for (;;) {
-        const double t = now_s();
-        if (t >= target) break;
-        if (target - t > 200e-6) std::this_thread::sleep_for(std::chrono::microseconds((int)((target - t - 100e-6) * 1e6)));
-      }
+      // sleep to the arrival (a client that spins would take a core the dispatcher may need)
+      for (double t = now_s(); t < target; t = now_s())
+        std::this_thread::sleep_for(std::chrono::microseconds(std::max(1, (int)((target - t) * 1e6))));
       const size_t o = offset[i];
       const int r = sigops_server_submit(s, curves + o, -1, sigs + o * 64, msgs + o * 32, pks + o * 32, count[i], out + o * 64,
                                          status ? status + o : nullptr, &handles[i]);
-      if (r != SIGOPS_OK) {
-        handles[i] = 0;
-        int ok = SIGOPS_OK;
-        rc.compare_exchange_strong(ok, r);
-      }
+      if (r != SIGOPS_OK) record(r);
+      state[i].store(r == SIGOPS_OK ? 1 : 2, std::memory_order_release);
     }
   };
   std::vector<std::thread> clients;
-  for (size_t j = 1; j < std::min(kLoadClients, nreq); ++j) clients.emplace_back(client, j);
-  client(0);
-  for (std::thread& c : clients) c.join();
+  for (size_t j = 0; j < std::min(kLoadClients, nreq); ++j) clients.emplace_back(client, j);
   for (size_t i = 0; i < nreq; ++i) {
-    if (!handles[i]) {
+    int st;
+    while ((st = state[i].load(std::memory_order_acquire)) == 0) std::this_thread::sleep_for(std::chrono::microseconds(20));
+    if (st == 2) {
       latency_ms[i] = -1;
       continue;
     }
     double lat = 0;
     const int r = sigops_server_wait(s, handles[i], -1, &lat);
     latency_ms[i] = lat;
-    if (r != SIGOPS_OK) {
-      int ok = SIGOPS_OK;
-      rc.compare_exchange_strong(ok, r);
-    }
+    if (r != SIGOPS_OK) record(r);
   }
+  for (std::thread& c : clients) c.join();
   if (wall_s) *wall_s = now_s() - t0;
   return rc.load();
 }

@@ -103,6 +103,8 @@ extern "C" {
                                 pks: *const u8, n: usize, out: *mut u8, status: *mut u8, handle: *mut u64) -> c_int;
     pub fn sigops_server_wait(server: *mut SigopsServer, handle: u64, timeout_ms: c_int, latency_ms: *mut f64) -> c_int;
     pub fn sigops_server_cancel(server: *mut SigopsServer, handle: u64) -> c_int;
+    pub fn sigops_server_dispatch_stats(server: *mut SigopsServer, iterations: *mut u64, max_gap_ms: *mut f64,
+        max_driver_ms: *mut f64) -> c_int;
     pub fn sigops_server_kernel_stats(server: *mut SigopsServer, tiles: *mut u64, items: *mut u64, work_s: *mut f64,
         idle_s: *mut f64, sm_moves: *mut u64) -> c_int;
     pub fn sigops_server_test_fault(server: *mut SigopsServer, fault: c_int) -> c_int;

@@ -72,6 +72,7 @@ SIGNATURES = {
     "sigops_server_submit": (ctypes.c_int, [_vp, _vp, ctypes.c_int, _vp, _vp, _vp, _sz, _vp, _vp, ctypes.POINTER(ctypes.c_uint64)]),
     "sigops_server_wait": (ctypes.c_int, [_vp, ctypes.c_uint64, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
     "sigops_server_cancel": (ctypes.c_int, [_vp, ctypes.c_uint64]),
+    "sigops_server_dispatch_stats": (ctypes.c_int, [_vp, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "sigops_server_kernel_stats": (ctypes.c_int, [_vp, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "sigops_server_test_fault": (ctypes.c_int, [_vp, ctypes.c_int]),
     "sigops_test_fail_allocations": (ctypes.c_int, [ctypes.c_int]),

@@ -96,6 +96,15 @@ class Server:
         return {"tiles": t.value, "items": i.value, "work_s": w.value, "idle_s": d.value, "sm_moves": mv.value,
                 "busy_fraction": w.value / tot if tot > 0 else 0.0}
 
+    def dispatch_stats(self) -> dict:
+        """Dispatcher iterations, the longest gap between two of them with
+        requests in flight and its longest driver call, since the previous
+        call (ms)."""
+        it, gap, drv = ctypes.c_uint64(), ctypes.c_double(), ctypes.c_double()
+        check(lib.sigops_server_dispatch_stats(self.ptr, ctypes.byref(it), ctypes.byref(gap), ctypes.byref(drv)),
+              "sigops_server_dispatch_stats")
+        return {"iterations": it.value, "max_gap_ms": gap.value, "max_driver_ms": drv.value}
+
     def test_fault(self, fault: int):
         """Failure injection on the host (1: the dispatcher thread stops)."""
         check(lib.sigops_server_test_fault(self.ptr, fault), "sigops_server_test_fault")
@@ -179,11 +188,12 @@ def measure(ctx, W, loads=(0.25, 0.5, 0.75, 0.9), seconds: float = 10.0, seed: i
             slot_items: int = 0, sat_items: int = 2_000_000, variant: int | None = None, warmup_seconds: float = 1.0) -> dict:
     """Saturation, a discarded warm-up run at half load, then open-loop Poisson
     load levels; latency percentiles in ms.  slots = 0 sizes the request rings
-    to hold the whole saturation backlog (plus 10%)."""
+    to hold the whole saturation backlog (plus 10%), and at least 1M items
+    (about 50 ms of work at saturation, 200 MB of pinned memory)."""
     pool, regions = curve_sorted_pool(W)
     per = slot_items or 16384
     if slots <= 0:
-        slots = max(8, int(np.ceil(1.1 * sat_items / per)))
+        slots = max(int(np.ceil(1_048_576 / per)), int(np.ceil(1.1 * sat_items / per)))
     srv = Server(ctx, slots=slots, slot_items=slot_items, variant=variant)
     try:
         mean_size = float(np.mean(np.clip(np.floor(np.exp(np.random.default_rng(1).uniform(0, np.log(2048), 200000))), 1, 2048)))
@@ -203,8 +213,10 @@ def measure(ctx, W, loads=(0.25, 0.5, 0.75, 0.9), seconds: float = 10.0, seed: i
             rate = load * sat / mean_size
             offs, cnts, arr = request_stream(regions, rate, seconds, seed + 1 + k)
             k0 = srv.kernel_stats()
+            srv.dispatch_stats()
             rc, lat, wall, out, st = srv.run_load(pool, offs, cnts, arr)
             k1 = srv.kernel_stats()
+            dsp = srv.dispatch_stats()
             ok = lat >= 0
             work, idle, tiles = k1["work_s"] - k0["work_s"], k1["idle_s"] - k0["idle_s"], k1["tiles"] - k0["tiles"]
             res["levels"].append({
@@ -213,7 +225,9 @@ def measure(ctx, W, loads=(0.25, 0.5, 0.75, 0.9), seconds: float = 10.0, seed: i
                 "p50_ms": float(np.percentile(lat[ok], 50)), "p99_ms": float(np.percentile(lat[ok], 99)),
                 "p999_ms": float(np.percentile(lat[ok], 99.9)), "rc": int(rc),
                 "kernel_busy": work / (work + idle) if work + idle > 0 else 0.0,
-                "warp_ms_per_tile": 1e3 * work / tiles if tiles else 0.0, "sm_moves": k1["sm_moves"] - k0["sm_moves"]})
+                "warp_ms_per_tile": 1e3 * work / tiles if tiles else 0.0, "sm_moves": k1["sm_moves"] - k0["sm_moves"],
+                "dispatch_max_gap_ms": dsp["max_gap_ms"], "dispatch_max_driver_ms": dsp["max_driver_ms"],
+                "launches": srv.stats()["launches"]})
         res["stats"] = srv.stats()
         res["kernel_stats"] = srv.kernel_stats()
         return res
