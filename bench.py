@@ -25,6 +25,7 @@ One JSON line on stdout (rank 0).  Keys beyond the common contract:
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import os
 import statistics
@@ -364,6 +365,28 @@ def main():
         else:
             plain_mismatch += int((po[:, 0] != out[sel, 0]).sum())
 
+    # ---- threads per signature (secp256k1): one lane against a lane pair per
+    # signature, for one warp alone (latency) and for all of the batch's
+    # secp256k1 items (throughput); outputs compared
+    lanes = {}
+    c0 = parts[0]
+    k1_sig, k1_msg, k1_n = c0[2], c0[3], c0[1]
+    for name, cnt in (("one_warp_16", 16), ("all_secp256k1", k1_n)):
+        row = {"items": int(cnt)}
+        outs = {}
+        for ln in (1, 2):
+            o = torch.zeros((cnt, 64), dtype=torch.uint8, device=dev)
+            st_ = torch.zeros(cnt, dtype=torch.uint8, device=dev)
+            ms = ctypes.c_float()
+            check(lib.sigops_probe_k1_lanes(ctx.ptr, ln, k1_sig.data_ptr(), k1_msg.data_ptr(), cnt, o.data_ptr(), st_.data_ptr(),
+                                            ctypes.byref(ms)), "sigops_probe_k1_lanes")
+            row[f"ms_{ln}_lane"] = ms.value
+            outs[ln] = (o, st_)
+        row["sigs_per_s_1_lane"] = cnt / (row["ms_1_lane"] * 1e-3)
+        row["sigs_per_s_2_lanes"] = cnt / (row["ms_2_lane"] * 1e-3)
+        row["outputs_equal"] = bool(torch.equal(outs[1][0], outs[2][0]) and torch.equal(outs[1][1], outs[2][1]))
+        lanes[name] = row
+
     # ---- end to end through the public API with page-locked host buffers
     e2e = None
     if not args.no_e2e:
@@ -456,6 +479,7 @@ def main():
                                     f"ed25519 {wmb['ed25519']:.0f} (profiles/work_model.json)")},
         "e2e": e2e,
         "serving": serving,
+        "threads_per_signature": dict(lanes, note="secp256k1 recovery, 1 lane vs a lane pair per signature (GLV halves on the two lanes)"),
         "cpu_baseline": cpu,
         # per step: classify + the fused kernel, or classify + three single-curve kernels
         "gpu_launches": (4 if split else 2) * args.steps,

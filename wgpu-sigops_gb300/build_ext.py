@@ -22,7 +22,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libsigops.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
-SOURCES = ["k_k1.cu", "k_r1.cu", "k_ed.cu", "k_sign.cu", "k_batched.cu", "k_batched_0.cu", "k_batched_1.cu", "k_batched_2.cu", "k_batched_3.cu", "k_batched_k1.cu", "k_batched_r1.cu", "k_batched_ed.cu", "k_batched_k1_w.cu", "k_batched_r1_w.cu", "k_batched_ed_w.cu", "k_misc.cu", "host.cu", "serving.cu", "noalloc.cu", "autotune.cu"]
+SOURCES = ["k_k1.cu", "k_r1.cu", "k_ed.cu", "k_sign.cu", "k_batched.cu", "k_batched_0.cu", "k_batched_1.cu", "k_batched_2.cu", "k_batched_3.cu", "k_batched_k1.cu", "k_batched_r1.cu", "k_batched_ed.cu", "k_batched_k1_w.cu", "k_batched_r1_w.cu", "k_batched_ed_w.cu", "k_misc.cu", "k_split.cu", "host.cu", "serving.cu", "noalloc.cu", "autotune.cu"]
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC,-O2", "-I" + INCLUDE, "-Xptxas", "-v"]

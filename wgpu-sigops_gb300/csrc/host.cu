@@ -795,6 +795,30 @@ int sigops_probe_mul(sigops_ctx* ctx, int form, double* rate) {
 
 int sigops_probe_imad(sigops_ctx* ctx, double* rate) { return sigops_probe_mul(ctx, 0, rate); }
 
+int sigops_probe_k1_lanes(sigops_ctx* ctx, int lanes, const uint8_t* d_sigs, const uint8_t* d_msgs, size_t n, uint8_t* d_out,
+                          uint8_t* d_status, float* ms) {
+  if ((lanes != 1 && lanes != 2) || !d_sigs || !d_msgs || !d_out || !d_status || !ms || n == 0)
+    return fail(SIGOPS_E_INVAL, "sigops_probe_k1_lanes: bad arguments");
+  auto misaligned = [](const void* p) { return ((uintptr_t)p & 15u) != 0; };
+  if (misaligned(d_sigs) || misaligned(d_msgs) || misaligned(d_out)) return fail(SIGOPS_E_INVAL, "device buffers must be 16-byte aligned");
+  sigops_ctx* c = resolve(ctx);
+  if (!c) return SIGOPS_E_NODEV;
+  std::lock_guard<std::mutex> g(c->mu);
+  SG_CUDA(cudaSetDevice(c->device));
+  cudaEvent_t a, b;
+  SG_CUDA(cudaEventCreate(&a));
+  SG_CUDA(cudaEventCreate(&b));
+  SG_CUDA(launch_k1_lanes(lanes, d_sigs, d_msgs, n, 0, c->d_gtab[0], d_out, d_status, c->stream));  // warm-up
+  SG_CUDA(cudaEventRecord(a, c->stream));
+  SG_CUDA(launch_k1_lanes(lanes, d_sigs, d_msgs, n, 0, c->d_gtab[0], d_out, d_status, c->stream));
+  SG_CUDA(cudaEventRecord(b, c->stream));
+  SG_CUDA(cudaEventSynchronize(b));
+  SG_CUDA(cudaEventElapsedTime(ms, a, b));
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  return SIGOPS_OK;
+}
+
 int sigops_device_info(sigops_ctx* ctx, int* num_sms, int* g1, int* g2, int* g3) {
   sigops_ctx* c = resolve(ctx);
   if (!c) return SIGOPS_E_NODEV;

@@ -92,6 +92,10 @@ void fork_streams_destroy(ForkStreams* f);
 cudaError_t launch_batched(const uint8_t* curves, const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks, size_t n, uint8_t* out,
                            uint8_t* status, uint32_t* idx, void* scratch, void* defer, const GenTables& tabs, uint32_t* err, int grid,
                            int variant, int classify_grid, const ForkStreams* fork, cudaStream_t stream);
+// secp256k1 recovery by 1 or 2 lanes per signature (k_split.cu)
+cudaError_t launch_k1_lanes(int lanes, const uint8_t* sigs, const uint8_t* msgs, size_t n, size_t threads, const uint32_t* gtab,
+                            uint8_t* out, uint8_t* status, cudaStream_t stream);
+
 // Record the calling thread's last-error message (sigops_last_error) and
 // return code (host.cu).
 int report(int code, const char* what);
