@@ -419,17 +419,44 @@ __device__ __forceinline__ uint32_t serve_next(const ServeArgs& a, uint32_t sm, 
 }
 
 // consumer warps: one tile at a time until the feeder closes and the rings are empty
+constexpr int SERVE_MAX_SEGS = 4;  // tiles a warp works on at once (their items fill its 32 lanes)
+
+// lane 0, after claiming the tile at `pos`: claim the next tiles of the same
+// curve while their items still fit the warp's lanes (a request's last tile
+// is mostly partial: a tenth of the lanes would idle).  Returns the tiles
+// held; their positions in segs[].
+__device__ __forceinline__ uint32_t serve_fill(const ServeArgs& a, uint32_t curve, uint64_t pos, uint64_t* segs) {
+  const ServeTile* ring = a.tiles + (size_t)curve * a.tile_cap;
+  segs[0] = pos;
+  uint32_t cnt = 1, total = min((ring[(uint32_t)(pos % a.tile_cap)].shape >> 16) & 0xffu, 32u);
+#pragma unroll 1
+  while (cnt < SERVE_MAX_SEGS && total < 32) {
+    const uint64_t tail = ld_acquire_gpu_u64(&a.dev->ring_tail[curve]);
+    const uint64_t head = *(volatile uint64_t*)&a.dev->ring_head[curve];
+    if (head >= tail) break;
+    const uint32_t n = min((ring[(uint32_t)(head % a.tile_cap)].shape >> 16) & 0xffu, 32u);
+    if (total + n > 32) break;
+    if (atomicCAS((unsigned long long*)&a.dev->ring_head[curve], head, head + 1) != head) continue;  // taken meanwhile: look again
+    segs[cnt++] = head;
+    total += n;
+  }
+  return cnt;
+}
+
+// consumer warps: one group of tiles at a time until the feeder closes and the rings are empty
 __device__ __forceinline__ void serve_consumer(const ServeArgs& a, uint32_t* stage) {
   const unsigned lane = threadIdx.x & 31u;
   const uint32_t sm = (smid() / SERVE_SMS_PER_SLOT) % SERVE_MODE_SLOTS;
   if (lane == 0) *(volatile uint32_t*)&a.dev->seen[sm] = 1u;
 #pragma unroll 1
   for (;;) {
-    uint32_t got = 0, curve = 0;
+    uint32_t got = 0, curve = 0, cnt = 0;
     uint64_t pos = 0, t_look = 0, t_got = 0;
+    uint64_t segs[SERVE_MAX_SEGS] = {0, 0, 0, 0};
     if (lane == 0) {
       t_look = globaltimer_ns();
       got = serve_next(a, sm, curve, pos);
+      if (got == 1) cnt = serve_fill(a, curve, pos, segs);
       t_got = globaltimer_ns();
       atomicAdd(&a.dev->idle_ns, (unsigned long long)(t_got - t_look));
       if (!got) atomicOr(&a.ctl->err, DEV_ERR_QUEUE_TIMEOUT);  // no tile and no close within the poll budget
@@ -437,26 +464,45 @@ __device__ __forceinline__ void serve_consumer(const ServeArgs& a, uint32_t* sta
     got = __shfl_sync(0xffffffffu, got, 0);
     if (got != 1) return;
     curve = __shfl_sync(0xffffffffu, curve, 0);
-    pos = __shfl_sync(0xffffffffu, pos, 0);
-    const ServeTile tl = a.tiles[(size_t)curve * a.tile_cap + (uint32_t)(pos % a.tile_cap)];
-    const uint32_t req = tl.shape & 0xffffu, n = min((tl.shape >> 16) & 0xffu, 32u);
-    {  // inputs into the staging area
+    cnt = __shfl_sync(0xffffffffu, cnt, 0);
+    // the tiles held: lanes base[j] .. base[j] + n[j] - 1 work on tile j
+    ServeTile tl[SERVE_MAX_SEGS];
+    uint32_t base[SERVE_MAX_SEGS], nseg[SERVE_MAX_SEGS];
+    uint32_t total = 0;
+#pragma unroll
+    for (int j = 0; j < SERVE_MAX_SEGS; ++j) {
+      const uint64_t p = __shfl_sync(0xffffffffu, segs[j], 0);
+      tl[j] = ServeTile{0, 0, 0, 0};
+      nseg[j] = 0;
+      base[j] = total;
+      if ((uint32_t)j < cnt) {
+        tl[j] = a.tiles[(size_t)curve * a.tile_cap + (uint32_t)(p % a.tile_cap)];
+        nseg[j] = min((tl[j].shape >> 16) & 0xffu, 32u - total);
+        total += nseg[j];
+      }
+    }
+    {  // inputs into the staging area: item base[j] + i of tile j at slot base[j] + i
       uint4* st4 = reinterpret_cast<uint4*>(stage);
-      const uint8_t* sig = a.sig + (size_t)tl.first * 64;
-      const uint8_t* msg = a.msg + (size_t)tl.first * 32;
-      const uint8_t* pk = a.pk + (size_t)tl.first * 32;
+#pragma unroll
+      for (int j = 0; j < SERVE_MAX_SEGS; ++j) {
+        const uint32_t n = nseg[j];
+        uint4* dst = st4 + base[j] * 8;
+        const uint8_t* sig = a.sig + (size_t)tl[j].first * 64;
+        const uint8_t* msg = a.msg + (size_t)tl[j].first * 32;
+        const uint8_t* pk = a.pk + (size_t)tl[j].first * 32;
 #pragma unroll 1
-      for (uint32_t c = lane; c < 4 * n; c += 32) st4[(c >> 2) * 8 + (c & 3)] = ld_sys_v4(sig + 16 * c);
+        for (uint32_t c = lane; c < 4 * n; c += 32) dst[(c >> 2) * 8 + (c & 3)] = ld_sys_v4(sig + 16 * c);
 #pragma unroll 1
-      for (uint32_t c = lane; c < 2 * n; c += 32) st4[(c >> 1) * 8 + 4 + (c & 1)] = ld_sys_v4(msg + 16 * c);
-      if (curve == 2) {
+        for (uint32_t c = lane; c < 2 * n; c += 32) dst[(c >> 1) * 8 + 4 + (c & 1)] = ld_sys_v4(msg + 16 * c);
+        if (curve == 2) {
 #pragma unroll 1
-        for (uint32_t c = lane; c < 2 * n; c += 32) st4[(c >> 1) * 8 + 6 + (c & 1)] = ld_sys_v4(pk + 16 * c);
+          for (uint32_t c = lane; c < 2 * n; c += 32) dst[(c >> 1) * 8 + 6 + (c & 1)] = ld_sys_v4(pk + 16 * c);
+        }
       }
     }
     __syncwarp();
     uint32_t st = 0;
-    if (lane < n) {
+    if (lane < total) {
       uint32_t* w = stage + lane * 32;
       uint32_t o[16];
       if (curve == 0) st = serve_item<0>(w, w + 16, w + 24, a.tabs.k1, o);
@@ -466,24 +512,31 @@ __device__ __forceinline__ void serve_consumer(const ServeArgs& a, uint32_t* sta
       for (int k = 0; k < 16; ++k) w[k] = o[k];
     }
     __syncwarp();
-    {  // result records into the pinned output ring
-      const uint4* st4 = reinterpret_cast<const uint4*>(stage);
-      uint4* out = reinterpret_cast<uint4*>(a.out + (size_t)tl.first * 64);
+#pragma unroll
+    for (int j = 0; j < SERVE_MAX_SEGS; ++j) {  // result records into the pinned output ring
+      const uint32_t n = nseg[j];
+      const uint4* src = reinterpret_cast<const uint4*>(stage) + base[j] * 8;
+      uint4* out = reinterpret_cast<uint4*>(a.out + (size_t)tl[j].first * 64);
 #pragma unroll 1
-      for (uint32_t c = lane; c < 4 * n; c += 32) out[c] = st4[(c >> 2) * 8 + (c & 3)];
+      for (uint32_t c = lane; c < 4 * n; c += 32) out[c] = src[(c >> 2) * 8 + (c & 3)];
+      if (lane >= base[j] && lane < base[j] + n) a.st[tl[j].first + (lane - base[j])] = (uint8_t)st;
     }
-    if (lane < n) a.st[tl.first + lane] = (uint8_t)st;
-    __threadfence_system();  // this lane's stores before the request's completion entry
+    __threadfence_system();  // this lane's stores before the requests' completion entries
     __syncwarp();
     if (lane == 0) {
-      if (atomicAdd(&a.count[req], n) + n == tl.target) {
-        __threadfence_system();
-        const uint64_t cpos = atomicAdd((unsigned long long*)&a.dev->comp_tail, 1ull);
-        st_release_sys_u64(&a.comp[cpos % a.R], serve_completion(cpos, req, tl.seq));
+#pragma unroll
+      for (int j = 0; j < SERVE_MAX_SEGS; ++j) {
+        if ((uint32_t)j >= cnt) break;
+        const uint32_t req = tl[j].shape & 0xffffu;
+        if (atomicAdd(&a.count[req], nseg[j]) + nseg[j] == tl[j].target) {
+          __threadfence_system();
+          const uint64_t cpos = atomicAdd((unsigned long long*)&a.dev->comp_tail, 1ull);
+          st_release_sys_u64(&a.comp[cpos % a.R], serve_completion(cpos, req, tl[j].seq));
+        }
       }
       atomicSub(&a.dev->busy[sm], 1u);
-      atomicAdd(&a.dev->tiles_done, 1ull);
-      atomicAdd(&a.dev->items_done, (unsigned long long)n);
+      atomicAdd(&a.dev->tiles_done, (unsigned long long)cnt);
+      atomicAdd(&a.dev->items_done, (unsigned long long)total);
       atomicAdd(&a.dev->work_ns, (unsigned long long)(globaltimer_ns() - t_got));
     }
   }
