@@ -175,8 +175,11 @@ __device__ __forceinline__ uint4 ld_sys_v4(const void* p) {
 // A warp's staging area: 32 items x 32 words (signature 0-15, message 16-23,
 // key 24-31); a result record replaces its item's signature words.  Items are
 // read from and written to the pinned rings as consecutive 16-byte chunks
-// (lane + 32 j: whole 128-byte lines).  (Exchanging them by shuffles instead,
-// with no shared memory, doubled a lone request's latency: measured.)
+// (lane + 32 j: whole 128-byte lines), one load in flight per lane: the
+// forms that keep several host-memory loads in flight per lane (all of a
+// lane's loads issued before its stores, weak loads the compiler batches,
+// loads exchanged by shuffles) each doubled a lone request's latency and made
+// a tile 20% slower under load (measured).
 constexpr int SERVE_STAGE_WORDS = 32 * 32;
 
 // One item of a served request
