@@ -267,6 +267,9 @@ int sigops_autotune(sigops_ctx* ctx, size_t probe_items, char* report, size_t re
  * flight at most (slots <= 0 selects 32), within hbm_fraction (default 0.25)
  * of the device memory free at creation.  Returns NULL on failure. */
 sigops_server* sigops_server_create(sigops_ctx* ctx, int slots, size_t slot_items, double hbm_fraction);
+/* Stops the kernel and the server's threads and frees everything; no other
+ * thread may be inside a call on the server.  Requests still in flight are
+ * dropped (their buffers are not written after this returns). */
 void sigops_server_destroy(sigops_server* server);
 size_t sigops_server_slot_items(sigops_server* server);
 /* Shape of the persistent kernel: 0 = 256-thread blocks, one per SM (default);

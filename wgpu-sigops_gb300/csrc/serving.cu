@@ -10,18 +10,21 @@
 //  * one persistent kernel (serve.cuh, launched cooperatively so that all its
 //    blocks are resident): a feeder warp copies published tiles into three
 //    device-resident tile rings, one per curve, and every other warp claims
-//    tiles of its SM's current curve, copies their items from the pinned
+//    tiles of its TPC's current curve, copies their items from the pinned
 //    rings into shared memory, verifies them and copies the results into the
 //    pinned output ring; the warp whose tile completes a request appends it
 //    to a pinned completion ring.
 //
 // Requests that arrive while others run become tiles behind them, and the
 // warps of the one kernel take them up as they free: continuous batching with
-// no launch, copy or host round trip per request.  A dispatcher thread on the
-// host copies each finished request's results to the caller's buffers,
-// relaunches the kernel when it has closed (idle or its lifetime cap) and work
-// is waiting, and fails the requests in flight if the kernel reports an
-// expired device wait.
+// no launch, copy or host round trip per request.  The host reads the
+// completion ring and copies each finished request's results to the caller's
+// buffers: the dispatcher thread does, and so does every thread waiting for a
+// request.  The dispatcher also relaunches the kernel when it has closed (idle
+// or its lifetime cap) and work is waiting, and fails the requests in flight
+// if the kernel reports an expired device wait.  It makes no driver call while
+// requests flow (the kernel reports its exit in a mapped word; free device
+// memory is read by a monitor thread).
 //
 // Admission is live, at submit time: a request is admitted when the item ring
 // (pinned; its tiles and counters in device memory, within hbm_fraction of
