@@ -420,12 +420,21 @@ def main():
     work = wmb["secp256k1_glv"] * counts[0] + wmb["secp256r1"] * counts[1] + wmb["ed25519"] * counts[2]
     achieved = work / (ms_step * 1e-3)
 
+    # DRAM traffic and pipe utilisation of the curve kernels in the configurations the
+    # step ran, from ncu captures on the 262,144-item mix (profiles/traffic_batched.json;
+    # the traffic is per-thread local memory, so it scales with the items)
     traffic = None
+    pipes = None
     tpath = os.path.join(ROOT, "profiles", "traffic_batched.json")
-    if os.path.exists(tpath):
+    if split and os.path.exists(tpath):
         with open(tpath) as f:
             t = json.load(f)
-        traffic = t.get("dram_bytes_per_sig", 0) * n if t.get("dram_bytes_per_sig") else None
+        v = info["variants"]["batched"]["variant"] - 4
+        cfgs = {"secp256k1": v % 8, "secp256r1": (v // 8) % 8, "ed25519": v // 64}
+        per = t.get("per_sig_bytes", {})
+        if all(str(cfgs[c]) in per.get(c, {}) for c in cfgs):
+            traffic = sum(per[c][str(cfgs[c])] * counts[k] for k, c in enumerate(("secp256k1", "secp256r1", "ed25519")))
+            pipes = {c: dict(t.get("pipes", {}).get(c, {}).get(str(cfgs[c]), {}), configuration=cfgs[c]) for c in cfgs}
 
     serving = None
     if args.serving_seconds > 0:
@@ -467,7 +476,7 @@ def main():
         "plain": {"ms_per_step": plain_ms, "value": dist.sum(n) / (plain_ms * 1e-3), "batched_over_plain": plain_ms / ms_step,
                   "outputs_equal_batched": plain_mismatch == 0, "per_curve": per_curve},
         "roofline": {"bound": "imad", "achieved": achieved / 1e12, "peak": mul_peak / 1e12, "unit": "Tmul32/s",
-                     "frac": achieved / mul_peak, "traffic": traffic,
+                     "frac": achieved / mul_peak, "traffic": traffic, "ncu_pipes": pipes,
                      # the same work against the plain mad.lo rate (the pipe's issue limit; half the
                      # counted multiplies are .hi forms, which issue at about 40% of that rate)
                      "frac_of_mad_lo": achieved / mul_forms["mad.lo"],
