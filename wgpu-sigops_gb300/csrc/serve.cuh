@@ -121,6 +121,7 @@ struct ServeArgs {
   BatchTables tabs;
   uint64_t idle_ns, life_ns;  // feeder: close after this long without a tile / in all
   uint32_t warps_per_sm;      // consumer warps an SM holds (a round of tiles)
+  uint32_t warp_cap;          // tiles a TPC works on at once while its curve has no backlog
   uint32_t launch;            // this launch's number (ServeCtl::exited)
 };
 
@@ -375,7 +376,11 @@ __device__ __forceinline__ uint32_t serve_next(const ServeArgs& a, uint32_t sm, 
 #pragma unroll 1
   for (uint32_t p = 0; p < SERVE_WAIT_MAX_POLLS; ++p) {
     const uint32_t cur = min(*(volatile uint32_t*)&a.dev->mode[sm], 2u);
-    if (ring_waiting(a, cur)) {
+    const uint64_t waiting = ring_waiting(a, cur);
+    // without a backlog a TPC holds at most warp_cap tiles, so that light load
+    // spreads over more TPCs (fewer warps per SM run faster) instead of
+    // filling the TPCs already on the curve
+    if (waiting && (waiting >= a.warp_cap || *(volatile uint32_t*)busy < a.warp_cap)) {
       atomicAdd(busy, 1u);  // counted from the claim on: the feeder sees the TPC's running tiles
       if (serve_claim(a, cur, pos)) {
         curve = cur;

@@ -172,6 +172,7 @@ cudaError_t launch_kernel(sigops_server* s) {
   a.idle_ns = 20ull * 1000 * 1000;    // close after 20 ms without a tile
   a.life_ns = 2000ull * 1000 * 1000;  // and after 2 s in all (the dispatcher relaunches)
   a.warps_per_sm = (uint32_t)(grid / s->cv.num_sms) * (uint32_t)(block / 32);
+  a.warp_cap = 8 * sg::SERVE_SMS_PER_SLOT;  // 8 warps per SM: the 256 x 1 shape's full load
   a.launch = ++s->launch_no;
   sg::serve_reset_kernel<<<1, 1, 0, s->stream>>>(s->dev, (uint32_t)grid * (uint32_t)(block / 32));
   cudaError_t e = cudaGetLastError();
