@@ -378,7 +378,7 @@ def main():
             o = torch.zeros((cnt, 64), dtype=torch.uint8, device=dev)
             st_ = torch.zeros(cnt, dtype=torch.uint8, device=dev)
             ms = ctypes.c_float()
-            check(lib.sigops_probe_k1_lanes(ctx.ptr, ln, k1_sig.data_ptr(), k1_msg.data_ptr(), cnt, o.data_ptr(), st_.data_ptr(),
+            check(lib.sigops_probe_k1_lanes(ctx.ptr, ln, 0, k1_sig.data_ptr(), k1_msg.data_ptr(), cnt, o.data_ptr(), st_.data_ptr(),
                                             ctypes.byref(ms)), "sigops_probe_k1_lanes")
             row[f"ms_{ln}_lane"] = ms.value
             outs[ln] = (o, st_)

@@ -374,11 +374,12 @@ int sigops_probe_mul(sigops_ctx* ctx, int form, double* per_second);
 /* Threads per signature, measured: secp256k1 recovery of the n signatures in
  * device buffers d_sigs / d_msgs by one thread per signature (lanes = 1, the
  * plain path) or by a lane pair per signature (lanes = 2: the GLV halves of
- * both scalars on the two lanes, partial sums combined by shuffles).  Results
+ * both scalars on the two lanes, partial sums combined by shuffles), in
+ * blocks of `block` threads (a multiple of 32 up to 256; 0 = 256).  Results
  * go to d_out (n x 64) / d_status (n); *ms = the kernel's time, CUDA events,
  * after one warm-up launch.  Test and measurement only.  No counterpart in the
  * reference. */
-int sigops_probe_k1_lanes(sigops_ctx* ctx, int lanes, const uint8_t* d_sigs, const uint8_t* d_msgs, size_t n, uint8_t* d_out,
+int sigops_probe_k1_lanes(sigops_ctx* ctx, int lanes, int block, const uint8_t* d_sigs, const uint8_t* d_msgs, size_t n, uint8_t* d_out,
                           uint8_t* d_status, float* ms);
 
 /* Number of SMs and the plain kernels' grid (blocks) for `curve`. */

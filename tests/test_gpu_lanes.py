@@ -29,7 +29,7 @@ def test_lane_pair_equals_one_lane():
         st = torch.full((n,), 0xFF, dtype=torch.uint8, device="cuda")
         ms = ctypes.c_float()
         torch.cuda.synchronize()
-        check(lib.sigops_probe_k1_lanes(w.default_context().ptr, lanes, d_sig.data_ptr(), d_msg.data_ptr(), n, out.data_ptr(),
+        check(lib.sigops_probe_k1_lanes(w.default_context().ptr, lanes, 0, d_sig.data_ptr(), d_msg.data_ptr(), n, out.data_ptr(),
                                         st.data_ptr(), ctypes.byref(ms)), "sigops_probe_k1_lanes")
         res[lanes] = (out.cpu().numpy(), st.cpu().numpy())
     assert (res[1][1] != 0xFF).all()

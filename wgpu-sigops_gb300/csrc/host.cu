@@ -277,6 +277,16 @@ Layout layout_for(int curve, size_t n) {
   return l;
 }
 
+// The plain kernel of `curve` for a batch of n: the tuned launch variant, or
+// for a batch too small to fill the GPU, one-warp blocks spread over the SMs
+// (secp256k1 with a lane pair per signature while few warps are needed)
+cudaError_t launch_plain_for(sigops_ctx* c, int curve, const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks, size_t n, uint8_t* out,
+                             uint8_t* status, cudaStream_t stream) {
+  if (plain_small_batch(n, c->num_sms))
+    return launch_plain_small(curve, sigs, msgs, pks, n, c->d_gtab[curve], out, status, c->d_err, c->num_sms, stream);
+  return launch_plain(curve, sigs, msgs, pks, n, c->d_gtab[curve], out, status, c->d_err, c->variant[curve], stream);
+}
+
 int run_host_call(sigops_ctx* ctx, int curve, const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks, size_t n, uint8_t* out,
                   uint8_t* out_status) {
   if (n == 0) return SIGOPS_OK;
@@ -292,8 +302,8 @@ int run_host_call(sigops_ctx* ctx, int curve, const uint8_t* sigs, const uint8_t
   memcpy(c->h_buf + l.msg, msgs, n * 32);
   if (curve == SIGOPS_ED25519) memcpy(c->h_buf + l.pk, pks, n * 32);
   SG_CUDA(cudaMemcpyAsync(c->d_buf, c->h_buf, l.out, cudaMemcpyHostToDevice, c->stream));
-  SG_CUDA(launch_plain(curve, c->d_buf + l.sig, c->d_buf + l.msg, c->d_buf + l.pk, n, c->d_gtab[curve], c->d_buf + l.out,
-                       c->d_buf + l.status, c->d_err, c->variant[curve], c->stream));
+  SG_CUDA(launch_plain_for(c, curve, c->d_buf + l.sig, c->d_buf + l.msg, c->d_buf + l.pk, n, c->d_buf + l.out, c->d_buf + l.status,
+                           c->stream));
   SG_CUDA(cudaMemcpyAsync(c->h_buf + l.out, c->d_buf + l.out, l.total - l.out, cudaMemcpyDeviceToHost, c->stream));
   rc = check_device_errors(c);
   if (rc) return rc;
@@ -541,7 +551,7 @@ int sigops_plain_device(sigops_ctx* ctx, int curve, const uint8_t* d_sigs, const
   std::lock_guard<std::mutex> g(c->mu);
   SG_CUDA(cudaSetDevice(c->device));
   cudaStream_t s = stream ? (cudaStream_t)stream : c->stream;
-  SG_CUDA(launch_plain(curve, d_sigs, d_msgs, d_pks, n, c->d_gtab[curve], d_out, d_status, c->d_err, c->variant[curve], s));
+  SG_CUDA(launch_plain_for(c, curve, d_sigs, d_msgs, d_pks, n, d_out, d_status, s));
   return SIGOPS_OK;
 }
 
@@ -795,9 +805,9 @@ int sigops_probe_mul(sigops_ctx* ctx, int form, double* rate) {
 
 int sigops_probe_imad(sigops_ctx* ctx, double* rate) { return sigops_probe_mul(ctx, 0, rate); }
 
-int sigops_probe_k1_lanes(sigops_ctx* ctx, int lanes, const uint8_t* d_sigs, const uint8_t* d_msgs, size_t n, uint8_t* d_out,
+int sigops_probe_k1_lanes(sigops_ctx* ctx, int lanes, int block, const uint8_t* d_sigs, const uint8_t* d_msgs, size_t n, uint8_t* d_out,
                           uint8_t* d_status, float* ms) {
-  if ((lanes != 1 && lanes != 2) || !d_sigs || !d_msgs || !d_out || !d_status || !ms || n == 0)
+  if ((lanes != 1 && lanes != 2) || block < 0 || block > 256 || block % 32 || !d_sigs || !d_msgs || !d_out || !d_status || !ms || n == 0)
     return fail(SIGOPS_E_INVAL, "sigops_probe_k1_lanes: bad arguments");
   auto misaligned = [](const void* p) { return ((uintptr_t)p & 15u) != 0; };
   if (misaligned(d_sigs) || misaligned(d_msgs) || misaligned(d_out)) return fail(SIGOPS_E_INVAL, "device buffers must be 16-byte aligned");
@@ -808,9 +818,9 @@ int sigops_probe_k1_lanes(sigops_ctx* ctx, int lanes, const uint8_t* d_sigs, con
   cudaEvent_t a, b;
   SG_CUDA(cudaEventCreate(&a));
   SG_CUDA(cudaEventCreate(&b));
-  SG_CUDA(launch_k1_lanes(lanes, d_sigs, d_msgs, n, 0, c->d_gtab[0], d_out, d_status, c->stream));  // warm-up
+  SG_CUDA(launch_k1_lanes(lanes, d_sigs, d_msgs, n, block, c->d_gtab[0], d_out, d_status, c->stream));  // warm-up
   SG_CUDA(cudaEventRecord(a, c->stream));
-  SG_CUDA(launch_k1_lanes(lanes, d_sigs, d_msgs, n, 0, c->d_gtab[0], d_out, d_status, c->stream));
+  SG_CUDA(launch_k1_lanes(lanes, d_sigs, d_msgs, n, block, c->d_gtab[0], d_out, d_status, c->stream));
   SG_CUDA(cudaEventRecord(b, c->stream));
   SG_CUDA(cudaEventSynchronize(b));
   SG_CUDA(cudaEventElapsedTime(ms, a, b));

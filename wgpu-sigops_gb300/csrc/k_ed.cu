@@ -58,6 +58,13 @@ cudaError_t launch_plain_ed(const uint8_t* sigs, const uint8_t* msgs, const uint
   return cudaGetLastError();
 }
 
+// a batch too small to fill the GPU: one warp per block, spread over the SMs
+cudaError_t launch_plain_ed_small(const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks, size_t n, const uint32_t* btab,
+                                  uint8_t* valid, uint8_t* status, uint32_t* err, cudaStream_t stream) {
+  ed_plain_kernel<32, 1><<<(unsigned)((n + 31) / 32), 32, 0, stream>>>(sigs, msgs, pks, n, btab, valid, status, err);
+  return cudaGetLastError();
+}
+
 int occupancy_plain_ed(int variant) {
   int b = 0;
   if (variant == 1) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, ed_plain_kernel<256, 2>, 256, 0);

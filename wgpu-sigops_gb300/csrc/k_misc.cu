@@ -145,6 +145,17 @@ cudaError_t launch_plain(int curve, const uint8_t* sigs, const uint8_t* msgs, co
   }
 }
 
+cudaError_t launch_plain_small(int curve, const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks, size_t n, const uint32_t* gtab,
+                               uint8_t* out, uint8_t* status, uint32_t* err, int num_sms, cudaStream_t stream) {
+  if (n == 0) return cudaSuccess;
+  switch (curve) {
+    case CURVE_SECP256K1: return launch_plain_k1_small(sigs, msgs, n, gtab, out, status, num_sms, stream);
+    case CURVE_SECP256R1: return launch_plain_r1_small(sigs, msgs, n, gtab, out, status, err, stream);
+    case CURVE_ED25519: return launch_plain_ed_small(sigs, msgs, pks, n, gtab, out, status, err, stream);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
 int plain_max_blocks_per_sm(int curve, int variant) {
   switch (curve) {
     case CURVE_SECP256K1: return occupancy_plain_k1(variant);

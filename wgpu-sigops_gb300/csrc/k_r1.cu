@@ -16,6 +16,14 @@ cudaError_t launch_plain_r1(const uint8_t* sigs, const uint8_t* msgs, size_t n, 
   return cudaGetLastError();
 }
 
+// a batch too small to fill the GPU: one warp per block, so the warps spread
+// over the SMs (a lone warp runs a signature faster than eight sharing an SM)
+cudaError_t launch_plain_r1_small(const uint8_t* sigs, const uint8_t* msgs, size_t n, const uint32_t* gtab, uint8_t* out, uint8_t* status,
+                                  uint32_t* err, cudaStream_t stream) {
+  ecdsa_plain_kernel<R1Traits, 32, 1><<<(unsigned)((n + 31) / 32), 32, 0, stream>>>(sigs, msgs, n, gtab, out, status, err);
+  return cudaGetLastError();
+}
+
 int occupancy_plain_r1(int variant) {
   int b = 0;
   if (variant == 1) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, ecdsa_plain_kernel<R1Traits, 256, 2>, 256, 0);

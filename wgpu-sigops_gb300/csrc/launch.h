@@ -21,6 +21,19 @@ inline int plain_variant_block(int variant) { return variant == 2 ? 128 : 256; }
 cudaError_t launch_plain(int curve, const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks, size_t n, const uint32_t* gtab,
                          uint8_t* out, uint8_t* status, uint32_t* err, int variant, cudaStream_t stream);
 int plain_max_blocks_per_sm(int curve, int variant);
+// a batch of at most 320 signatures per SM (10 warps: one partial wave of the
+// tuned kernels, which would pile whole blocks onto some SMs): one-warp blocks
+// spread evenly over the SMs, secp256k1 with a lane pair per signature while
+// that takes at most two warps per SM (k_split.cu, k_r1.cu, k_ed.cu)
+inline bool plain_small_batch(size_t n, int num_sms) { return n <= (size_t)num_sms * 320; }
+cudaError_t launch_plain_small(int curve, const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks, size_t n, const uint32_t* gtab,
+                               uint8_t* out, uint8_t* status, uint32_t* err, int num_sms, cudaStream_t stream);
+cudaError_t launch_plain_k1_small(const uint8_t* sigs, const uint8_t* msgs, size_t n, const uint32_t* gtab, uint8_t* out, uint8_t* status,
+                                  int num_sms, cudaStream_t stream);
+cudaError_t launch_plain_r1_small(const uint8_t* sigs, const uint8_t* msgs, size_t n, const uint32_t* gtab, uint8_t* out, uint8_t* status,
+                                  uint32_t* err, cudaStream_t stream);
+cudaError_t launch_plain_ed_small(const uint8_t* sigs, const uint8_t* msgs, const uint8_t* pks, size_t n, const uint32_t* btab,
+                                  uint8_t* valid, uint8_t* status, uint32_t* err, cudaStream_t stream);
 cudaError_t launch_plain_k1(const uint8_t* sigs, const uint8_t* msgs, size_t n, const uint32_t* gtab, uint8_t* out, uint8_t* status,
                             uint32_t* err, int variant, cudaStream_t stream);
 cudaError_t launch_plain_r1(const uint8_t* sigs, const uint8_t* msgs, size_t n, const uint32_t* gtab, uint8_t* out, uint8_t* status,
@@ -93,7 +106,7 @@ cudaError_t launch_batched(const uint8_t* curves, const uint8_t* sigs, const uin
                            uint8_t* status, uint32_t* idx, void* scratch, void* defer, const GenTables& tabs, uint32_t* err, int grid,
                            int variant, int classify_grid, const ForkStreams* fork, cudaStream_t stream);
 // secp256k1 recovery by 1 or 2 lanes per signature (k_split.cu)
-cudaError_t launch_k1_lanes(int lanes, const uint8_t* sigs, const uint8_t* msgs, size_t n, size_t threads, const uint32_t* gtab,
+cudaError_t launch_k1_lanes(int lanes, const uint8_t* sigs, const uint8_t* msgs, size_t n, int block, const uint32_t* gtab,
                             uint8_t* out, uint8_t* status, cudaStream_t stream);
 
 // Record the calling thread's last-error message (sigops_last_error) and
