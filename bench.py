@@ -17,6 +17,9 @@ One JSON line on stdout (rank 0).  Keys beyond the common contract:
                counted by the host build of the kernel source) x sigs/s, against
                the rate of the same instruction form (mad.lo.cc / madc.hi.cc
                carry-chain rows) measured in-process
+  drop_in_calls one call of ecrecover / ecverify (array form, table passed,
+               host buffers) per curve at the reference's benchmark sizes
+               (2^10..2^14; P-256 2^8..2^13): ms per call, outputs compared
   cpu_baseline the C restatement of the reference's CPU path (oracle port)
                on a bounded sample of the same batch, all host threads; its
                outputs are compared bit for bit with the GPU's on that sample
@@ -54,6 +57,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU-baseline sample duration")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-drop-in", action="store_true", help="skip the per-call timings at the reference's benchmark sizes")
     ap.add_argument("--serving-seconds", type=float, default=60.0, help="seconds per serving load level (0 = skip serving)")
     ap.add_argument("--variant", type=int, default=-1, help="batched kernel launch variant (-1 = library default)")
     ap.add_argument("--plain-variant", type=int, default=-1, help="plain kernels launch variant (-1 = library default)")
@@ -387,6 +391,39 @@ def main():
         row["outputs_equal"] = bool(torch.equal(outs[1][0], outs[2][0]) and torch.equal(outs[1][1], outs[2][1]))
         lanes[name] = row
 
+    # ---- one drop-in call per curve at the reference's own benchmark sizes
+    # (secp256k1 and ed25519 2^10..2^14, P-256 2^8..2^13: src/benchmarks/secp256k1_ecdsa.rs:10-11,
+    # src/benchmarks/ed25519_eddsa.rs:11-12, src/benchmarks/secp256r1_ecdsa.rs:13-14): the
+    # array form of ecrecover / ecverify with the generator table passed, host buffers in and
+    # out, copies and the table check inside the call; outputs compared with the batched run
+    drop_in = None
+    if not args.no_drop_in:
+        from wgpu_sig_ops import ed25519_eddsa, precompute, secp256k1_ecdsa, secp256r1_ecdsa
+
+        drop_in = {}
+        curve_calls = (("secp256k1", secp256k1_ecdsa.ecrecover_arrays, precompute.secp256k1_bases, range(10, 15)),
+                       ("secp256r1", secp256r1_ecdsa.ecrecover_arrays, precompute.secp256r1_bases, range(8, 14)),
+                       ("ed25519", ed25519_eddsa.ecverify_arrays, precompute.ed25519_bases, range(10, 15)))
+        for c, (name, fn, bases, logs) in enumerate(curve_calls):
+            sel = parts[c][7]
+            table = np.asarray(bases(13), dtype=np.uint32)
+            rows = []
+            for lg in logs:
+                m = min(1 << lg, len(sel))
+                idx = sel[:m]
+                call_args = (W.sigs[idx], W.msgs[idx]) + ((W.pks[idx],) if c == 2 else ())
+                for _ in range(2):
+                    res, st_ = fn(*call_args, table_limbs=table, log_limb_size=13, ctx=ctx)
+                ts = []
+                for _ in range(5):
+                    t0 = time.perf_counter()
+                    res, st_ = fn(*call_args, table_limbs=table, log_limb_size=13, ctx=ctx)
+                    ts.append(time.perf_counter() - t0)
+                same = bool((st_ == status[idx]).all() and ((res == out[idx]).all() if c < 2 else (res == out[idx, 0]).all()))
+                t = statistics.median(ts)
+                rows.append({"n": m, "ms_per_call": t * 1e3, "sigs_per_s": m / t, "matches_batched": same})
+            drop_in[name] = rows
+
     # ---- end to end through the public API with page-locked host buffers
     e2e = None
     if not args.no_e2e:
@@ -487,6 +524,7 @@ def main():
                                     f"the kernel source: secp256k1 (GLV) {wmb['secp256k1_glv']:.0f}, P-256 {wmb['secp256r1']:.0f}, "
                                     f"ed25519 {wmb['ed25519']:.0f} (profiles/work_model.json)")},
         "e2e": e2e,
+        "drop_in_calls": drop_in,
         "serving": serving,
         "threads_per_signature": dict(lanes, note="secp256k1 recovery, 1 lane vs a lane pair per signature (GLV halves on the two lanes)"),
         "cpu_baseline": cpu,

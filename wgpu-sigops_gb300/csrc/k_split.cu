@@ -34,7 +34,10 @@ SG_NOINL JPoint k1_glv_half(const u256 u1, const u256 u2, const APoint R, const 
   K1Glv::split(u2, k1, neg1, k2, neg2);
   APoint R1 = neg1 ? W::neg(R) : R;
   APoint tab[NR];
-  coz_table<F, false, NR>(R1, tab);
+  u256 zc;  // the chain runs on E' (coz_table_iso); generator entries enter as psi(P)
+  coz_table_iso<F, NR>(R1, tab, zc);
+  const u256 zc2 = F::sqr(zc);
+  const u256 zc3 = F::mul(zc2, zc);
   const bool flip = half ? neg1 != neg2 : false;
   const u256 beta = K1Glv::BETA();
   u256 a = u1, b = u256_zero();
@@ -67,12 +70,13 @@ SG_NOINL JPoint k1_glv_half(const u256 u1, const u256 u2, const APoint R, const 
       bool ng;
       const uint32_t d = booth_digit(kg, pos / WG, WG, ng);
       if (d) {
-        APoint e = load_apoint<WG>(gtab2, goff + d - 1);
+        APoint e = iso_point<F>(load_apoint<WG>(gtab2, goff + d - 1), zc2, zc3);
         if (ng) e = W::neg(e);
         acc = W::madd(acc, e);
       }
     }
   }
+  if (!W::is_inf(acc)) acc.Z = F::mul(acc.Z, zc);  // back to E; infinity keeps Z exactly 0
   return acc;
 }
 

@@ -120,9 +120,13 @@ SG_HD APoint load_apoint(const uint32_t* t, uint32_t idx) {
 // last Z followed by Z_k^-1 = Z_(k+1)^-1 d_(k+1) down the chain (no prefix
 // products).  No step meets an exceptional case: R has prime order above NR,
 // so kR != +-R for 2 <= k <= NR - 1 and R.y != 0.
+//
+// coz_chain builds the entries, tab[k] at its own Z_k = dz[1] ... dz[k]
+// (Z_0 = 1); coz_table makes them affine, coz_table_iso brings them to the
+// last Z without an inversion.
 template <class F, bool A_M3, int NR>
-SG_HD void coz_table(const APoint R, APoint* tab) {
-  u256 dz[NR];  // dz[1] = Z(2R); dz[k] = Z(tab[k]) / Z(tab[k-1]) for k >= 2
+SG_HD void coz_chain(const APoint R, APoint* tab, u256* dz) {
+  // dz[1] = Z(2R); dz[k] = Z(tab[k]) / Z(tab[k-1]) for k >= 2
   const u256 B = F::sqr(R.x);
   const u256 E = F::sqr(R.y);
   const u256 L = F::sqr(E);
@@ -152,6 +156,12 @@ SG_HD void coz_table(const APoint R, APoint* tab) {
     px = W1;
     py = A1;
   }
+}
+
+template <class F, bool A_M3, int NR>
+SG_HD void coz_table(const APoint R, APoint* tab) {
+  u256 dz[NR];
+  coz_chain<F, A_M3, NR>(R, tab, dz);
   u256 z = dz[1];
 #pragma unroll 1
   for (int k = 2; k < NR; ++k) z = F::mul(z, dz[k]);
@@ -163,6 +173,42 @@ SG_HD void coz_table(const APoint R, APoint* tab) {
     tab[k].y = F::mul(tab[k].y, F::mul(z2, inv));
     if (k > 1) inv = F::mul(inv, dz[k]);
   }
+}
+
+// The same multiples for a curve with a = 0, without the inversion: every
+// entry is brought to the chain's last Z, zc = Z_(NR-1), by s_k = zc / Z_k =
+// dz[k+1] ... dz[NR-1] (X s_k^2, Y s_k^3).  The entries are then affine points
+// of the isomorphic curve E': y^2 = x^3 + b zc^6, the image of E under
+// psi(x, y) = (zc^2 x, zc^3 y).  With a = 0 neither the doubling nor the
+// additions read a curve constant, so a chain on E' runs the same formulas;
+// a point of E added into it enters as psi(P) (two multiplications), and a
+// Jacobian result (X, Y, Z) on E' is (X, Y, Z zc) on E.  Against coz_table
+// this saves the inversion and the product of the dz (NR-2 multiplications)
+// and costs the same per entry.  psi commutes with negation and with
+// phi(x, y) = (beta x, y).  NR >= 2.
+template <class F, int NR>
+SG_HD void coz_table_iso(const APoint R, APoint* tab, u256& zc) {
+  u256 dz[NR];
+  coz_chain<F, false, NR>(R, tab, dz);
+  u256 sk = dz[NR - 1];  // s_(NR-2)
+#pragma unroll 1
+  for (int k = NR - 2;; --k) {
+    const u256 s2 = F::sqr(sk);
+    tab[k].x = F::mul(tab[k].x, s2);
+    tab[k].y = F::mul(tab[k].y, F::mul(s2, sk));
+    if (k == 0) break;
+    sk = F::mul(sk, dz[k]);
+  }
+  zc = sk;  // s_0 = Z_(NR-1) / Z_0
+}
+
+// psi(P) for P affine on E, zc2 = zc^2, zc3 = zc^3 (see coz_table_iso)
+template <class F>
+SG_HD APoint iso_point(const APoint& p, const u256& zc2, const u256& zc3) {
+  APoint r;
+  r.x = F::mul(p.x, zc2);
+  r.y = F::mul(p.y, zc3);
+  return r;
 }
 
 // u1 * G + u2 * R, signed fixed windows, one shared doubling chain.
@@ -274,7 +320,10 @@ SG_NOINL JPoint k1_glv_lincomb(const u256 u1, const u256 u2, const APoint R, con
   K1Glv::split(u2, k1, neg1, k2, neg2);
   APoint R1 = neg1 ? W::neg(R) : R;
   APoint tab[NR];
-  coz_table<F, false, NR>(R1, tab);
+  u256 zc;  // the chain runs on E' (coz_table_iso); generator entries enter as psi(P)
+  coz_table_iso<F, NR>(R1, tab, zc);
+  const u256 zc2 = F::sqr(zc);
+  const u256 zc3 = F::mul(zc2, zc);
   // phi(+-R) multiples: (beta x, +-y); k2's sign relative to k1's
   const bool flip2 = neg1 != neg2;
   const u256 beta = K1Glv::BETA();
@@ -311,18 +360,19 @@ SG_NOINL JPoint k1_glv_lincomb(const u256 u1, const u256 u2, const APoint R, con
       bool ng;
       uint32_t d = booth_digit(a, pos / WG, WG, ng);
       if (d) {
-        APoint e = load_apoint<WG>(gtab2, d - 1);
+        APoint e = iso_point<F>(load_apoint<WG>(gtab2, d - 1), zc2, zc3);
         if (ng) e = W::neg(e);
         acc = W::madd(acc, e);
       }
       d = booth_digit(b, pos / WG, WG, ng);
       if (d) {
-        APoint e = load_apoint<WG>(gtab2, HALF + d - 1);
+        APoint e = iso_point<F>(load_apoint<WG>(gtab2, HALF + d - 1), zc2, zc3);
         if (ng) e = W::neg(e);
         acc = W::madd(acc, e);
       }
     }
   }
+  if (!W::is_inf(acc)) acc.Z = F::mul(acc.Z, zc);  // back to E; infinity keeps Z exactly 0
   return acc;
 }
 
