@@ -17,6 +17,9 @@ One JSON line on stdout (rank 0).  Keys beyond the common contract:
                counted by the host build of the kernel source) x sigs/s, against
                the rate of the same instruction form (mad.lo.cc / madc.hi.cc
                carry-chain rows) measured in-process
+  warp_phases  secp256k1 by persistent warps, free-running (as the serving
+               kernel's) or starting each group of 32 together (as a plain
+               kernel's block): time per group, outputs compared
   drop_in_calls one call of ecrecover / ecverify (array form, table passed,
                host buffers) per curve at the reference's benchmark sizes
                (2^10..2^14; P-256 2^8..2^13): ms per call, outputs compared
@@ -391,6 +394,30 @@ def main():
         row["outputs_equal"] = bool(torch.equal(outs[1][0], outs[2][0]) and torch.equal(outs[1][1], outs[2][1]))
         lanes[name] = row
 
+    # ---- warp phases (secp256k1): persistent warps taking 32 items at a time,
+    # free-running as the serving kernel's warps, against warps that start every
+    # group together as a plain kernel's block; the batch's secp256k1 items four
+    # times over, so that the middle of the run (where the group times are
+    # averaged) is steady
+    phases = {}
+    ph_sig, ph_msg, ph_n = k1_sig.repeat(4, 1), k1_msg.repeat(4, 1), 4 * k1_n
+    ph_res = {}
+    for sync in (0, 1):
+        o = torch.zeros((ph_n, 64), dtype=torch.uint8, device=dev)
+        st_ = torch.zeros(ph_n, dtype=torch.uint8, device=dev)
+        times = torch.zeros(2 * ((ph_n + 31) // 32), dtype=torch.int64, device=dev)
+        ms = ctypes.c_float()
+        check(lib.sigops_probe_phase(ctx.ptr, sync, ph_sig.data_ptr(), ph_msg.data_ptr(), ph_n, o.data_ptr(), st_.data_ptr(),
+                                     times.data_ptr(), ctypes.byref(ms)), "sigops_probe_phase")
+        t = times.cpu().numpy().reshape(-1, 2).astype(np.float64)
+        lo, hi = t[:, 0].min(), t[:, 1].max()
+        mid = (t[:, 0] > lo + 0.2 * (hi - lo)) & (t[:, 1] < lo + 0.8 * (hi - lo))
+        phases["synchronised" if sync else "free_running"] = {"kernel_ms": ms.value, "group_ms": float((t[mid, 1] - t[mid, 0]).mean() / 1e6)}
+        ph_res[sync] = (o, st_)
+    phases["outputs_equal"] = bool(all(torch.equal(ph_res[k][0][:k1_n], c0[5]) and torch.equal(ph_res[k][1][:k1_n], c0[6]) for k in (0, 1))
+                                   and torch.equal(ph_res[0][0], ph_res[1][0]) and torch.equal(ph_res[0][1], ph_res[1][1]))
+    del ph_sig, ph_msg, ph_res
+
     # ---- one drop-in call per curve at the reference's own benchmark sizes
     # (secp256k1 and ed25519 2^10..2^14, P-256 2^8..2^13: src/benchmarks/secp256k1_ecdsa.rs:10-11,
     # src/benchmarks/ed25519_eddsa.rs:11-12, src/benchmarks/secp256r1_ecdsa.rs:13-14): the
@@ -527,6 +554,9 @@ def main():
         "drop_in_calls": drop_in,
         "serving": serving,
         "threads_per_signature": dict(lanes, note="secp256k1 recovery, 1 lane vs a lane pair per signature (GLV halves on the two lanes)"),
+        "warp_phases": dict(phases, items=int(4 * k1_n), block="256 x 1 per SM",
+                            note=("secp256k1 recovery by persistent warps, 32 items per group; group_ms = mean over the groups in "
+                                  "the middle 60% of the run")),
         "cpu_baseline": cpu,
         # per step: classify + the fused kernel, or classify + three single-curve kernels
         "gpu_launches": (4 if split else 2) * args.steps,

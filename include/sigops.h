@@ -382,6 +382,18 @@ int sigops_probe_mul(sigops_ctx* ctx, int form, double* per_second);
 int sigops_probe_k1_lanes(sigops_ctx* ctx, int lanes, int block, const uint8_t* d_sigs, const uint8_t* d_msgs, size_t n, uint8_t* d_out,
                           uint8_t* d_status, float* ms);
 
+/* Warp phases, measured: secp256k1 recovery of the n signatures in device
+ * buffers d_sigs / d_msgs (one thread per signature) by persistent warps, one
+ * 256-thread block per SM, each warp taking 32 items at a time: free-running
+ * (sync = 0, as the serving kernel's warps) or with a block's warps starting
+ * every group together (sync = 1, as a plain kernel's block).  Results go to
+ * d_out (n x 64) / d_status (n); d_times (2 ceil(n / 32) words) receives the
+ * global-timer start and end of each group of 32 items (ns); *ms = the
+ * kernel's time, CUDA events.  Test and measurement only.  No counterpart in
+ * the reference. */
+int sigops_probe_phase(sigops_ctx* ctx, int sync, const uint8_t* d_sigs, const uint8_t* d_msgs, size_t n, uint8_t* d_out,
+                       uint8_t* d_status, uint64_t* d_times, float* ms);
+
 /* Number of SMs and the plain kernels' grid (blocks) for `curve`. */
 int sigops_device_info(sigops_ctx* ctx, int* num_sms, int* plain_grid_k1, int* plain_grid_r1, int* plain_grid_ed);
 

@@ -829,6 +829,37 @@ int sigops_probe_k1_lanes(sigops_ctx* ctx, int lanes, int block, const uint8_t* 
   return SIGOPS_OK;
 }
 
+int sigops_probe_phase(sigops_ctx* ctx, int sync, const uint8_t* d_sigs, const uint8_t* d_msgs, size_t n, uint8_t* d_out,
+                       uint8_t* d_status, uint64_t* d_times, float* ms) {
+  if ((sync != 0 && sync != 1) || !d_sigs || !d_msgs || !d_out || !d_status || !d_times || !ms || n == 0)
+    return fail(SIGOPS_E_INVAL, "sigops_probe_phase: bad arguments");
+  auto misaligned = [](const void* p) { return ((uintptr_t)p & 15u) != 0; };
+  if (misaligned(d_sigs) || misaligned(d_msgs) || misaligned(d_out) || ((uintptr_t)d_times & 7u))
+    return fail(SIGOPS_E_INVAL, "device buffers must be 16-byte aligned (times: 8)");
+  sigops_ctx* c = resolve(ctx);
+  if (!c) return SIGOPS_E_NODEV;
+  std::lock_guard<std::mutex> g(c->mu);
+  SG_CUDA(cudaSetDevice(c->device));
+  unsigned long long* counter = nullptr;
+  SG_CUDA(dev_alloc((void**)&counter, sizeof(unsigned long long)));
+  cudaEvent_t a = nullptr, b = nullptr;
+  cudaError_t e = cudaEventCreate(&a);
+  if (e == cudaSuccess) e = cudaEventCreate(&b);
+  if (e == cudaSuccess) e = cudaMemsetAsync(counter, 0, sizeof(unsigned long long), c->stream);
+  if (e == cudaSuccess) e = cudaEventRecord(a, c->stream);
+  if (e == cudaSuccess)
+    e = launch_k1_phase(sync != 0, d_sigs, d_msgs, n, c->d_gtab[0], d_out, d_status, counter, (unsigned long long*)d_times, c->num_sms,
+                        c->stream);
+  if (e == cudaSuccess) e = cudaEventRecord(b, c->stream);
+  if (e == cudaSuccess) e = cudaEventSynchronize(b);
+  if (e == cudaSuccess) e = cudaEventElapsedTime(ms, a, b);
+  if (a) cudaEventDestroy(a);
+  if (b) cudaEventDestroy(b);
+  dev_free(counter);
+  if (e != cudaSuccess) return fail(SIGOPS_E_CUDA, "sigops_probe_phase: %s", cudaGetErrorString(e));
+  return SIGOPS_OK;
+}
+
 int sigops_device_info(sigops_ctx* ctx, int* num_sms, int* g1, int* g2, int* g3) {
   sigops_ctx* c = resolve(ctx);
   if (!c) return SIGOPS_E_NODEV;

@@ -56,24 +56,24 @@ SG_NOINL JPoint k1_glv_half(const u256 u1, const u256 u2, const APoint R, const 
 #pragma unroll 1
   for (int pos = TOP; pos >= 0; --pos) {
     acc = W::dbl(acc);
-    if (pos % WR == 0) {
+    // the R-side then the G-side window through one addition site
+    const uint32_t first = pos % WR == 0 ? 0u : 1u;
+    const uint32_t last = pos % WG == 0 ? 2u : 1u;
+#pragma unroll 1
+    for (uint32_t src = first; src < last; ++src) {
       bool ng;
-      const uint32_t d = booth_digit(kr, pos / WR, WR, ng);
-      if (d) {
-        APoint e = tab[d - 1];
+      const uint32_t d = src == 0 ? booth_digit(kr, pos / WR, WR, ng) : booth_digit(kg, pos / WG, WG, ng);
+      if (!d) continue;
+      APoint e;
+      if (src == 0) {
+        e = tab[d - 1];
         if (half) e.x = F::mul(e.x, beta);
-        if (ng != flip) e = W::neg(e);
-        acc = W::madd(acc, e);
+        if (flip) ng = !ng;
+      } else {
+        e = iso_point<F>(load_apoint<WG>(gtab2, goff + d - 1), zc2, zc3);
       }
-    }
-    if (pos % WG == 0) {
-      bool ng;
-      const uint32_t d = booth_digit(kg, pos / WG, WG, ng);
-      if (d) {
-        APoint e = iso_point<F>(load_apoint<WG>(gtab2, goff + d - 1), zc2, zc3);
-        if (ng) e = W::neg(e);
-        acc = W::madd(acc, e);
-      }
+      if (ng) e = W::neg(e);
+      acc = W::madd(acc, e);
     }
   }
   if (!W::is_inf(acc)) acc.Z = F::mul(acc.Z, zc);  // back to E; infinity keeps Z exactly 0
@@ -173,6 +173,70 @@ cudaError_t launch_k1_lanes(int lanes, const uint8_t* sigs, const uint8_t* msgs,
   const unsigned grid = (unsigned)((tot + block - 1) / block);
   if (lanes == 1) k1_lanes_kernel<1><<<grid, block, 0, stream>>>(sigs, msgs, n, gtab, out, status);
   else k1_lanes_kernel<2><<<grid, block, 0, stream>>>(sigs, msgs, n, gtab, out, status);
+  return cudaGetLastError();
+}
+
+// Warp phases, measured: secp256k1 recovery, one thread per signature, by
+// persistent warps that each take 32 items at a time.  Free-running (SYNC
+// false), a warp takes its next items as soon as it is done, as the serving
+// kernel's warps do, and after a few groups the warps of an SM are spread over
+// the phases of a recovery (square root, inversions, doubling chain) at any
+// one time.  Synchronised (SYNC true), a block's warps start every group
+// together, as a plain kernel's block does.  The two differ in how much of the
+// code the warps of an SM need at once, so in how often a warp waits for its
+// next instruction to be fetched.  times[2g], times[2g + 1]: global-timer
+// start and end of group g (items 32g .. 32g + 31).
+__device__ __forceinline__ unsigned long long phase_clock() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+template <bool SYNC>
+__global__ void __launch_bounds__(256, 1) k1_phase_kernel(const uint8_t* __restrict__ sigs, const uint8_t* __restrict__ msgs, size_t n,
+                                                          const uint32_t* __restrict__ gtab, uint8_t* __restrict__ out,
+                                                          uint8_t* __restrict__ status, unsigned long long* counter, unsigned long long* times) {
+  __shared__ unsigned long long block_base;
+  const unsigned lane = threadIdx.x & 31u;
+#pragma unroll 1
+  for (;;) {
+    unsigned long long base = 0;
+    if constexpr (SYNC) {
+      __syncthreads();  // every warp is done reading block_base
+      if (threadIdx.x == 0) block_base = atomicAdd(counter, (unsigned long long)blockDim.x);
+      __syncthreads();
+      if (block_base >= n) return;  // the same for the whole block
+      base = block_base + 32ull * (threadIdx.x >> 5);
+    } else {
+      if (lane == 0) base = atomicAdd(counter, 32ull);
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (base >= n) return;
+    }
+    if (base < n) {  // a synchronised block's last round may leave warps without items
+      const unsigned long long t0 = phase_clock();
+      const size_t i = base + lane;
+      if (i < n) {
+        uint32_t s[16], m[8], o[16];
+        load_words(sigs, i, 16, s);
+        load_words(msgs, i, 8, m);
+        const uint8_t st = ecdsa_recover<K1Traits, true>(s, m, gtab, o);
+        store_words(out, i, 16, o);
+        status[i] = st;
+      }
+      __syncwarp();
+      if (lane == 0) {
+        times[2 * (base / 32)] = t0;
+        times[2 * (base / 32) + 1] = phase_clock();
+      }
+    }
+  }
+}
+
+// one 256-thread block per SM (counter: one zeroed word)
+cudaError_t launch_k1_phase(bool sync, const uint8_t* sigs, const uint8_t* msgs, size_t n, const uint32_t* gtab, uint8_t* out,
+                            uint8_t* status, unsigned long long* counter, unsigned long long* times, int num_sms, cudaStream_t stream) {
+  if (sync) k1_phase_kernel<true><<<num_sms, 256, 0, stream>>>(sigs, msgs, n, gtab, out, status, counter, times);
+  else k1_phase_kernel<false><<<num_sms, 256, 0, stream>>>(sigs, msgs, n, gtab, out, status, counter, times);
   return cudaGetLastError();
 }
 

@@ -108,6 +108,10 @@ cudaError_t launch_batched(const uint8_t* curves, const uint8_t* sigs, const uin
 // secp256k1 recovery by 1 or 2 lanes per signature (k_split.cu)
 cudaError_t launch_k1_lanes(int lanes, const uint8_t* sigs, const uint8_t* msgs, size_t n, int block, const uint32_t* gtab,
                             uint8_t* out, uint8_t* status, cudaStream_t stream);
+// secp256k1 recovery by persistent warps, free-running or block-synchronised,
+// with per-group timings (k_split.cu)
+cudaError_t launch_k1_phase(bool sync, const uint8_t* sigs, const uint8_t* msgs, size_t n, const uint32_t* gtab, uint8_t* out,
+                            uint8_t* status, unsigned long long* counter, unsigned long long* times, int num_sms, cudaStream_t stream);
 
 // Record the calling thread's last-error message (sigops_last_error) and
 // return code (host.cu).

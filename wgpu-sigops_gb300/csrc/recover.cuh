@@ -228,24 +228,29 @@ SG_NOINL JPoint ecdsa_lincomb(const u256 u1, const u256 u2, const APoint R, cons
   JPoint acc = W::infinity();
 #pragma unroll 1
   for (int pos = TOP; pos >= 0; --pos) {
-    acc = W::dbl(acc);
-    if (pos % WR == 0) {
-      bool neg;
-      uint32_t d = booth_digit(u2, pos / WR, WR, neg);
-      if (d) {
-        APoint e = tab[d - 1];
-        if (neg) e = W::neg(e);
-        acc = W::madd(acc, e);
-      }
-    }
+    // the generator entry is read before the doubling, which hides the read
+    bool gneg = false;
+    uint32_t gd = 0;
+    APoint ge;
     if (pos % WG == 0) {
-      bool neg;
-      uint32_t d = booth_digit(u1, pos / WG, WG, neg);
-      if (d) {
-        APoint e = load_apoint<WG>(gtab, d - 1);
-        if (neg) e = W::neg(e);
-        acc = W::madd(acc, e);
-      }
+      gd = booth_digit(u1, pos / WG, WG, gneg);
+      if (gd) ge = load_apoint<WG>(gtab, gd - 1);
+    }
+    acc = W::dbl(acc);
+    // u2 R's then u1 G's window through one addition site (one copy of the
+    // mixed addition in the loop: see k1_glv_lincomb)
+    const uint32_t first = pos % WR == 0 ? 0u : 1u;
+    const uint32_t last = pos % WG == 0 ? 2u : 1u;
+#pragma unroll 1
+    for (uint32_t src = first; src < last; ++src) {
+      bool neg = gneg;
+      const uint32_t d = src == 0 ? booth_digit(u2, pos / WR, WR, neg) : gd;
+      if (!d) continue;
+      APoint e;
+      if (src == 0) e = tab[d - 1];
+      else e = ge;
+      if (neg) e = W::neg(e);
+      acc = W::madd(acc, e);
     }
   }
   return acc;
@@ -340,36 +345,28 @@ SG_NOINL JPoint k1_glv_lincomb(const u256 u1, const u256 u2, const APoint R, con
 #pragma unroll 1
   for (int pos = TOP; pos >= 0; --pos) {
     acc = W::dbl(acc);
-    if (pos % WR == 0) {
+    // the window additions at this position, in the order k1 R, k2 phi(R),
+    // a G, b 2^128 G, through one addition site: one copy of the mixed
+    // addition in the loop instead of four keeps the loop's code small
+    // enough for the instruction cache when warps run different phases
+    const uint32_t first = pos % WR == 0 ? 0u : 2u;
+    const uint32_t last = pos % WG == 0 ? 4u : 2u;
+#pragma unroll 1
+    for (uint32_t src = first; src < last; ++src) {
+      const bool rs = src < 2;
+      const u256 k = src == 0 ? k1 : src == 1 ? k2 : src == 2 ? a : b;
       bool ng;
-      uint32_t d = booth_digit(k1, pos / WR, WR, ng);
-      if (d) {
-        APoint e = tab[d - 1];
-        if (ng) e = W::neg(e);
-        acc = W::madd(acc, e);
+      const uint32_t d = rs ? booth_digit(k, pos / WR, WR, ng) : booth_digit(k, pos / WG, WG, ng);
+      if (!d) continue;
+      APoint e;
+      if (rs) {
+        e = tab[d - 1];
+        if (src == 1) e.x = F::mul(e.x, beta);
+      } else {
+        e = iso_point<F>(load_apoint<WG>(gtab2, (src == 3 ? (uint32_t)HALF : 0u) + d - 1), zc2, zc3);
       }
-      d = booth_digit(k2, pos / WR, WR, ng);
-      if (d) {
-        APoint e = tab[d - 1];
-        e.x = F::mul(e.x, beta);
-        if (ng != flip2) e = W::neg(e);
-        acc = W::madd(acc, e);
-      }
-    }
-    if (pos % WG == 0) {
-      bool ng;
-      uint32_t d = booth_digit(a, pos / WG, WG, ng);
-      if (d) {
-        APoint e = iso_point<F>(load_apoint<WG>(gtab2, d - 1), zc2, zc3);
-        if (ng) e = W::neg(e);
-        acc = W::madd(acc, e);
-      }
-      d = booth_digit(b, pos / WG, WG, ng);
-      if (d) {
-        APoint e = iso_point<F>(load_apoint<WG>(gtab2, HALF + d - 1), zc2, zc3);
-        if (ng) e = W::neg(e);
-        acc = W::madd(acc, e);
-      }
+      if (ng != (src == 1 && flip2)) e = W::neg(e);
+      acc = W::madd(acc, e);
     }
   }
   if (!W::is_inf(acc)) acc.Z = F::mul(acc.Z, zc);  // back to E; infinity keeps Z exactly 0

@@ -126,6 +126,8 @@ extern "C" {
     pub fn sigops_probe_mul(ctx: *mut SigopsCtx, form: c_int, per_second: *mut f64) -> c_int;
     pub fn sigops_probe_k1_lanes(ctx: *mut SigopsCtx, lanes: c_int, block: c_int, d_sigs: *const u8, d_msgs: *const u8, n: usize,
         d_out: *mut u8, d_status: *mut u8, ms: *mut f32) -> c_int;
+    pub fn sigops_probe_phase(ctx: *mut SigopsCtx, sync: c_int, d_sigs: *const u8, d_msgs: *const u8, n: usize, d_out: *mut u8,
+        d_status: *mut u8, d_times: *mut u64, ms: *mut f32) -> c_int;
     pub fn sigops_device_info(ctx: *mut SigopsCtx, num_sms: *mut c_int, plain_grid_k1: *mut c_int, plain_grid_r1: *mut c_int,
                               plain_grid_ed: *mut c_int) -> c_int;
     pub fn sigops_test_field(ctx: *mut SigopsCtx, field: c_int, op: c_int, a: *const u8, b: *const u8, out: *mut u8, n: usize) -> c_int;

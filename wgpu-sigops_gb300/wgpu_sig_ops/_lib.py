@@ -83,6 +83,7 @@ SIGNATURES = {
     "sigops_probe_imad": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_double)]),
     "sigops_probe_mul": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
     "sigops_probe_k1_lanes": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _vp, _vp, ctypes.c_size_t, _vp, _vp, ctypes.POINTER(ctypes.c_float)]),
+    "sigops_probe_phase": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp, ctypes.c_size_t, _vp, _vp, _vp, ctypes.POINTER(ctypes.c_float)]),
     "sigops_test_wait_expiry": (ctypes.c_int, [_vp, ctypes.c_uint32]),
     "sigops_device_info": (ctypes.c_int, [_vp] + [ctypes.POINTER(ctypes.c_int)] * 4),
     "sigops_test_field": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp, _sz]),
