@@ -18,7 +18,8 @@
 #define SG_DEV __device__ __forceinline__
 // once-per-signature routines (exponentiation chains, scalar multiplication):
 // compiled once and called, which keeps kernels small enough to compile fast
-#define SG_NOINL __host__ __device__ __noinline__
+// (inline: a non-template one may sit in a header included by several units)
+#define SG_NOINL inline __host__ __device__ __noinline__
 #else
 #define SG_HD inline
 #define SG_DEV inline

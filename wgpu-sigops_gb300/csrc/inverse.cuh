@@ -142,8 +142,11 @@ SG_HD void s30_to_wide(const S30& s, u256& lo, int32_t& top) {
   lo = x;
 }
 
-// x^-1 mod M for 0 < x < M, M odd, gcd(x, M) = 1 (returns 0 for x = 0)
-SG_HD u256 divstep_inverse(const u256& x, const u256& Mu, uint32_t minv30) {
+// x^-1 mod M for 0 < x < M, M odd, gcd(x, M) = 1 (returns 0 for x = 0).
+// A called function: the modulus is an argument, so every field of a kernel
+// (p and n of each curve) shares one copy of the divstep code, which keeps
+// the code that out-of-phase warps need at once small.
+SG_NOINL u256 divstep_inverse(const u256& x, const u256& Mu, uint32_t minv30) {
   const S30 M = s30_from_u256(Mu);
   S30 f = M, g = s30_from_u256(x), d, e;
 #pragma unroll
