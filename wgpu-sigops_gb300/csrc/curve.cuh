@@ -197,13 +197,16 @@ struct Edw {
     return r;
   }
 
-  // p + q, q in projective Niels form: 8M (complete); with need_t false T is
-  // left stale (7M), for a result that only a doubling reads
-  SG_HD static EPoint add(const EPoint& p, const ENiels& q, bool need_t = true) {
+  // p + q for either form of q: projective Niels (8M, complete), or (affine
+  // set) affine Niels held in the same struct with q.z unused, which skips the
+  // Z1 Z2 product (7M).  With need_t false T is left stale (one M fewer), for
+  // a result that only a doubling reads.  One formula for both lets a doubling
+  // chain add through one site.
+  SG_HD static EPoint add_either(const EPoint& p, const ENiels& q, bool affine, bool need_t) {
     u256 A = F::mul(F::sub(p.Y, p.X), q.ymx);
     u256 B = F::mul(F::add(p.Y, p.X), q.ypx);
     u256 C = F::mul(p.T, q.t2d);
-    u256 D = F::mul(p.Z, q.z);
+    u256 D = affine ? p.Z : F::mul(p.Z, q.z);
     D = F::add(D, D);
     u256 E = F::sub(B, A), Fv = F::sub(D, C), G = F::add(D, C), H = F::add(B, A);
     EPoint r;
@@ -214,20 +217,8 @@ struct Edw {
     return r;
   }
 
-  // p + q, q affine Niels: 7M (6M with need_t false, as above)
-  SG_HD static EPoint madd(const EPoint& p, const EAffNiels& q, bool need_t = true) {
-    u256 A = F::mul(F::sub(p.Y, p.X), q.ymx);
-    u256 B = F::mul(F::add(p.Y, p.X), q.ypx);
-    u256 C = F::mul(p.T, q.t2d);
-    u256 D = F::add(p.Z, p.Z);
-    u256 E = F::sub(B, A), Fv = F::sub(D, C), G = F::add(D, C), H = F::add(B, A);
-    EPoint r;
-    r.X = F::mul(E, Fv);
-    r.Y = F::mul(G, H);
-    r.T = need_t ? F::mul(E, H) : p.T;
-    r.Z = F::mul(Fv, G);
-    return r;
-  }
+  // p + q, q in projective Niels form
+  SG_HD static EPoint add(const EPoint& p, const ENiels& q, bool need_t = true) { return add_either(p, q, false, need_t); }
 
   SG_HD static ENiels to_niels(const EPoint& p) {
     ENiels n;
@@ -238,7 +229,6 @@ struct Edw {
     return n;
   }
   SG_HD static ENiels neg(const ENiels& q) { ENiels r; r.ypx = q.ymx; r.ymx = q.ypx; r.z = q.z; r.t2d = F::neg(q.t2d); return r; }
-  SG_HD static EAffNiels neg(const EAffNiels& q) { EAffNiels r; r.ypx = q.ymx; r.ymx = q.ypx; r.t2d = F::neg(q.t2d); return r; }
 
   // canonical encoding: y little-endian, sign of x in bit 255
   // (src/wgsl/ed25519_curve.wgsl compress; curve25519-dalek EdwardsPoint::compress)

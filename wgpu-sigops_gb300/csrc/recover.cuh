@@ -535,23 +535,29 @@ SG_NOINL EPoint ed_lincomb(const u256 s, const u256 k, const EPoint negA, const 
 #pragma unroll 1
   for (int pos = TOP; pos >= 0; --pos) {
     acc = Edw::dbl(acc, pos % WR == 0 || pos % WG == 0);
-    if (pos % WR == 0) {
+    // [k](-A)'s then [s]B's window through one addition site (one copy of the
+    // addition in the loop: see k1_glv_lincomb)
+    const uint32_t first = pos % WR == 0 ? 0u : 1u;
+    const uint32_t last = pos % WG == 0 ? 2u : 1u;
+#pragma unroll 1
+    for (uint32_t src = first; src < last; ++src) {
       bool neg;
-      uint32_t d = booth_digit(k, pos / WR, WR, neg);
-      if (d) {
-        ENiels e = tab[d - 1];
-        if (neg) e = Edw::neg(e);
-        acc = Edw::add(acc, e, pos % WG == 0);  // T only for a generator addition at this position
+      const uint32_t d = src == 0 ? booth_digit(k, pos / WR, WR, neg) : booth_digit(s, pos / WG, WG, neg);
+      if (!d) continue;
+      ENiels e;
+      if (src == 0) {
+        e = tab[d - 1];
+      } else {
+        const EAffNiels g = load_eniels<WG>(btab, d - 1);
+        e.ypx = g.ypx;
+        e.ymx = g.ymx;
+        e.z = u256_zero();  // unused: affine
+        e.t2d = g.t2d;
       }
-    }
-    if (pos % WG == 0) {
-      bool neg;
-      uint32_t d = booth_digit(s, pos / WG, WG, neg);
-      if (d) {
-        EAffNiels e = load_eniels<WG>(btab, d - 1);
-        if (neg) e = Edw::neg(e);
-        acc = Edw::madd(acc, e, false);  // a doubling or the compression comes next
-      }
+      if (neg) e = Edw::neg(e);
+      // T only where a generator addition follows at this position; none after
+      // the generator's (a doubling or the compression comes next)
+      acc = Edw::add_either(acc, e, src == 1, src == 0 && pos % WG == 0);
     }
   }
   return acc;
