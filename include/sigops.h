@@ -274,8 +274,25 @@ void sigops_server_destroy(sigops_server* server);
 size_t sigops_server_slot_items(sigops_server* server);
 /* Shape of the persistent kernel: 0 = 256-thread blocks, one per SM (default);
  * 1 = 128 x 3 per SM (170 registers); 2 = 256 x 2 (128 registers).  Applies
- * from the next launch of the kernel.  No counterpart in the reference. */
+ * from the next launch of the kernel, and ends an adaptive choice.  No
+ * counterpart in the reference. */
 int sigops_server_set_variant(sigops_server* server, int variant);
+
+/* Adaptive shape: each launch of the persistent kernel takes high_shape while
+ * the arrival rate (items accepted by submit per second, a moving average of
+ * 10 ms samples that follows a rise within a few samples and a fall over about
+ * 100 ms) is at least switch_items_per_s, and low_shape once it falls below
+ * 80% of it.  A running launch of the other shape is asked to close (after
+ * every tile already published) once it has run 20 ms.  Typically
+ * low_shape has the fewer warps per SM (lower latency) and high_shape the
+ * higher saturation.  SIGOPS_E_INVAL for a bad shape or a rate <= 0.  No
+ * counterpart in the reference. */
+int sigops_server_set_adaptive(sigops_server* server, int low_shape, int high_shape, double switch_items_per_s);
+
+/* The shape of the running (or last) launch, the number of shape switches
+ * the adaptive choice asked for, and the arrival-rate estimate (items/s).
+ * Any pointer may be NULL. */
+int sigops_server_shape_stats(sigops_server* server, int* shape, uint64_t* switches, double* items_per_s);
 
 /* Queue one request of n items.  curves: n tags, or NULL with uniform_curve
  * set for a single-curve request; pks may be NULL for ECDSA-only requests.

@@ -1,9 +1,9 @@
 """The continuous-batching serving loop: each request's result is the same
 alone and in the mix, for every shape of the persistent kernel; requests that
 arrive while others run are worked off by the running kernel (no launch per
-request); admission refuses what does not fit; cancel, the kernel's idle close
-and relaunch, a dispatcher that stops and failed allocations are handled
-without a device fault."""
+request); admission refuses what does not fit; the adaptive shape follows the
+load; cancel, the kernel's idle close and relaunch, a dispatcher that stops and
+failed allocations are handled without a device fault."""
 import time
 
 import numpy as np
@@ -271,3 +271,48 @@ def test_poisson_load_short(w, W):
     assert res["stats"]["launches"] >= 1
     ks = res["kernel_stats"]
     assert ks["items"] >= res["stats"]["items_done"] and ks["tiles"] * 32 >= ks["items"] and ks["work_s"] > 0
+
+
+def test_adaptive_shape(w, ref):
+    """With an adaptive shape the server runs the low-latency shape under light
+    load, switches to the high-throughput shape while items arrive faster than
+    the switch rate, and goes back once the load is gone; every result equals
+    the batched engine's."""
+    from wgpu_sig_ops.serving import Server, request_stream
+
+    pool, regions, ref_out, ref_st = ref
+    # rings for about 0.4 s of the stream below: only the dispatcher thread
+    # relaunches the kernel (the shape switch closes it), so the rings must
+    # ride out that thread going unscheduled for a while on a busy host
+    srv = Server(w.default_context(), slots=256, slot_items=4096)
+    srv.set_adaptive(0, 1, 1.0e6)
+    sl = slice(0, 100)
+    out, st, _ = srv.wait(srv.submit(pool["curves"][sl], pool["sigs"][sl], pool["msgs"][sl], pool["pks"][sl]))
+    assert srv.shape_stats()["shape"] == 0
+    assert (out == ref_out[sl]).all() and (st == ref_st[sl]).all()
+    # 1.5 s of Poisson arrivals at about 2.7M items/s (mean request ~270 items)
+    offs, cnts, arr = request_stream(regions, 10000.0, 1.5, seed=9)
+    rc, lat, wall, out, st = srv.run_load(pool, offs, cnts, arr)
+    busy = srv.shape_stats()
+    assert rc == 0 and (lat > 0).all()
+    assert busy["switches"] >= 1 and busy["shape"] == 1, busy
+    for o, c in zip(offs, cnts):
+        s2 = slice(int(o), int(o) + int(c))
+        assert (out[s2] == ref_out[s2]).all() and (st[s2] == ref_st[s2]).all()
+    # quiet again: the kernel closes when idle, and the next launch takes the low shape
+    time.sleep(0.4)
+    out, st, _ = srv.wait(srv.submit(pool["curves"][sl], pool["sigs"][sl], pool["msgs"][sl], pool["pks"][sl]))
+    quiet = srv.shape_stats()
+    srv.close()
+    assert quiet["shape"] == 0, quiet
+    assert (out == ref_out[sl]).all() and (st == ref_st[sl]).all()
+    from wgpu_sig_ops._lib import SIGOPS_E_INVAL, SigopsError
+
+    bad = Server(w.default_context(), slots=2, slot_items=64)
+    try:
+        for args in ((0, 3, 1.0), (-1, 1, 1.0), (0, 1, 0.0)):
+            with pytest.raises(SigopsError) as e:
+                bad.set_adaptive(*args)
+            assert e.value.code == SIGOPS_E_INVAL
+    finally:
+        bad.close()

@@ -107,6 +107,18 @@ struct sigops_server {
   uint32_t launch_no = 0;    // number of the running (or last) launch
   double exit_checked = 0;   // last driver-side look at the kernel (a fault would leave ServeCtl::exited unset)
   std::atomic<int> shape{0};
+  // adaptive shape (sigops_server_set_adaptive): each launch takes high_shape
+  // while the arrival rate is at least switch_rate items/s and low_shape once
+  // it falls below 80% of it; switch_rate 0 = the fixed shape above
+  int low_shape = 0, high_shape = 0;
+  double switch_rate = 0;
+  int running_shape = 0;    // shape of the running (or last) launch
+  bool switching = false;   // the running launch was asked to close for a new shape
+  double launched_at = 0;   // when it started
+  uint64_t shape_switches = 0;
+  uint64_t items_in = 0;    // items accepted by submit
+  uint64_t rate_items = 0;  // items_in at the last rate sample
+  double rate_t = 0, rate = 0;  // arrival rate, items/s (moving average of 10 ms samples)
   // host state, under mu
   std::mutex mu;
   std::condition_variable cond;
@@ -147,9 +159,21 @@ int grid_for(sigops_server* s, int shape, int* block) {
   return e == cudaSuccess ? b * s->cv.num_sms : 0;
 }
 
+// caller holds mu: the shape the next launch should have
+int wanted_shape(const sigops_server* s) {
+  if (s->switch_rate <= 0) return s->shape.load(std::memory_order_relaxed);
+  if (s->rate >= s->switch_rate) return s->high_shape;
+  if (s->rate < 0.8 * s->switch_rate) return s->low_shape;
+  return s->running_shape;  // between the two thresholds: keep the shape
+}
+
 // caller holds mu; the kernel is not running
 cudaError_t launch_kernel(sigops_server* s) {
-  const int shape = s->shape.load(std::memory_order_relaxed);
+  const int shape = wanted_shape(s);
+  s->running_shape = shape;
+  s->switching = false;
+  s->launched_at = now_s();
+  __atomic_store_n(&s->ctl->stop, 0u, __ATOMIC_RELEASE);  // a shape switch's close request (destroy sets it only after the dispatcher ended)
   int block = 0;
   const int grid = grid_for(s, shape, &block);
   if (grid <= 0) return cudaErrorInvalidConfiguration;
@@ -265,6 +289,53 @@ bool collect_completions(sigops_server* s, std::unique_lock<std::mutex>& lk, std
   return changed;
 }
 
+// The persistent kernel, under the lock: notice its exit (its last warp writes
+// ServeCtl::exited) and relaunch it when published tiles wait.  The
+// dispatcher calls this, and so does every thread waiting in
+// sigops_server_wait, so that a dispatcher the OS leaves unscheduled delays no
+// relaunch.  driver_check: also ask the driver, every 50 ms, about a launch
+// that has not reported its exit (a kernel that could not write the word);
+// only the dispatcher does, since driver calls from other threads can hold a
+// thread for milliseconds.  Returns whether requests failed.
+bool service_kernel(sigops_server* s, bool driver_check) {
+  bool changed = false;
+  bool exited = false;
+  if (s->running) {
+    exited = __atomic_load_n(&s->ctl->exited, __ATOMIC_ACQUIRE) == s->launch_no;
+    const double t = now_s();
+    if (!exited && driver_check && t - s->exit_checked > 0.05) {
+      s->exit_checked = t;
+      exited = cudaEventQuery(s->ev_exit) != cudaErrorNotReady;
+      s->max_driver = std::max(s->max_driver, now_s() - t);
+    }
+  }
+  if (exited) {
+    s->running = false;
+    const uint32_t err = __atomic_exchange_n(&s->ctl->err, 0u, __ATOMIC_ACQ_REL);
+    if (err) {
+      // a device wait expired: tiles may be lost, so nothing in flight can be trusted
+      s->broken = true;
+      fail_inflight(s, SIGOPS_E_TIMEDOUT);
+      changed = true;
+    }
+  }
+  if (!s->running && !s->broken && !s->stop && __atomic_load_n(&s->ctl->tiles_fed, __ATOMIC_ACQUIRE) < s->tiles_published) {
+    const double t = now_s();
+    cudaError_t e = cudaSetDevice(s->cv.device);  // a waiting thread may not have the device current
+    if (e == cudaSuccess) e = launch_kernel(s);
+    s->max_driver = std::max(s->max_driver, now_s() - t);
+    if (e == cudaSuccess) {
+      s->running = true;
+      s->launches++;
+    } else {
+      s->broken = true;
+      fail_inflight(s, SIGOPS_E_CUDA);
+      changed = true;
+    }
+  }
+  return changed;
+}
+
 void worker_loop(sigops_server* s) {
   cudaSetDevice(s->cv.device);
   std::unique_lock<std::mutex> lk(s->mu);
@@ -280,42 +351,24 @@ void worker_loop(sigops_server* s) {
       s->iterations++;
     }
     bool changed = collect_completions(s, lk, finished);
-    // the persistent kernel: notice its exit (its last warp writes ServeCtl::exited;
-    // the driver is asked only every 50 ms: its calls from other threads can hold
-    // this one for milliseconds), relaunch it when work waits
-    bool exited = false;
-    if (s->running) {
-      exited = __atomic_load_n(&s->ctl->exited, __ATOMIC_ACQUIRE) == s->launch_no;
+    {  // arrival rate; with an adaptive shape, a running launch of the other shape is asked to close
+      // 10 ms samples; the estimate follows a rise within a few samples (an
+      // overloaded low shape builds a backlog) and a fall over about 100 ms
       const double t = now_s();
-      if (!exited && t - s->exit_checked > 0.05) {
-        s->exit_checked = t;
-        exited = cudaEventQuery(s->ev_exit) != cudaErrorNotReady;
-        s->max_driver = std::max(s->max_driver, now_s() - t);
+      if (t - s->rate_t >= 0.01) {
+        const double inst = s->rate_t > 0 ? (double)(s->items_in - s->rate_items) / (t - s->rate_t) : 0.0;
+        const double k = inst > s->rate ? 0.5 : 0.1;
+        s->rate += k * (inst - s->rate);
+        s->rate_t = t;
+        s->rate_items = s->items_in;
+      }
+      if (s->running && !s->switching && s->switch_rate > 0 && wanted_shape(s) != s->running_shape && t - s->launched_at > 0.02) {
+        s->switching = true;
+        s->shape_switches++;
+        __atomic_store_n(&s->ctl->stop, 1u, __ATOMIC_RELEASE);  // the kernel finishes every published tile, then exits
       }
     }
-    if (exited) {
-      s->running = false;
-      const uint32_t err = __atomic_exchange_n(&s->ctl->err, 0u, __ATOMIC_ACQ_REL);
-      if (err) {
-        // a device wait expired: tiles may be lost, so nothing in flight can be trusted
-        s->broken = true;
-        fail_inflight(s, SIGOPS_E_TIMEDOUT);
-        changed = true;
-      }
-    }
-    if (!s->running && !s->broken && __atomic_load_n(&s->ctl->tiles_fed, __ATOMIC_ACQUIRE) < s->tiles_published) {
-      const double t = now_s();
-      const cudaError_t e = launch_kernel(s);
-      s->max_driver = std::max(s->max_driver, now_s() - t);
-      if (e == cudaSuccess) {
-        s->running = true;
-        s->launches++;
-      } else {
-        s->broken = true;
-        fail_inflight(s, SIGOPS_E_CUDA);
-        changed = true;
-      }
-    }
+    if (service_kernel(s, true)) changed = true;
     reclaim(s);
     if (changed) s->cond.notify_all();
     // poll completions every 20 us while requests are in flight
@@ -354,7 +407,28 @@ extern "C" {
 
 int sigops_server_set_variant(sigops_server* s, int variant) {
   if (!s || variant < 0 || variant >= kServeShapes) return SIGOPS_E_INVAL;
+  std::lock_guard<std::mutex> g(s->mu);
   s->shape.store(variant, std::memory_order_relaxed);
+  s->switch_rate = 0;
+  return SIGOPS_OK;
+}
+
+int sigops_server_set_adaptive(sigops_server* s, int low_shape, int high_shape, double switch_items_per_s) {
+  if (!s || low_shape < 0 || low_shape >= kServeShapes || high_shape < 0 || high_shape >= kServeShapes || !(switch_items_per_s > 0))
+    return SIGOPS_E_INVAL;
+  std::lock_guard<std::mutex> g(s->mu);
+  s->low_shape = low_shape;
+  s->high_shape = high_shape;
+  s->switch_rate = switch_items_per_s;
+  return SIGOPS_OK;
+}
+
+int sigops_server_shape_stats(sigops_server* s, int* shape, uint64_t* switches, double* items_per_s) {
+  if (!s) return SIGOPS_E_INVAL;
+  std::lock_guard<std::mutex> g(s->mu);
+  if (shape) *shape = s->running_shape;
+  if (switches) *switches = s->shape_switches;
+  if (items_per_s) *items_per_s = s->rate;
   return SIGOPS_OK;
 }
 
@@ -500,6 +574,7 @@ int sigops_server_submit(sigops_server* s, const uint8_t* curves, int uniform_cu
     s->handles[r->id] = r;
     s->slots_taken++;
     s->queued_items += n;
+    s->items_in += n;
     *handle = r->id;
   }
   // inputs into the pinned ring grouped by curve (secp256k1, P-256, ed25519),
@@ -569,6 +644,7 @@ int sigops_server_wait(sigops_server* s, uint64_t handle, int timeout_ms, double
   const auto deadline = Clock::now() + std::chrono::milliseconds(timeout_ms < 0 ? 0 : timeout_ms);
   while (!pred()) {
     collect_completions(s, lk, finished);
+    if (s->alive && service_kernel(s, false)) s->cond.notify_all();
     if (pred()) break;
     if (timeout_ms >= 0 && Clock::now() >= deadline) return SIGOPS_E_TIMEDOUT;
     s->cond.wait_for(lk, std::chrono::microseconds(50));

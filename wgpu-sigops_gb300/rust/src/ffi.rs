@@ -99,6 +99,8 @@ extern "C" {
     pub fn sigops_server_destroy(server: *mut SigopsServer);
     pub fn sigops_server_slot_items(server: *mut SigopsServer) -> usize;
     pub fn sigops_server_set_variant(server: *mut SigopsServer, variant: c_int) -> c_int;
+    pub fn sigops_server_set_adaptive(server: *mut SigopsServer, low_shape: c_int, high_shape: c_int, switch_items_per_s: f64) -> c_int;
+    pub fn sigops_server_shape_stats(server: *mut SigopsServer, shape: *mut c_int, switches: *mut u64, items_per_s: *mut f64) -> c_int;
     pub fn sigops_server_submit(server: *mut SigopsServer, curves: *const u8, uniform_curve: c_int, sigs: *const u8, msgs: *const u8,
                                 pks: *const u8, n: usize, out: *mut u8, status: *mut u8, handle: *mut u64) -> c_int;
     pub fn sigops_server_wait(server: *mut SigopsServer, handle: u64, timeout_ms: c_int, latency_ms: *mut f64) -> c_int;

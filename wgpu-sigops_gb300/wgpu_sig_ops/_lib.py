@@ -69,6 +69,8 @@ SIGNATURES = {
     "sigops_server_destroy": (None, [_vp]),
     "sigops_server_slot_items": (_sz, [_vp]),
     "sigops_server_set_variant": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "sigops_server_set_adaptive": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_double]),
+    "sigops_server_shape_stats": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_double)]),
     "sigops_server_submit": (ctypes.c_int, [_vp, _vp, ctypes.c_int, _vp, _vp, _vp, _sz, _vp, _vp, ctypes.POINTER(ctypes.c_uint64)]),
     "sigops_server_wait": (ctypes.c_int, [_vp, ctypes.c_uint64, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
     "sigops_server_cancel": (ctypes.c_int, [_vp, ctypes.c_uint64]),

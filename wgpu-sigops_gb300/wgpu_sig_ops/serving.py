@@ -44,6 +44,17 @@ class Server:
         """Shape of the persistent kernel (0..2), from its next launch on."""
         check(lib.sigops_server_set_variant(self.ptr, variant), "sigops_server_set_variant")
 
+    def set_adaptive(self, low_shape: int, high_shape: int, switch_items_per_s: float):
+        """Each launch takes high_shape while items arrive at switch_items_per_s
+        or more, low_shape below 80% of it."""
+        check(lib.sigops_server_set_adaptive(self.ptr, low_shape, high_shape, float(switch_items_per_s)), "sigops_server_set_adaptive")
+
+    def shape_stats(self) -> dict:
+        """Shape of the running (or last) launch, adaptive switches, arrival rate."""
+        sh, sw, r = ctypes.c_int(), ctypes.c_uint64(), ctypes.c_double()
+        check(lib.sigops_server_shape_stats(self.ptr, ctypes.byref(sh), ctypes.byref(sw), ctypes.byref(r)), "sigops_server_shape_stats")
+        return {"shape": sh.value, "switches": sw.value, "items_per_s": r.value}
+
     def submit(self, curves, sigs: np.ndarray, msgs: np.ndarray, pks: np.ndarray | None = None) -> int:
         """Queue one request; ``curves`` is an array of tags or a single curve id."""
         sigs = np.ascontiguousarray(sigs, dtype=np.uint8).reshape(-1, 64)
@@ -185,15 +196,21 @@ def request_stream(regions: dict, rate_rps: float, seconds: float, seed: int, ma
 
 
 def measure(ctx, W, loads=(0.25, 0.5, 0.75, 0.9), seconds: float = 10.0, seed: int = 5001, slots: int = 0,
-            slot_items: int = 0, sat_items: int = 2_000_000, variant: int | None = None, warmup_seconds: float = 1.0) -> dict:
+            slot_items: int = 0, sat_items: int = 2_000_000, variant: int | None = None, warmup_seconds: float = 1.0,
+            adaptive: tuple | None = None) -> dict:
     """Saturation, a discarded warm-up run at half load, then open-loop Poisson
     load levels; latency percentiles in ms.  slots = 0 sizes the request rings
     to hold the whole saturation backlog (plus 10%), and at least 1M items
-    (about 50 ms of work at saturation, 200 MB of pinned memory)."""
+    (about 50 ms of work at saturation, 200 MB of pinned memory).  adaptive:
+    (low_shape, high_shape, switch_items_per_s) for Server.set_adaptive, set
+    after the saturation run, which runs high_shape (the shape a sustained
+    overload gets)."""
     pool, regions = curve_sorted_pool(W)
     per = slot_items or 16384
     if slots <= 0:
         slots = max(int(np.ceil(1_048_576 / per)), int(np.ceil(1.1 * sat_items / per)))
+    if adaptive is not None:
+        variant = adaptive[1]
     srv = Server(ctx, slots=slots, slot_items=slot_items, variant=variant)
     try:
         mean_size = float(np.mean(np.clip(np.floor(np.exp(np.random.default_rng(1).uniform(0, np.log(2048), 200000))), 1, 2048)))
@@ -206,6 +223,9 @@ def measure(ctx, W, loads=(0.25, 0.5, 0.75, 0.9), seconds: float = 10.0, seed: i
         sat = float(cnts[lat >= 0].sum()) / wall
         res = {"saturation_sigs_per_s": sat, "mean_request_items": mean_size, "slot_items": srv.slot_items, "slots": slots, "kernel_shape": 0 if variant is None else variant,
                "seconds_per_level": seconds, "warmup_seconds": warmup_seconds, "levels": []}
+        if adaptive is not None:
+            res["adaptive"] = {"low_shape": adaptive[0], "high_shape": adaptive[1], "switch_items_per_s": float(adaptive[2])}
+            srv.set_adaptive(*adaptive)
         if warmup_seconds > 0:  # an open-loop run at half load whose latencies are discarded
             offs, cnts, arr = request_stream(regions, 0.5 * sat / mean_size, warmup_seconds, seed + 100)
             check(srv.run_load(pool, offs, cnts, arr)[0], "warm-up run")
@@ -214,9 +234,11 @@ def measure(ctx, W, loads=(0.25, 0.5, 0.75, 0.9), seconds: float = 10.0, seed: i
             offs, cnts, arr = request_stream(regions, rate, seconds, seed + 1 + k)
             k0 = srv.kernel_stats()
             srv.dispatch_stats()
+            sh0 = srv.shape_stats()
             rc, lat, wall, out, st = srv.run_load(pool, offs, cnts, arr)
             k1 = srv.kernel_stats()
             dsp = srv.dispatch_stats()
+            sh1 = srv.shape_stats()
             ok = lat >= 0
             work, idle, tiles = k1["work_s"] - k0["work_s"], k1["idle_s"] - k0["idle_s"], k1["tiles"] - k0["tiles"]
             res["levels"].append({
@@ -227,7 +249,7 @@ def measure(ctx, W, loads=(0.25, 0.5, 0.75, 0.9), seconds: float = 10.0, seed: i
                 "kernel_busy": work / (work + idle) if work + idle > 0 else 0.0,
                 "warp_ms_per_tile": 1e3 * work / tiles if tiles else 0.0, "sm_moves": k1["sm_moves"] - k0["sm_moves"],
                 "dispatch_max_gap_ms": dsp["max_gap_ms"], "dispatch_max_driver_ms": dsp["max_driver_ms"],
-                "launches": srv.stats()["launches"]})
+                "launches": srv.stats()["launches"], "shape_at_end": sh1["shape"], "shape_switches": sh1["switches"] - sh0["switches"]})
         res["stats"] = srv.stats()
         res["kernel_stats"] = srv.kernel_stats()
         return res
