@@ -280,9 +280,8 @@ int sigops_server_set_variant(sigops_server* server, int variant);
 
 /* Adaptive shape: each launch of the persistent kernel takes high_shape while
  * the arrival rate (items accepted by submit per second, a moving average of
- * 10 ms samples that follows a rise within a few samples and a fall over about
- * 100 ms) is at least switch_items_per_s, and low_shape once it falls below
- * 80% of it.  A running launch of the other shape is asked to close (after
+ * 10 ms samples with weight 1/4: about 40 ms to follow a step) is at least
+ * switch_items_per_s, and low_shape once it falls below 80% of it.  A running launch of the other shape is asked to close (after
  * every tile already published) once it has run 20 ms.  Typically
  * low_shape has the fewer warps per SM (lower latency) and high_shape the
  * higher saturation.  SIGOPS_E_INVAL for a bad shape or a rate <= 0.  No
