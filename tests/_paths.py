@@ -10,7 +10,7 @@ HOSTCHECK_LIB = os.path.join(ROOT, "tests", "hostcheck", "libhostcheck.so")
 
 def build_hostcheck() -> str:
     """g++ build of the kernels' arithmetic for the host (test-only library)."""
-    deps = [HOSTCHECK_SRC] + [os.path.join(PKG, "csrc", f) for f in os.listdir(os.path.join(PKG, "csrc")) if f.endswith(".cuh")]
+    deps = [HOSTCHECK_SRC] + [os.path.join(PKG, "csrc", f) for f in os.listdir(os.path.join(PKG, "csrc")) if f.endswith((".cuh", ".h"))]
     if os.path.exists(HOSTCHECK_LIB) and all(os.path.getmtime(HOSTCHECK_LIB) >= os.path.getmtime(d) for d in deps):
         return HOSTCHECK_LIB
     subprocess.run(["g++", "-O2", "-std=c++17", "-shared", "-fPIC", "-o", HOSTCHECK_LIB + ".tmp", HOSTCHECK_SRC], check=True)

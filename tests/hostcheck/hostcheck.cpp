@@ -4,6 +4,7 @@
 // the library.
 #include <string.h>
 #include "../../wgpu-sigops_gb300/csrc/tables.cuh"
+#include "../../wgpu-sigops_gb300/csrc/serve_policy.h"
 
 using namespace sg;
 
@@ -354,3 +355,24 @@ extern "C" void hc_batched_deferred(int curve, const uint8_t* sigs, const uint8_
   else if (curve == 1) deferred_ecdsa<R1Traits, false>(sigs, msgs, n, batch, g_r1, out, status);
   else deferred_ed(sigs, msgs, pks, n, batch, out, status);
 }
+
+// The serving loop's adaptive shape (serve_policy.h) over simulated arrivals:
+// a dispatcher that looks every step_s seconds, items_cum[i] = items accepted
+// by step i.  shapes[i] = the shape a launch at step i would take (a shape
+// switch needs a relaunch; here every step counts as one), rates[i] = the
+// estimate.  switch_rate 0 = the fixed shape.
+extern "C" void hc_shape_policy_run(int low, int high, double switch_rate, int fixed, const uint64_t* items_cum, int steps, double step_s,
+                                    int* shapes, double* rates) {
+  sg::ShapePolicy p;
+  p.low = low;
+  p.high = high;
+  p.switch_rate = switch_rate;
+  int running = p.wanted(fixed, fixed);
+  for (int i = 0; i < steps; ++i) {
+    p.observe((i + 1) * step_s, items_cum[i]);
+    running = p.wanted(fixed, running);
+    shapes[i] = running;
+    rates[i] = p.rate;
+  }
+}
+

@@ -50,6 +50,7 @@
 #include "../../include/sigops.h"
 #include "launch.h"
 #include "serve.cuh"
+#include "serve_policy.h"
 
 namespace {
 
@@ -107,18 +108,14 @@ struct sigops_server {
   uint32_t launch_no = 0;    // number of the running (or last) launch
   double exit_checked = 0;   // last driver-side look at the kernel (a fault would leave ServeCtl::exited unset)
   std::atomic<int> shape{0};
-  // adaptive shape (sigops_server_set_adaptive): each launch takes high_shape
-  // while the arrival rate is at least switch_rate items/s and low_shape once
-  // it falls below 80% of it; switch_rate 0 = the fixed shape above
-  int low_shape = 0, high_shape = 0;
-  double switch_rate = 0;
+  // adaptive shape (sigops_server_set_adaptive; serve_policy.h); without it
+  // every launch takes the fixed shape above
+  sg::ShapePolicy policy;
   int running_shape = 0;    // shape of the running (or last) launch
   bool switching = false;   // the running launch was asked to close for a new shape
   double launched_at = 0;   // when it started
   uint64_t shape_switches = 0;
   uint64_t items_in = 0;    // items accepted by submit
-  uint64_t rate_items = 0;  // items_in at the last rate sample
-  double rate_t = 0, rate = 0;  // arrival rate, items/s (moving average of 10 ms samples)
   // host state, under mu
   std::mutex mu;
   std::condition_variable cond;
@@ -160,12 +157,7 @@ int grid_for(sigops_server* s, int shape, int* block) {
 }
 
 // caller holds mu: the shape the next launch should have
-int wanted_shape(const sigops_server* s) {
-  if (s->switch_rate <= 0) return s->shape.load(std::memory_order_relaxed);
-  if (s->rate >= s->switch_rate) return s->high_shape;
-  if (s->rate < 0.8 * s->switch_rate) return s->low_shape;
-  return s->running_shape;  // between the two thresholds: keep the shape
-}
+int wanted_shape(const sigops_server* s) { return s->policy.wanted(s->shape.load(std::memory_order_relaxed), s->running_shape); }
 
 // caller holds mu; the kernel is not running
 cudaError_t launch_kernel(sigops_server* s) {
@@ -352,20 +344,9 @@ void worker_loop(sigops_server* s) {
     }
     bool changed = collect_completions(s, lk, finished);
     {  // arrival rate; with an adaptive shape, a running launch of the other shape is asked to close
-      // 10 ms samples, weight 1/4: a step reaches two thirds of its height in
-      // about 40 ms (an overloaded low shape builds a backlog meanwhile), and
-      // the scatter of single samples (about 7% at half load, with requests of
-      // 1..2048 items) is averaged down to about 3%.  The same weight for rises
-      // and falls: a faster rise would follow the samples' upward scatter and
-      // sit above the mean.
       const double t = now_s();
-      if (t - s->rate_t >= 0.01) {
-        const double inst = s->rate_t > 0 ? (double)(s->items_in - s->rate_items) / (t - s->rate_t) : 0.0;
-        s->rate += 0.25 * (inst - s->rate);
-        s->rate_t = t;
-        s->rate_items = s->items_in;
-      }
-      if (s->running && !s->switching && s->switch_rate > 0 && wanted_shape(s) != s->running_shape && t - s->launched_at > 0.02) {
+      s->policy.observe(t, s->items_in);
+      if (s->running && !s->switching && s->policy.switch_rate > 0 && wanted_shape(s) != s->running_shape && t - s->launched_at > 0.02) {
         s->switching = true;
         s->shape_switches++;
         __atomic_store_n(&s->ctl->stop, 1u, __ATOMIC_RELEASE);  // the kernel finishes every published tile, then exits
@@ -412,7 +393,7 @@ int sigops_server_set_variant(sigops_server* s, int variant) {
   if (!s || variant < 0 || variant >= kServeShapes) return SIGOPS_E_INVAL;
   std::lock_guard<std::mutex> g(s->mu);
   s->shape.store(variant, std::memory_order_relaxed);
-  s->switch_rate = 0;
+  s->policy.switch_rate = 0;
   return SIGOPS_OK;
 }
 
@@ -420,9 +401,9 @@ int sigops_server_set_adaptive(sigops_server* s, int low_shape, int high_shape, 
   if (!s || low_shape < 0 || low_shape >= kServeShapes || high_shape < 0 || high_shape >= kServeShapes || !(switch_items_per_s > 0))
     return SIGOPS_E_INVAL;
   std::lock_guard<std::mutex> g(s->mu);
-  s->low_shape = low_shape;
-  s->high_shape = high_shape;
-  s->switch_rate = switch_items_per_s;
+  s->policy.low = low_shape;
+  s->policy.high = high_shape;
+  s->policy.switch_rate = switch_items_per_s;
   return SIGOPS_OK;
 }
 
@@ -431,7 +412,7 @@ int sigops_server_shape_stats(sigops_server* s, int* shape, uint64_t* switches, 
   std::lock_guard<std::mutex> g(s->mu);
   if (shape) *shape = s->running_shape;
   if (switches) *switches = s->shape_switches;
-  if (items_per_s) *items_per_s = s->rate;
+  if (items_per_s) *items_per_s = s->policy.rate;
   return SIGOPS_OK;
 }
 
