@@ -20,11 +20,13 @@
 // no launch, copy or host round trip per request.  The host reads the
 // completion ring and copies each finished request's results to the caller's
 // buffers: the dispatcher thread does, and so does every thread waiting for a
-// request.  The dispatcher also relaunches the kernel when it has closed (idle
-// or its lifetime cap) and work is waiting, and fails the requests in flight
-// if the kernel reports an expired device wait.  It makes no driver call while
-// requests flow (the kernel reports its exit in a mapped word; free device
-// memory is read by a monitor thread).
+// request.  Both also relaunch the kernel when it has closed (idle, its
+// lifetime cap, or a shape switch) and work is waiting, and fail the requests
+// in flight if the kernel reports an expired device wait.  Apart from those
+// launches no driver call is made while requests flow (the kernel reports its
+// exit in a mapped word; free device memory is read by a monitor thread).
+// With an adaptive shape (serve_policy.h) the dispatcher estimates the arrival
+// rate and asks a launch of the other shape to close.
 //
 // Admission is live, at submit time: a request is admitted when the item ring
 // (pinned; its tiles and counters in device memory, within hbm_fraction of
