@@ -376,3 +376,26 @@ extern "C" void hc_shape_policy_run(int low, int high, double switch_rate, int f
   }
 }
 
+// coz_table_iso against coz_table for the secp256k1 point R = (x, y) (32-byte
+// little-endian integers): entry k of the first, at the common Z zc, must be
+// the affine entry k of the second mapped by (x, y) -> (x zc^2, y zc^3).
+// Returns the number of coordinates that differ (0..32).
+extern "C" int hc_coz_iso_mismatches(const uint8_t* x_le, const uint8_t* y_le) {
+  using F = FpK1;
+  constexpr int NR = 16;
+  APoint R;
+  R.x = F::from_int(load_le(x_le));
+  R.y = F::from_int(load_le(y_le));
+  APoint aff[NR], iso[NR];
+  u256 zc;
+  coz_table<F, false, NR>(R, aff);
+  coz_table_iso<F, NR>(R, iso, zc);
+  const u256 z2 = F::sqr(zc), z3 = F::mul(z2, zc);
+  int bad = 0;
+  for (int k = 0; k < NR; ++k) {
+    bad += !u256_eq(F::canon(F::mul(aff[k].x, z2)), F::canon(iso[k].x));
+    bad += !u256_eq(F::canon(F::mul(aff[k].y, z3)), F::canon(iso[k].y));
+  }
+  return bad;
+}
+

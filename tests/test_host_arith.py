@@ -434,3 +434,21 @@ def test_batched_shared_inversions(hc, curve, batch):
             else:
                 exp = bytes.fromhex(v["pubkey"]) if v["pubkey"] else bytes(64)
             assert (out.raw[64 * k:64 * k + 64], st.raw[k]) == (exp, v["status"]), (m, k)
+
+
+def test_coz_table_iso(hc):
+    """The inversion-free secp256k1 table of R multiples: each entry at the
+    chain's last Z equals the affine entry mapped to the isomorphic curve,
+    (x zc^2, y zc^3), for the generator, its negation and random points."""
+    hc.hc_coz_iso_mismatches.argtypes = [ctypes.c_char_p, ctypes.c_char_p]
+    c = o.SECP256K1
+    rng = random.Random(17)
+    points = [c.g, (c.g[0], c.p - c.g[1])]
+    while len(points) < 40:
+        x = rng.randrange(1, c.p)
+        rhs = (x * x * x + c.b) % c.p
+        y = pow(rhs, (c.p + 1) // 4, c.p)
+        if y * y % c.p == rhs:
+            points.append((x, y))
+    for x, y in points:
+        assert hc.hc_coz_iso_mismatches(le(x), le(y)) == 0, (hex(x), hex(y))
